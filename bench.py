@@ -1,0 +1,450 @@
+"""Benchmark of the bandwidth-bound hot path on one GB300 (or N replicas).
+
+Workload (one "step"): the plain bandwidth configuration of the reference's
+hot path -
+    mtv  y = A x,  A 16384 x 16384 row-major, float32   (amt::mtv)
+    dot  a . b,    two float32 vectors of length 2^28   (amt::dot_prod)
+    mtv  the same in float64
+    dot  the same in float64
+entries uniform[-1, 1) from seed 1.  Every input is far larger than the
+129 MB L2, so no L2 flush is needed between iterations.
+
+Reported metric: GB/s of algorithmic traffic (A once plus the vectors,
+i.e. (M*N + M + N) * s for mtv and 2 n s for dot, summed over the four
+calls) per second, whole job.
+
+  value     device-resident inputs, kernels timed with CUDA events on the
+            launching stream;
+  e2e       the same step through the public host-buffer C ABI
+            (gbblas_?mtv_host / gbblas_?dot_host) from pinned host memory,
+            host<->device copies inside the timed region;
+  roofline  the dominant kernel's achieved GB/s against the measured HBM
+            copy bandwidth in MEASURED_PEAKS.json;
+  cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP
+            code, oracle/oracle.c) on the host cores, on a bounded sample.
+
+`--impl reference` times the reference's CPU implementation of the same
+workload instead (the compiled reference where it exists, otherwise the
+oracle port) and prints the same line with "impl": "reference".
+
+Multi-GPU: the path does not shard; `--gpus N` under torchrun runs N
+independent replicas (weak scaling), max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "openmp-blas_gb300"))
+
+M = N = 16384
+NDOT = 1 << 28
+SEED = 1
+
+METRIC = "GEMV GB/s"
+UNIT = "GB/s"
+WORKLOAD = ("bandwidth path: mtv y=A.x (A 16384x16384 row-major) + dot (2^28), float32 and float64, "
+            "U[-1,1) seed 1")
+
+
+def op_bytes():
+    """Algorithmic bytes of each call in one step."""
+    return {
+        "mtv_f32": (M * N + M + N) * 4,
+        "dot_f32": 2 * NDOT * 4,
+        "mtv_f64": (M * N + M + N) * 8,
+        "dot_f64": 2 * NDOT * 8,
+    }
+
+
+def step_bytes() -> int:
+    return sum(op_bytes().values())
+
+
+def config(extra=None):
+    c = {"workload": WORKLOAD, "M": M, "N": N, "dot_n": NDOT, "layout": "row-major",
+         "dtypes": ["f32", "f64"], "bytes_per_step": step_bytes(),
+         "l2": "inputs larger than L2 (no flush needed)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ------------------------------------------------------------------ distributed
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(backend: str):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def reduce_max(value: float, device=None) -> float:
+    """Max of `value` over ranks (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def aggregate(per_rank_units: float, world: int, max_seconds: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    `per_rank_units` in at most `max_seconds`."""
+    return per_rank_units * world / max_seconds
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9], parts[4]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        smax = max(r[1] for r in rows)
+        loaded = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ CPU side
+
+def cpu_step_oracle(bufs) -> None:
+    from oracle import oracle as O
+    O.mtv_raw(1, M, N, bufs["A32"], bufs["x32"], bufs["y32"])
+    O.dot(bufs["a32"], bufs["b32"])
+    O.mtv_raw(1, M, N, bufs["A64"], bufs["x64"], bufs["y64"])
+    O.dot(bufs["a64"], bufs["b64"])
+
+
+def cpu_buffers_from(host):
+    import numpy as np
+    return {k: (v.numpy() if hasattr(v, "numpy") else v) for k, v in host.items()} | {
+        "y32": np.zeros(M, np.float32), "y64": np.zeros(M, np.float64)}
+
+
+def make_cpu_inputs():
+    """Seeded U[-1,1) inputs generated on the CPU (reference arm)."""
+    import numpy as np
+    rng = np.random.default_rng(SEED)
+    out = {}
+    for tag, dt in (("32", np.float32), ("64", np.float64)):
+        out["A" + tag] = rng.uniform(-1, 1, M * N).astype(dt)
+        out["x" + tag] = rng.uniform(-1, 1, N).astype(dt)
+        out["a" + tag] = rng.uniform(-1, 1, NDOT).astype(dt)
+        out["b" + tag] = rng.uniform(-1, 1, NDOT).astype(dt)
+    return out
+
+
+def time_cpu(bufs, min_seconds=10.0, max_steps=50):
+    """Oracle on all host cores: 1 warm-up step, then steps until min_seconds."""
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    cpu_step_oracle(bufs)
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max_steps and (time.perf_counter() - t_start) < min_seconds:
+        t0 = time.perf_counter()
+        cpu_step_oracle(bufs)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def cpu_kind():
+    from oracle import oracle as O
+    return "reference" if O.ref_available() else "port"
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    backend = "nccl"
+    ws, rank, local = dist_init(backend)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import gbblas
+    gbblas.lib()
+    gbblas.call("gbblas_init")
+
+    g = torch.Generator(device=dev).manual_seed(SEED + rank)
+
+    def U(n, dt):
+        return torch.rand(n, generator=g, device=dev, dtype=dt).mul_(2).sub_(1)
+
+    t = {}
+    for tag, dt in (("32", torch.float32), ("64", torch.float64)):
+        t["A" + tag] = U(M * N, dt)
+        t["x" + tag] = U(N, dt)
+        t["y" + tag] = torch.zeros(M, dtype=dt, device=dev)
+        t["a" + tag] = U(NDOT, dt)
+        t["b" + tag] = U(NDOT, dt)
+        t["r" + tag] = torch.zeros(1, dtype=dt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream or None
+    L = gbblas.lib()
+
+    ops = [
+        ("mtv_f32", lambda: gbblas.call("gbblas_smtv", 1, M, N, t["A32"].data_ptr(), t["x32"].data_ptr(),
+                                        t["y32"].data_ptr(), sp)),
+        ("dot_f32", lambda: gbblas.call("gbblas_sdot", NDOT, t["a32"].data_ptr(), t["b32"].data_ptr(),
+                                        t["r32"].data_ptr(), sp)),
+        ("mtv_f64", lambda: gbblas.call("gbblas_dmtv", 1, M, N, t["A64"].data_ptr(), t["x64"].data_ptr(),
+                                        t["y64"].data_ptr(), sp)),
+        ("dot_f64", lambda: gbblas.call("gbblas_ddot", NDOT, t["a64"].data_ptr(), t["b64"].data_ptr(),
+                                        t["r64"].data_ptr(), sp)),
+    ]
+
+    def step():
+        for _, f in ops:
+            f()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, per-op events on the launching stream
+    nops = len(ops)
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nops)]
+          for _ in range(args.steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    launches0 = gbblas.kernel_launches()
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        start.record(stream)
+        for s in range(args.steps):
+            for i, (_, f) in enumerate(ops):
+                ev[s][i][0].record(stream)
+                f()
+                ev[s][i][1].record(stream)
+        end.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    launches = gbblas.kernel_launches() - launches0
+    clocks = clk.summary()
+    total_s = start.elapsed_time(end) / 1e3
+    total_s = reduce_max(total_s, dev)
+    per_op_ms = {name: statistics.mean(ev[s][i][0].elapsed_time(ev[s][i][1]) for s in range(args.steps))
+                 for i, (name, _) in enumerate(ops)}
+
+    sb = step_bytes()
+    value = aggregate(sb * args.steps, ws, total_s) / 1e9
+    ms_per_step = total_s * 1e3 / args.steps
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    dom = max(per_op_ms, key=per_op_ms.get)
+    ob = op_bytes()
+    achieved = ob[dom] / (per_op_ms[dom] / 1e3) / 1e9
+    kernels = {name: {"ms": round(per_op_ms[name], 4), "GB_s": round(ob[name] / (per_op_ms[name] / 1e3) / 1e9, 1),
+                      "frac": round(ob[name] / (per_op_ms[name] / 1e3) / 1e9 / peak, 4)} for name in per_op_ms}
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom)
+
+    # ---- results against device-side checks (cheap sanity, not the parity tests)
+    results = {"dot_f32": t["r32"].item(), "dot_f64": t["r64"].item()}
+
+    # ---- e2e: the same step through the host-buffer C ABI from pinned memory
+    host = {}
+    for k in ("A32", "x32", "a32", "b32", "A64", "x64", "a64", "b64"):
+        host[k] = torch.empty(t[k].shape, dtype=t[k].dtype, pin_memory=True)
+        host[k].copy_(t[k])
+    hy32 = torch.zeros(M, dtype=torch.float32, pin_memory=True)
+    hy64 = torch.zeros(M, dtype=torch.float64, pin_memory=True)
+    hr32 = np.zeros(1, np.float32)
+    hr64 = np.zeros(1, np.float64)
+    for k in host:
+        host[k] = host[k]
+    p = {k: v.data_ptr() for k, v in host.items()}
+
+    def e2e_step():
+        gbblas.call("gbblas_smtv_host", 1, M, N, p["A32"], p["x32"], hy32.data_ptr())
+        gbblas.call("gbblas_sdot_host", NDOT, p["a32"], p["b32"], hr32.ctypes.data)
+        gbblas.call("gbblas_dmtv_host", 1, M, N, p["A64"], p["x64"], hy64.data_ptr())
+        gbblas.call("gbblas_ddot_host", NDOT, p["a64"], p["b64"], hr64.ctypes.data)
+
+    e2e_steps = max(1, min(args.steps, 5))
+    e2e_step()  # warm-up (allocates the staging arena)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = reduce_max(time.perf_counter() - t0, dev)
+    barrier()
+    h2d = sum(host[k].numel() * host[k].element_size() for k in host)
+    d2h = M * 4 + 4 + M * 8 + 8
+    e2e = {"value": round(aggregate(sb * e2e_steps, ws, e2e_s) / 1e9, 2), "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+           "api": "gbblas_smtv_host/gbblas_sdot_host/gbblas_dmtv_host/gbblas_ddot_host (pinned host buffers)"}
+
+    # ---- CPU baseline (rank 0 only): the oracle on the host cores
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        bufs = cpu_buffers_from({k: host[k] for k in ("A32", "x32", "a32", "b32", "A64", "x64", "a64", "b64")})
+        times = time_cpu(bufs, min_seconds=args.cpu_seconds)
+        cpu = {"value": round(sb / statistics.mean(times) / 1e9, 3), "unit": UNIT,
+               "cores": os.cpu_count(), "kind": cpu_kind(),
+               "sample": f"{len(times)} full steps (all four calls at full size) after 1 warm-up, "
+                         f"mean {statistics.mean(times) * 1e3:.1f} ms/step, OpenMP on all host cores"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+            "kernels": kernels,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "results": results,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return  # one host, one CPU baseline: other ranks exit without work
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    kind = cpu_kind()
+    bufs = make_cpu_inputs()
+    bufs["y32"] = __import__("numpy").zeros(M, "float32")
+    bufs["y64"] = __import__("numpy").zeros(M, "float64")
+    O.set_threads(os.cpu_count() or 1)
+    for _ in range(args.warmup):
+        cpu_step_oracle(bufs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_step_oracle(bufs)
+    dt = time.perf_counter() - t0
+    value = step_bytes() * args.steps / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic", "config": config({"parallelism": "host CPU (OpenMP)"}),
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
+                         "sample": f"{args.steps} full steps after {args.warmup} warm-up, all host cores; "
+                                   + ("reference headers compiled unmodified" if kind == "reference" else
+                                      "oracle/oracle.c restatement of the reference's OpenMP code "
+                                      "(the reference sources are not on this machine)")},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gbblas":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * gbblas.h - C ABI of the GB300 (sm_103a) implementation of OpenMP-BLAS's
+ * dense hot path: mtm (GEMM), mtv / vtm (GEMV) and dot.
+ *
+ * The C++ drop-in headers include/mtm.hpp, include/mtv.hpp and
+ * include/dot.hpp keep the reference's amt:: templates and call the
+ * *_host entry points below; any other language binds these functions
+ * directly (ctypes, cgo, JNI...).  No C++ or CUDA type appears in a
+ * signature: sizes are int64_t, strides are in elements, streams are
+ * `void*` holding a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Conventions shared by every entry point
+ *   - Status codes, never exceptions.  GBBLAS_STATUS_SUCCESS is 0.
+ *   - Layouts follow uBLAS: GBBLAS_FIRST_ORDER is column-major (strides
+ *     {1, rows}), GBBLAS_LAST_ORDER is row-major (strides {cols, 1}).
+ *   - Plain entry points take DEVICE pointers and are asynchronous on the
+ *     given stream.  *_host entry points take HOST pointers, stage through a
+ *     library-owned device pool, and return after the result is back in host
+ *     memory (the reference's "call the lambda and the result is there").
+ *   - Shape rules are the reference's: matrices have both extents > 1, the
+ *     inner dimensions must agree (reference include/mtm.hpp:234-250,
+ *     include/mtv.hpp:126-144 and 189-208, include/dot.hpp:196-214).  A
+ *     violation returns GBBLAS_STATUS_SHAPE_MISMATCH (the reference throws
+ *     std::runtime_error; the drop-in headers turn the status back into that
+ *     exception).
+ *   - Results are deterministic: reductions use a fixed order, no atomics.
+ */
+#ifndef GBBLAS_H
+#define GBBLAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBBLAS_VERSION_MAJOR 0
+#define GBBLAS_VERSION_MINOR 1
+
+typedef enum gbblas_status {
+  GBBLAS_STATUS_SUCCESS = 0,
+  GBBLAS_STATUS_INVALID_VALUE = 1,   /* null pointer, negative size, bad enum */
+  GBBLAS_STATUS_SHAPE_MISMATCH = 2,  /* operands are not matrices/vectors or dims disagree */
+  GBBLAS_STATUS_ALLOC_FAILED = 3,    /* device or pinned-host allocation failed */
+  GBBLAS_STATUS_CUDA_ERROR = 4,      /* a CUDA runtime call or launch failed */
+  GBBLAS_STATUS_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+  GBBLAS_STATUS_NOT_SUPPORTED = 6,   /* combination not provided (e.g. FP8 with double) */
+  GBBLAS_STATUS_NO_DEVICE = 7        /* no sm_103 device visible */
+} gbblas_status;
+
+typedef enum gbblas_layout {
+  GBBLAS_FIRST_ORDER = 0, /* column-major, uBLAS layout::first_order */
+  GBBLAS_LAST_ORDER = 1   /* row-major,    uBLAS layout::last_order  */
+} gbblas_layout;
+
+/* Arithmetic used by single-precision GEMM. */
+typedef enum gbblas_accuracy {
+  GBBLAS_ACCURACY_FP32 = 0,   /* FP32 FMA on the CUDA cores (the reference's arithmetic) */
+  GBBLAS_ACCURACY_BF16X3 = 1, /* FP32-accurate: a = hi + lo in BF16, hi*hi + hi*lo + lo*hi
+                                 on tcgen05 tensor cores, FP32 accumulation in TMEM */
+  GBBLAS_ACCURACY_FP8 = 2,    /* low accuracy: E4M3 operands with one scale per 128
+                                 elements along K, FP32 accumulation */
+  GBBLAS_ACCURACY_AUTO = 3    /* BF16X3 where the shape suits the tensor-core tiles,
+                                 FP32 otherwise */
+} gbblas_accuracy;
+
+/* ---------------------------------------------------------------- library */
+
+/* Human-readable name of a status code (static storage). */
+const char* gbblas_status_string(gbblas_status s);
+
+/* Message of the last failure on the calling host thread ("" if none). */
+const char* gbblas_last_error(void);
+
+/* Version string, e.g. "gbblas 0.1 (sm_103a)". */
+const char* gbblas_version(void);
+
+/* Make the library ready on the current device: checks it is sm_103 and
+ * creates the device pool.  Optional; every entry point does it lazily. */
+gbblas_status gbblas_init(void);
+
+/* Number of kernels this library has launched in this process (all
+ * devices).  Benchmarks read it before and after a timed region. */
+uint64_t gbblas_kernel_launches(void);
+
+/* Release cached device and pinned-host memory held by the library for the
+ * current device.  Safe to call at any time no call is in flight. */
+gbblas_status gbblas_release_cache(void);
+
+/* ------------------------------------------------------------------ mtm */
+
+/* C += A * B (single precision).                      replaces amt::mtm,
+ * reference include/mtm.hpp:208-267 (lambda body: mtm_helper, 116-206).
+ * A is M x K with element strides (rsa, csa), B is K x N with (rsb, csb),
+ * C is M x N with (rsc, csc): element (i, j) of C is C[i*rsc + j*csc].
+ * Like the reference, C is ACCUMULATED into (zero it first for C = A*B).
+ * Any strides are accepted; one unit stride per operand takes the fast
+ * path.  `accuracy` picks the arithmetic (GBBLAS_ACCURACY_*). */
+gbblas_status gbblas_sgemm(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa,
+                           const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc, int64_t csc,
+                           gbblas_accuracy accuracy, void* stream);
+
+/* C += A * B (double precision, FP64 arithmetic).      replaces amt::mtm
+ * for double tensors, reference include/mtm.hpp:208-267 with
+ * include/simd_loop.hpp:132-158. */
+gbblas_status gbblas_dgemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                           const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
+                           void* stream);
+
+/* ------------------------------------------------------------------ mtv */
+
+/* y = A * x for M x N dense A of layout `la`, x of length N, y of length M.
+ *                                                   replaces amt::mtv,
+ * reference include/mtv.hpp:100-162.  As in the reference, a column-major A
+ * ACCUMULATES into y (include/mtv.hpp:15-70, simd_loop.hpp:62,74) and a
+ * row-major A OVERWRITES y (include/mtv.hpp:72-98).  A's strides are taken
+ * from the layout, not from the caller (reference line 154-156). */
+gbblas_status gbblas_smtv(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y,
+                          void* stream);
+gbblas_status gbblas_dmtv(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* x,
+                          double* y, void* stream);
+
+/* y = v^T * A for M x N dense A of layout `la`, v of length M, y of length N.
+ *                                                   replaces amt::vtm,
+ * reference include/mtv.hpp:164-236.  The reference intends this product but
+ * builds A^T's strides from the wrong extent (lines 224-227), so it is right
+ * only for square column-major A; this function computes y = v^T A for
+ * every shape.  Overwrite/accumulate follow the reference's delegation: a
+ * column-major A overwrites y, a row-major A accumulates into y. */
+gbblas_status gbblas_svtm(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* v, float* y,
+                          void* stream);
+gbblas_status gbblas_dvtm(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* v,
+                          double* y, void* stream);
+
+/* General form behind mtv/vtm: y = op(A) * x (+ y if accumulate != 0),
+ * op(A) = A if transpose == 0 else A^T, A M x N dense of layout la. */
+gbblas_status gbblas_sgemv(gbblas_layout la, int transpose, int64_t M, int64_t N, const float* A,
+                           const float* x, int accumulate, float* y, void* stream);
+gbblas_status gbblas_dgemv(gbblas_layout la, int transpose, int64_t M, int64_t N, const double* A,
+                           const double* x, int accumulate, double* y, void* stream);
+
+/* ------------------------------------------------------------------ dot */
+
+/* *result = sum_i a[i] * b[i] over n elements; result is a DEVICE pointer.
+ *                                             replaces amt::dot_prod,
+ * reference include/dot.hpp:176-224 (helper 143-174).  Single precision
+ * keeps Kahan-compensated FP32 partials and combines them in FP64, so it is
+ * at least as accurate as the reference's blocked OpenMP reduction.
+ * n == 0 writes 0. */
+gbblas_status gbblas_sdot(int64_t n, const float* a, const float* b, float* result, void* stream);
+gbblas_status gbblas_ddot(int64_t n, const double* a, const double* b, double* result, void* stream);
+
+/* amt::dot_prod_tuning_param (reference include/dot.hpp:92-141): the CPU
+ * block sizes b1, b2, b3 have no meaning on the GPU; they are validated
+ * (non-zero) and the call computes the same dot as gbblas_?dot. */
+gbblas_status gbblas_sdot_tuning(int64_t n, const float* a, const float* b, int64_t b1, int64_t b2,
+                                 int64_t b3, float* result, void* stream);
+gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, int64_t b1, int64_t b2,
+                                 int64_t b3, double* result, void* stream);
+
+/* ------------------------------------------------ host-buffer entry points
+ * Same operations on HOST pointers: inputs are copied to the device, the
+ * kernel runs, outputs come back, and the call returns when host memory
+ * holds the result.  Page-locked host buffers copy at full link speed;
+ * pageable ones are staged.  These are what the amt:: drop-in headers call. */
+gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa,
+                                const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc, int64_t csc,
+                                gbblas_accuracy accuracy);
+gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                                const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
+                                int64_t csc);
+gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x,
+                               float* y);
+gbblas_status gbblas_dmtv_host(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* x,
+                               double* y);
+gbblas_status gbblas_svtm_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* v,
+                               float* y);
+gbblas_status gbblas_dvtm_host(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* v,
+                               double* y);
+gbblas_status gbblas_sdot_host(int64_t n, const float* a, const float* b, float* result);
+gbblas_status gbblas_ddot_host(int64_t n, const double* a, const double* b, double* result);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* GBBLAS_H */

@@ -1,0 +1,433 @@
+// capi.cu - the extern "C" boundary (include/gbblas.h) and the host-side
+// runtime behind it: per-device context, per-stream scratch, host staging,
+// argument checking and status/error reporting.
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+namespace gbblas {
+
+// ------------------------------------------------------------------ errors
+namespace {
+thread_local char g_err[512] = {0};
+}
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+const char* last_error() { return g_err; }
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ----------------------------------------------------------------- context
+namespace {
+std::mutex g_ctx_mu;
+DeviceCtx* g_ctx[64] = {nullptr};
+}  // namespace
+
+gbblas_status get_ctx(DeviceCtx** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error("no CUDA device: %s", cudaGetErrorString(e));
+    return GBBLAS_STATUS_NO_DEVICE;
+  }
+  DeviceCtx* c = g_ctx[dev];
+  if (c) {
+    *out = c;
+    return GBBLAS_STATUS_SUCCESS;
+  }
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  if (!g_ctx[dev]) {
+    cudaDeviceProp p;
+    GB_CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    if (!(p.major == 10 && p.minor == 3)) {
+      set_error("device %d is sm_%d%d; this library is built for sm_103a (GB300)", dev, p.major, p.minor);
+      return GBBLAS_STATUS_NO_DEVICE;
+    }
+    DeviceCtx* n = new DeviceCtx();
+    n->device = dev;
+    n->num_sms = p.multiProcessorCount;
+    n->cc_major = p.major;
+    n->cc_minor = p.minor;
+    n->smem_optin = p.sharedMemPerBlockOptin;
+    g_ctx[dev] = n;
+  }
+  *out = g_ctx[dev];
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void** out) {
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceCtx::Scratch& s = c->scratch[stream];
+  if (s.bytes < bytes) {
+    size_t want = bytes < (1u << 20) ? (1u << 20) : bytes + bytes / 4;
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, want, stream);
+    if (e != cudaSuccess) {
+      set_error("scratch allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
+      return GBBLAS_STATUS_ALLOC_FAILED;
+    }
+    GB_CUDA_TRY(cudaMemsetAsync(p, 0, kScratchZeroBytes, stream));
+    if (s.ptr) GB_CUDA_TRY(cudaFreeAsync(s.ptr, stream));
+    s.ptr = p;
+    s.bytes = want;
+  }
+  *out = s.ptr;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out) {
+  if (!c->host_stream) GB_CUDA_TRY(cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking));
+  if (c->stage_bytes < bytes) {
+    if (c->stage) {
+      GB_CUDA_TRY(cudaStreamSynchronize(c->host_stream));
+      GB_CUDA_TRY(cudaFree(c->stage));
+      c->stage = nullptr;
+      c->stage_bytes = 0;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      set_error("staging allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+      return GBBLAS_STATUS_ALLOC_FAILED;
+    }
+    c->stage = p;
+    c->stage_bytes = bytes;
+  }
+  *out = c->stage;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+namespace {
+
+// ------------------------------------------------------- argument checks
+gbblas_status bad(gbblas_status s, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  char buf[512];
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  set_error("%s", buf);
+  return s;
+}
+
+bool layout_ok(gbblas_layout l) { return l == GBBLAS_FIRST_ORDER || l == GBBLAS_LAST_ORDER; }
+
+// Elements spanned by a rows x cols operand with strides (rs, cs).
+int64_t span(int64_t rows, int64_t cols, int64_t rs, int64_t cs) {
+  if (rows <= 0 || cols <= 0) return 0;
+  return (rows - 1) * rs + (cols - 1) * cs + 1;
+}
+
+template <typename T>
+gbblas_status check_gemm(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
+                         int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc) {
+  if (M < 0 || N < 0 || K < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: negative size");
+  if (rsa < 0 || csa < 0 || rsb < 0 || csb < 0 || rsc < 0 || csc < 0)
+    return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: strides must be non-negative");
+  if (M == 0 || N == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!C) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: C is null");
+  if (K > 0 && (!A || !B)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: A or B is null");
+  if ((M > 1 && rsc == 0) || (N > 1 && csc == 0))
+    return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: C strides must be non-zero (outputs would alias)");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status check_mv(gbblas_layout la, int64_t M, int64_t N, const T* A, const T* x, T* y) {
+  if (!layout_ok(la)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemv: layout must be 0 or 1");
+  if (M < 0 || N < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemv: negative size");
+  if ((M > 0 && N > 0) && (!A || !x || !y)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemv: null pointer");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+// y = op(A) x (+ y).  A is M x N dense in layout la.
+template <typename T>
+gbblas_status gemv_any(DeviceCtx* c, gbblas_layout la, bool transpose, int64_t M, int64_t N, const T* A,
+                       const T* x, bool accumulate, T* y, cudaStream_t s) {
+  const int64_t out_len = transpose ? N : M;
+  const int64_t red_len = transpose ? M : N;
+  if (out_len == 0) return GBBLAS_STATUS_SUCCESS;
+  if (red_len == 0) {
+    if (!accumulate) GB_CUDA_TRY(cudaMemsetAsync(y, 0, sizeof(T) * out_len, s));
+    return GBBLAS_STATUS_SUCCESS;
+  }
+  // Row-major A: rows contiguous (lda = N).  Column-major: columns contiguous (lda = M).
+  const bool rows_contig = (la == GBBLAS_LAST_ORDER) != transpose;
+  const int64_t lda = la == GBBLAS_LAST_ORDER ? N : M;
+  if (rows_contig) return launch_gemv_rows<T>(c, out_len, red_len, A, lda, x, y, accumulate, s);
+  return launch_gemv_cols<T>(c, out_len, red_len, A, lda, x, y, accumulate, s);
+}
+
+template <typename T>
+gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa,
+                       const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc,
+                       cudaStream_t s) {
+  if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
+  (void)acc;
+  return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+}
+
+// ----------------------------------------------------------- host staging
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct HostGuard {
+  DeviceCtx* c;
+  std::unique_lock<std::mutex> lk;
+  explicit HostGuard(DeviceCtx* c_) : c(c_), lk(c_->host_mu) {}
+};
+
+gbblas_status h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) GB_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+gbblas_status d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes) GB_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status gemm_host(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
+                        int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc) {
+  GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
+  if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t na = span(M, K, rsa, csa), nb = span(K, N, rsb, csb), nc = span(M, N, rsc, csc);
+  void* base;
+  GB_TRY(get_stage(c, round256(na * sizeof(T)) + round256(nb * sizeof(T)) + round256(nc * sizeof(T)), &base));
+  T* dA = static_cast<T*>(base);
+  T* dB = reinterpret_cast<T*>(static_cast<char*>(base) + round256(na * sizeof(T)));
+  T* dC = reinterpret_cast<T*>(reinterpret_cast<char*>(dB) + round256(nb * sizeof(T)));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(dA, A, na * sizeof(T), s));
+  GB_TRY(h2d(dB, B, nb * sizeof(T), s));
+  GB_TRY(h2d(dC, C, nc * sizeof(T), s));
+  GB_TRY(gemm_any<T>(c, M, N, K, dA, rsa, csa, dB, rsb, csb, dC, rsc, csc, acc, s));
+  GB_TRY(d2h(C, dC, nc * sizeof(T), s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status gemv_host(gbblas_layout la, bool transpose, int64_t M, int64_t N, const T* A, const T* x,
+                        bool accumulate, T* y) {
+  GB_TRY(check_mv<T>(la, M, N, A, x, y));
+  const int64_t out_len = transpose ? N : M, in_len = transpose ? M : N;
+  if (out_len == 0) return GBBLAS_STATUS_SUCCESS;
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t na = (size_t)(M * N), nx = (size_t)in_len, ny = (size_t)out_len;
+  void* base;
+  GB_TRY(get_stage(c, round256(na * sizeof(T)) + round256(nx * sizeof(T)) + round256(ny * sizeof(T)), &base));
+  T* dA = static_cast<T*>(base);
+  T* dx = reinterpret_cast<T*>(static_cast<char*>(base) + round256(na * sizeof(T)));
+  T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(dx) + round256(nx * sizeof(T)));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(dA, A, na * sizeof(T), s));
+  GB_TRY(h2d(dx, x, nx * sizeof(T), s));
+  if (accumulate) GB_TRY(h2d(dy, y, ny * sizeof(T), s));
+  GB_TRY(gemv_any<T>(c, la, transpose, M, N, dA, dx, accumulate, dy, s));
+  GB_TRY(d2h(y, dy, ny * sizeof(T), s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status dot_host(int64_t n, const T* a, const T* b, T* result) {
+  if (n < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot: negative size");
+  if (!result || (n > 0 && (!a || !b))) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot: null pointer");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t bytes = (size_t)n * sizeof(T);
+  void* base;
+  GB_TRY(get_stage(c, 2 * round256(bytes) + 256, &base));
+  T* da = static_cast<T*>(base);
+  T* db = reinterpret_cast<T*>(static_cast<char*>(base) + round256(bytes));
+  T* dr = reinterpret_cast<T*>(static_cast<char*>(base) + 2 * round256(bytes));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(da, a, bytes, s));
+  GB_TRY(h2d(db, b, bytes, s));
+  GB_TRY(launch_dot<T>(c, n, da, db, dr, s));
+  GB_TRY(d2h(result, dr, sizeof(T), s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status dot_dev(int64_t n, const T* a, const T* b, T* result, void* stream) {
+  if (n < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot: negative size");
+  if (!result || (n > 0 && (!a || !b))) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot: null pointer");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return launch_dot<T>(c, n, a, b, result, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status gemv_dev(gbblas_layout la, bool transpose, int64_t M, int64_t N, const T* A, const T* x,
+                       bool accumulate, T* y, void* stream) {
+  GB_TRY(check_mv<T>(la, M, N, A, x, y));
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return gemv_any<T>(c, la, transpose, M, N, A, x, accumulate, y, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
+                       int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc, void* stream) {
+  GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
+  if ((int)acc < 0 || (int)acc > 3) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return gemm_any<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, acc, as_stream(stream));
+}
+
+}  // namespace
+}  // namespace gbblas
+
+using namespace gbblas;
+
+extern "C" {
+
+const char* gbblas_status_string(gbblas_status s) {
+  switch (s) {
+    case GBBLAS_STATUS_SUCCESS: return "GBBLAS_STATUS_SUCCESS";
+    case GBBLAS_STATUS_INVALID_VALUE: return "GBBLAS_STATUS_INVALID_VALUE";
+    case GBBLAS_STATUS_SHAPE_MISMATCH: return "GBBLAS_STATUS_SHAPE_MISMATCH";
+    case GBBLAS_STATUS_ALLOC_FAILED: return "GBBLAS_STATUS_ALLOC_FAILED";
+    case GBBLAS_STATUS_CUDA_ERROR: return "GBBLAS_STATUS_CUDA_ERROR";
+    case GBBLAS_STATUS_TIMEOUT: return "GBBLAS_STATUS_TIMEOUT";
+    case GBBLAS_STATUS_NOT_SUPPORTED: return "GBBLAS_STATUS_NOT_SUPPORTED";
+    case GBBLAS_STATUS_NO_DEVICE: return "GBBLAS_STATUS_NO_DEVICE";
+  }
+  return "GBBLAS_STATUS_UNKNOWN";
+}
+
+const char* gbblas_last_error(void) { return gbblas::last_error(); }
+
+const char* gbblas_version(void) { return "gbblas 0.1 (sm_103a)"; }
+
+uint64_t gbblas_kernel_launches(void) { return gbblas::g_launches.load(); }
+
+gbblas_status gbblas_init(void) {
+  DeviceCtx* c;
+  return get_ctx(&c);
+}
+
+gbblas_status gbblas_release_cache(void) {
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (auto& kv : c->scratch) {
+      if (kv.second.ptr) GB_CUDA_TRY(cudaFreeAsync(kv.second.ptr, kv.first));
+    }
+    c->scratch.clear();
+  }
+  std::lock_guard<std::mutex> lk(c->host_mu);
+  if (c->stage) {
+    GB_CUDA_TRY(cudaStreamSynchronize(c->host_stream));
+    GB_CUDA_TRY(cudaFree(c->stage));
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_sgemm(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa, const float* B,
+                           int64_t rsb, int64_t csb, float* C, int64_t rsc, int64_t csc, gbblas_accuracy accuracy,
+                           void* stream) {
+  return gemm_dev<float>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, accuracy, stream);
+}
+
+gbblas_status gbblas_dgemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                           const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
+                           void* stream) {
+  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP32, stream);
+}
+
+gbblas_status gbblas_smtv(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y,
+                          void* stream) {
+  return gemv_dev<float>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y, stream);
+}
+gbblas_status gbblas_dmtv(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* x, double* y,
+                          void* stream) {
+  return gemv_dev<double>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y, stream);
+}
+gbblas_status gbblas_svtm(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* v, float* y,
+                          void* stream) {
+  return gemv_dev<float>(la, true, M, N, A, v, la == GBBLAS_LAST_ORDER, y, stream);
+}
+gbblas_status gbblas_dvtm(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* v, double* y,
+                          void* stream) {
+  return gemv_dev<double>(la, true, M, N, A, v, la == GBBLAS_LAST_ORDER, y, stream);
+}
+gbblas_status gbblas_sgemv(gbblas_layout la, int transpose, int64_t M, int64_t N, const float* A, const float* x,
+                           int accumulate, float* y, void* stream) {
+  return gemv_dev<float>(la, transpose != 0, M, N, A, x, accumulate != 0, y, stream);
+}
+gbblas_status gbblas_dgemv(gbblas_layout la, int transpose, int64_t M, int64_t N, const double* A,
+                           const double* x, int accumulate, double* y, void* stream) {
+  return gemv_dev<double>(la, transpose != 0, M, N, A, x, accumulate != 0, y, stream);
+}
+
+gbblas_status gbblas_sdot(int64_t n, const float* a, const float* b, float* result, void* stream) {
+  return dot_dev<float>(n, a, b, result, stream);
+}
+gbblas_status gbblas_ddot(int64_t n, const double* a, const double* b, double* result, void* stream) {
+  return dot_dev<double>(n, a, b, result, stream);
+}
+gbblas_status gbblas_sdot_tuning(int64_t n, const float* a, const float* b, int64_t b1, int64_t b2, int64_t b3,
+                                 float* result, void* stream) {
+  if (b1 <= 0 || b2 <= 0 || b3 <= 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot_tuning: block sizes must be > 0");
+  return dot_dev<float>(n, a, b, result, stream);
+}
+gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, int64_t b1, int64_t b2, int64_t b3,
+                                 double* result, void* stream) {
+  if (b1 <= 0 || b2 <= 0 || b3 <= 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot_tuning: block sizes must be > 0");
+  return dot_dev<double>(n, a, b, result, stream);
+}
+
+gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa,
+                                const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc, int64_t csc,
+                                gbblas_accuracy accuracy) {
+  return gemm_host<float>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, accuracy);
+}
+gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                                const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc) {
+  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP32);
+}
+gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y) {
+  return gemv_host<float>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y);
+}
+gbblas_status gbblas_dmtv_host(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* x, double* y) {
+  return gemv_host<double>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y);
+}
+gbblas_status gbblas_svtm_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* v, float* y) {
+  return gemv_host<float>(la, true, M, N, A, v, la == GBBLAS_LAST_ORDER, y);
+}
+gbblas_status gbblas_dvtm_host(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* v, double* y) {
+  return gemv_host<double>(la, true, M, N, A, v, la == GBBLAS_LAST_ORDER, y);
+}
+gbblas_status gbblas_sdot_host(int64_t n, const float* a, const float* b, float* result) {
+  return dot_host<float>(n, a, b, result);
+}
+gbblas_status gbblas_ddot_host(int64_t n, const double* a, const double* b, double* result) {
+  return dot_host<double>(n, a, b, result);
+}
+
+}  // extern "C"

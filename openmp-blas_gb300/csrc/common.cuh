@@ -1,0 +1,171 @@
+// common.cuh - shared host/device plumbing for the gbblas CUDA library.
+//
+// Host side: per-device context (SM count, per-stream scratch for the
+// deterministic two-stage reductions, the staging area used by the *_host
+// entry points), error bookkeeping and status helpers.
+// Device side: cache-hinted vector loads and warp/block reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <unordered_map>
+
+#include "../../include/gbblas.h"
+
+namespace gbblas {
+
+// ---------------------------------------------------------------- errors
+
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define GB_CUDA_TRY(call)                                                                   \
+  do {                                                                                      \
+    cudaError_t _e = (call);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      ::gbblas::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, \
+                          __LINE__);                                                        \
+      return GBBLAS_STATUS_CUDA_ERROR;                                                      \
+    }                                                                                       \
+  } while (0)
+
+#define GB_TRY(expr)                                \
+  do {                                              \
+    gbblas_status _s = (expr);                      \
+    if (_s != GBBLAS_STATUS_SUCCESS) return _s;     \
+  } while (0)
+
+// Count of kernels launched by the library (gbblas_kernel_launches()).
+void count_launch();
+
+// Check the launch that was just issued (and count it).
+inline gbblas_status check_launch(const char* what) {
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("launch of %s failed: %s", what, cudaGetErrorString(e));
+    return GBBLAS_STATUS_CUDA_ERROR;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+// --------------------------------------------------------------- context
+
+// One per device.  Scratch buffers are per stream so concurrent calls on
+// different streams never share one; growth is stream-ordered
+// (cudaMallocAsync / cudaFreeAsync on the owning stream).
+struct DeviceCtx {
+  int device = -1;
+  int num_sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+  std::mutex mu;
+  struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+  };
+  std::unordered_map<cudaStream_t, Scratch> scratch;
+  // *_host staging: one stream, one device arena, guarded by host_mu.
+  std::mutex host_mu;
+  cudaStream_t host_stream = nullptr;
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+};
+
+// Context of the current device, created on first use.  Fails with
+// GBBLAS_STATUS_NO_DEVICE when no device is visible or it is not sm_103.
+gbblas_status get_ctx(DeviceCtx** out);
+
+// Scratch of at least `bytes` for `stream`.  The first kScratchZeroBytes of a
+// fresh buffer are zeroed on the stream (reduction kernels keep their
+// completion counters there and return them to zero themselves).
+constexpr size_t kScratchZeroBytes = 256;
+gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void** out);
+
+// Staging arena of at least `bytes` for the *_host paths (caller holds host_mu).
+gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// ------------------------------------------------------ kernel launchers
+// (defined in the kernel translation units; all asynchronous on `stream`)
+
+// y[r] (+)= sum_c A[r*lda + c] * x[c] for r < rows, c < cols
+// (every output is a dot of a contiguous row with x).
+template <typename T>
+gbblas_status launch_gemv_rows(DeviceCtx* c, int64_t rows, int64_t cols, const T* A, int64_t lda,
+                               const T* x, T* y, bool accumulate, cudaStream_t stream);
+
+// y[r] (+)= sum_c A[r + c*lda] * x[c] (columns contiguous: axpy form).
+template <typename T>
+gbblas_status launch_gemv_cols(DeviceCtx* c, int64_t rows, int64_t cols, const T* A, int64_t lda,
+                               const T* x, T* y, bool accumulate, cudaStream_t stream);
+
+template <typename T>
+gbblas_status launch_dot(DeviceCtx* c, int64_t n, const T* a, const T* b, T* result, cudaStream_t stream);
+
+template <typename T>
+gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
+                              int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
+                              int64_t csc, cudaStream_t stream);
+
+}  // namespace gbblas
+
+// ----------------------------------------------------------- device helpers
+#ifdef __CUDACC__
+namespace gbblas::dev {
+
+// Streaming loads: read-only path, no L1 allocation (data is used once).
+__device__ __forceinline__ float4 ld_stream(const float4* p) {
+  float4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ double2 ld_stream(const double2* p) {
+  double2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float ld_stream(const float* p) {
+  float r;
+  asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ double ld_stream(const double* p) {
+  double r;
+  asm volatile("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block in a fixed order (deterministic).  `sh` holds >= 32 T.
+// Every thread gets the total.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  T t = lane < nwarps ? sh[lane] : T(0);
+  t = warp_sum(t);
+  return t;
+}
+
+}  // namespace gbblas::dev
+#endif

@@ -1,0 +1,206 @@
+"""Python binding of libgbblas.so (the C ABI in include/gbblas.h).
+
+This is a thin ctypes layer used by the tests, the benchmark and anyone who
+wants the GB300 kernels from Python.  Device operands are torch CUDA tensors
+(torch only supplies memory and streams); host operands are numpy arrays and
+go through the library's *_host entry points.  There is no CPU fallback: if
+the library or a GB300 is missing, calls raise.
+
+Layouts: FIRST_ORDER (0) = column-major, LAST_ORDER (1) = row-major.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _build
+
+FIRST_ORDER = 0
+LAST_ORDER = 1
+
+ACCURACY_FP32 = 0
+ACCURACY_BF16X3 = 1
+ACCURACY_FP8 = 2
+ACCURACY_AUTO = 3
+
+STATUS = {
+    0: "SUCCESS", 1: "INVALID_VALUE", 2: "SHAPE_MISMATCH", 3: "ALLOC_FAILED",
+    4: "CUDA_ERROR", 5: "TIMEOUT", 6: "NOT_SUPPORTED", 7: "NO_DEVICE",
+}
+
+LIB_PATH = _build.LIB
+
+#: every C-ABI symbol include/gbblas.h declares, with (restype, argtypes)
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_vp = ctypes.c_void_p
+SIGNATURES = {
+    "gbblas_status_string": (ctypes.c_char_p, [_int]),
+    "gbblas_last_error": (ctypes.c_char_p, []),
+    "gbblas_version": (ctypes.c_char_p, []),
+    "gbblas_init": (_int, []),
+    "gbblas_kernel_launches": (ctypes.c_uint64, []),
+    "gbblas_release_cache": (_int, []),
+    "gbblas_sgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _vp]),
+    "gbblas_dgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp]),
+    "gbblas_smtv": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_dmtv": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_svtm": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_dvtm": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_sgemv": (_int, [_int, _int, _i64, _i64, _vp, _vp, _int, _vp, _vp]),
+    "gbblas_dgemv": (_int, [_int, _int, _i64, _i64, _vp, _vp, _int, _vp, _vp]),
+    "gbblas_sdot": (_int, [_i64, _vp, _vp, _vp, _vp]),
+    "gbblas_ddot": (_int, [_i64, _vp, _vp, _vp, _vp]),
+    "gbblas_sdot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "gbblas_ddot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
+    "gbblas_dgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
+    "gbblas_smtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_dmtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_svtm_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_dvtm_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_sdot_host": (_int, [_i64, _vp, _vp, _vp]),
+    "gbblas_ddot_host": (_int, [_i64, _vp, _vp, _vp]),
+}
+
+_lib = None
+
+
+class GbblasError(RuntimeError):
+    def __init__(self, fn: str, status: int, msg: str):
+        super().__init__(f"{fn} -> {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def kernel_launches() -> int:
+    """Kernels launched by libgbblas.so so far in this process."""
+    return int(lib().gbblas_kernel_launches())
+
+
+def build(force: bool = False) -> str:
+    return _build.build(force=force)
+
+
+def lib(auto_build: bool = True):
+    """Load libgbblas.so (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        if auto_build:
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with gbblas.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(fn: str, status: int) -> None:
+    if status != 0:
+        raise GbblasError(fn, status, lib().gbblas_last_error().decode())
+
+
+def call(name: str, *args) -> None:
+    """Call a C-ABI function by name and raise GbblasError on a non-zero status."""
+    _check(name, getattr(lib(), name)(*args))
+
+
+def status_of(name: str, *args) -> int:
+    """Call a C-ABI function and return its raw status."""
+    return getattr(lib(), name)(*args)
+
+
+# ---------------------------------------------------------------- torch helpers
+
+def _stream_ptr(stream) -> int | None:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream or None
+
+
+def _pfx(t) -> str:
+    import torch
+    if t.dtype == torch.float32:
+        return "s"
+    if t.dtype == torch.float64:
+        return "d"
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def _dev(t) -> int:
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return t.data_ptr()
+
+
+def gemm(A, B, C, accuracy: int = ACCURACY_FP32, stream=None):
+    """C += A @ B on device tensors of any strides (2-D torch tensors)."""
+    M, K = A.shape
+    N = B.shape[1]
+    p = _pfx(A)
+    args = [M, N, K, _dev(A), A.stride(0), A.stride(1), _dev(B), B.stride(0), B.stride(1),
+            _dev(C), C.stride(0), C.stride(1)]
+    if p == "s":
+        args.append(accuracy)
+    call(f"gbblas_{p}gemm", *args, _stream_ptr(stream))
+    return C
+
+
+def mtv(layout: int, M: int, N: int, A, x, y, stream=None):
+    """amt::mtv on a dense buffer A (M x N in `layout`); see include/gbblas.h."""
+    call(f"gbblas_{_pfx(A)}mtv", layout, M, N, _dev(A), _dev(x), _dev(y), _stream_ptr(stream))
+    return y
+
+
+def vtm(layout: int, M: int, N: int, A, v, y, stream=None):
+    call(f"gbblas_{_pfx(A)}vtm", layout, M, N, _dev(A), _dev(v), _dev(y), _stream_ptr(stream))
+    return y
+
+
+def gemv(layout: int, transpose: bool, M: int, N: int, A, x, y, accumulate: bool, stream=None):
+    call(f"gbblas_{_pfx(A)}gemv", layout, int(transpose), M, N, _dev(A), _dev(x), int(accumulate), _dev(y),
+         _stream_ptr(stream))
+    return y
+
+
+def dot(a, b, out, stream=None):
+    """out[0] = a . b (out is a 1-element device tensor)."""
+    call(f"gbblas_{_pfx(a)}dot", a.numel(), _dev(a), _dev(b), _dev(out), _stream_ptr(stream))
+    return out
+
+
+# ---------------------------------------------------------------- numpy (host) helpers
+
+def _npfx(a) -> str:
+    import numpy as np
+    if a.dtype == np.float32:
+        return "s"
+    if a.dtype == np.float64:
+        return "d"
+    raise TypeError(f"unsupported dtype {a.dtype}")
+
+
+def gemm_host(M, N, K, a, rsa, csa, b, rsb, csb, c, rsc, csc, accuracy: int = ACCURACY_FP32):
+    p = _npfx(a)
+    args = [M, N, K, a.ctypes.data, rsa, csa, b.ctypes.data, rsb, csb, c.ctypes.data, rsc, csc]
+    if p == "s":
+        args.append(accuracy)
+    call(f"gbblas_{p}gemm_host", *args)
+
+
+def mtv_host(layout, M, N, a, x, y):
+    call(f"gbblas_{_npfx(a)}mtv_host", layout, M, N, a.ctypes.data, x.ctypes.data, y.ctypes.data)
+
+
+def vtm_host(layout, M, N, a, v, y):
+    call(f"gbblas_{_npfx(a)}vtm_host", layout, M, N, a.ctypes.data, v.ctypes.data, y.ctypes.data)
+
+
+def dot_host(a, b):
+    import numpy as np
+    out = np.zeros(1, a.dtype)
+    call(f"gbblas_{_npfx(a)}dot_host", a.size, a.ctypes.data, b.ctypes.data, out.ctypes.data)
+    return out[0]

@@ -1,0 +1,69 @@
+"""The C-ABI library without a GPU: it builds for sm_103a, loads, exports every
+symbol include/gbblas.h declares, validates arguments before touching a
+device, and fails loudly (GBBLAS_STATUS_NO_DEVICE) rather than computing
+anything on the CPU when no GB300 is present."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import gbblas
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "gbblas.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbblas_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_loads():
+    path = gbblas.build()
+    assert os.path.exists(path)
+    assert gbblas.lib().gbblas_version().decode().startswith("gbblas")
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared_symbols()
+    assert len(names) >= 20
+    L = gbblas.lib()
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in gbblas.SIGNATURES, f"{n} missing from the Python binding"
+
+
+def test_status_strings():
+    L = gbblas.lib()
+    for code, name in gbblas.STATUS.items():
+        assert L.gbblas_status_string(code).decode() == "GBBLAS_STATUS_" + name
+
+
+@pytest.mark.parametrize("fn,args", [
+    ("gbblas_sgemm", (-1, 2, 2, None, 1, 2, None, 1, 2, None, 1, 2, 0, None)),
+    ("gbblas_sgemm", (2, 2, 2, None, -1, 2, None, 1, 2, None, 1, 2, 0, None)),
+    ("gbblas_sgemm", (2, 2, 2, 16, 1, 2, 16, 1, 2, None, 1, 2, 0, None)),
+    ("gbblas_dgemm", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 0, 0, None)),
+    ("gbblas_smtv", (2, 4, 4, 16, 16, 16, None)),
+    ("gbblas_dvtm", (0, -3, 4, 16, 16, 16, None)),
+    ("gbblas_sdot", (-5, 16, 16, 16, None)),
+    ("gbblas_sdot", (5, None, 16, 16, None)),
+    ("gbblas_ddot_tuning", (5, 16, 16, 0, 1, 1, 16, None)),
+])
+def test_invalid_arguments_rejected_without_device(fn, args):
+    assert gbblas.status_of(fn, *args) == 1  # GBBLAS_STATUS_INVALID_VALUE
+    assert gbblas.lib().gbblas_last_error().decode()
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    a = np.ones(64, np.float32)
+    out = np.zeros(1, np.float32)
+    st = gbblas.status_of("gbblas_sdot_host", 64, a.ctypes.data, a.ctypes.data, out.ctypes.data)
+    assert st == 7  # GBBLAS_STATUS_NO_DEVICE
+    assert out[0] == 0
+    with pytest.raises(gbblas.GbblasError):
+        gbblas.dot_host(a, a)
