@@ -328,6 +328,11 @@ def run_gpu(args):
     # ---- results against device-side checks (cheap sanity, not the parity tests)
     results = {"dot_f32": t["r32"].item(), "dot_f64": t["r64"].item()}
 
+    if args.small:
+        if rank == 0:
+            print(json.dumps({"small_case": True, "per_op_ms": per_op_ms, "gpu_launches": int(launches)}))
+        return
+
     # ---- e2e: the same step through the host-buffer C ABI from pinned memory
     host = {}
     for k in ("A32", "x32", "a32", "b32", "A64", "x64", "a64", "b64"):
@@ -437,7 +442,15 @@ def main():
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: mtv 8192^2 and dot 2^26 (still larger than L2), "
+                         "no e2e and no CPU leg; not a benchmark result")
     args = ap.parse_args()
+    if args.small:
+        global M, N, NDOT
+        M = N = 8192
+        NDOT = 1 << 26
+        args.no_cpu = True
     if args.warmup < 3 and args.impl == "gbblas":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":

@@ -176,12 +176,12 @@ class tensor_core;
 template <std::size_t N, class L, class Container>
 class tensor_core<tensor_engine<extents<N>, L, Container>> {
  public:
-  using engine_type = tensor_engine<extents<N>, L, Container>;
+  using engine_type = tensor_engine<::boost::numeric::ublas::extents<N>, L, Container>;
   using container_type = Container;
   using value_type = typename Container::value_type;
   using layout_type = L;
-  using extents_type = extents<N>;
-  using strides_type = ublas::strides<N>;
+  using extents_type = ::boost::numeric::ublas::extents<N>;
+  using strides_type = ::boost::numeric::ublas::strides<N>;
   using size_type = std::size_t;
   using reference = value_type&;
   using const_reference = value_type const&;
