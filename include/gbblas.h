@@ -151,6 +151,27 @@ gbblas_status gbblas_dgemv(gbblas_layout la, int transpose, int64_t M, int64_t N
 gbblas_status gbblas_sdot(int64_t n, const float* a, const float* b, float* result, void* stream);
 gbblas_status gbblas_ddot(int64_t n, const double* a, const double* b, double* result, void* stream);
 
+/* Allocation-free form of gbblas_sdot.  No counterpart in the reference: the
+ * reference's dot allocates nothing because it runs on the CPU; this entry
+ * point exists for GPU callers that cannot allocate device memory when they
+ * call (a caller-owned memory pool or a pre-reserved serving loop that must
+ * not grow, or a foreign-language binding without access to cudaMalloc).
+ * It computes the same result as gbblas_sdot but calls no cudaMalloc,
+ * cudaFree or other allocating routine: its reduction scratch is one fixed
+ * 33,024-byte device array inside the library (room for 4096 per-CTA
+ * partials; a GB300 uses at most 608), which every GPU that loads the
+ * library keeps until the process exits.  Inputs and the DEVICE `result`
+ * pointer are the caller's, as for gbblas_sdot.
+ *   - The first call on each device looks up that array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the one array and it keeps the last call's contents;
+ *     the call clears the part that must start at zero.  Calls whose work
+ *     overlaps on the GPU (different streams, or different host threads
+ *     without ordering) race on the array: serialise them.
+ *   - A device whose grid would need more than 4096 partials gets
+ *     GBBLAS_STATUS_NOT_SUPPORTED with a message, never a partial result. */
+gbblas_status gbblas_sdot_noalloc(int64_t n, const float* a, const float* b, float* result, void* stream);
+
 /* amt::dot_prod_tuning_param (reference include/dot.hpp:92-141): the CPU
  * block sizes b1, b2, b3 have no meaning on the GPU; they are validated
  * (non-zero) and the call computes the same dot as gbblas_?dot. */

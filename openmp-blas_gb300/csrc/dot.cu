@@ -174,4 +174,106 @@ template gbblas_status launch_dot<float>(DeviceCtx*, int64_t, const float*, cons
 template gbblas_status launch_dot<double>(DeviceCtx*, int64_t, const double*, const double*, double*,
                                           cudaStream_t);
 
+// ------------------------------------------------------------------------
+// Allocation-free single-precision dot (gbblas_sdot_noalloc).
+//
+// Some callers cannot allocate device memory at call time: code running
+// under an allocator that forbids it (a caller-managed memory pool or a
+// real-time/serving loop that pre-reserves everything), or a host language
+// binding that cannot reach cudaMalloc.  For them the dot's reduction
+// scratch - the per-CTA FP64 partials and the completion counter that
+// gbblas_sdot takes from its per-stream pool - lives in one fixed device
+// array defined in this file instead.  Every GPU that loads the library
+// holds this array until the process exits.
+namespace {
+
+// Maximum number of per-CTA partials the array holds.  The dot grid is
+// (SMs x kDotCtasPerSm) CTAs at most: 608 on a 152-SM GB300.
+constexpr int kNoAllocMaxCtas = 4096;
+constexpr size_t kNoAllocBytes = kScratchZeroBytes + sizeof(double) * kNoAllocMaxCtas;  // 33,024 bytes
+
+// The scratch itself.  In host code `g_noalloc_scratch` names a host-side
+// stand-in, not device memory: its device address comes from
+// cudaGetSymbolAddress below and only that address is passed to kernels.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+struct NoAllocDev {
+  bool ready = false;
+  int num_sms = 0;
+  void* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDev g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+// Once per device, with that device current: check it is sm_103 and look up
+// the device address of the scratch array.  Allocates nothing.
+gbblas_status noalloc_setup(NoAllocDev** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    set_error("gbblas_sdot_noalloc: no usable CUDA device: %s", cudaGetErrorString(e));
+    return GBBLAS_STATUS_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocDev& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    int major = 0, minor = 0, sms = 0;
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (!(major == 10 && minor == 3)) {
+      set_error("gbblas_sdot_noalloc: device %d is sm_%d%d, not sm_103", dev, major, minor);
+      return GBBLAS_STATUS_NO_DEVICE;
+    }
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      set_error("gbblas_sdot_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return GBBLAS_STATUS_CUDA_ERROR;
+    }
+    d.num_sms = sms;
+    d.scratch = ptr;
+    d.ready = true;
+  }
+  *out = &d;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+}  // namespace
 }  // namespace gbblas
+
+extern "C" gbblas_status gbblas_sdot_noalloc(int64_t n, const float* a, const float* b, float* result,
+                                             void* stream) {
+  using namespace gbblas;
+  if (n < 0) {
+    set_error("gbblas_sdot_noalloc: negative size");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  if (!result || (n > 0 && (!a || !b))) {
+    set_error("gbblas_sdot_noalloc: null pointer");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  NoAllocDev* d = nullptr;
+  GB_TRY(noalloc_setup(&d));
+  cudaStream_t s = as_stream(stream);
+  const bool vec = aligned16(a) && aligned16(b);
+  const int64_t per_cta = (int64_t)kDotThreads * kDotUnroll * 4;
+  const int64_t want = (n + per_cta - 1) / per_cta;
+  const int64_t full = (int64_t)d->num_sms * kDotCtasPerSm;
+  const int64_t grid = want < full ? (want < 1 ? 1 : want) : full;
+  if (grid > kNoAllocMaxCtas) {
+    set_error("gbblas_sdot_noalloc: needs %lld reduction slots, the fixed scratch holds %d",
+              (long long)grid, kNoAllocMaxCtas);
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  unsigned* counter = static_cast<unsigned*>(d->scratch);
+  double* partials = reinterpret_cast<double*>(static_cast<char*>(d->scratch) + kScratchZeroBytes);
+  // The counter must start at zero; partials are fully rewritten by each call.
+  GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
+  if (vec)
+    dot_kernel<float, true><<<(unsigned)grid, kDotThreads, 0, s>>>(a, b, n, partials, counter, result);
+  else
+    dot_kernel<float, false><<<(unsigned)grid, kDotThreads, 0, s>>>(a, b, n, partials, counter, result);
+  return check_launch("dot_kernel (noalloc)");
+}

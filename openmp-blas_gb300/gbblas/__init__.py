@@ -51,6 +51,7 @@ SIGNATURES = {
     "gbblas_dgemv": (_int, [_int, _int, _i64, _i64, _vp, _vp, _int, _vp, _vp]),
     "gbblas_sdot": (_int, [_i64, _vp, _vp, _vp, _vp]),
     "gbblas_ddot": (_int, [_i64, _vp, _vp, _vp, _vp]),
+    "gbblas_sdot_noalloc": (_int, [_i64, _vp, _vp, _vp, _vp]),
     "gbblas_sdot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
     "gbblas_ddot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
     "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
