@@ -49,6 +49,7 @@ sys.path.insert(0, os.path.join(ROOT, "openmp-blas_gb300"))
 M = N = 16384
 NDOT = 1 << 28
 SEED = 1
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (vector and tensor), NVIDIA datasheet figure
 
 METRIC = "GEMV GB/s"
 UNIT = "GB/s"
@@ -129,52 +130,70 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, period_ms: int = 20):
         self.gpu = gpu_index
+        self.period = period_ms
         self.proc = None
-        self.path = None
+        self.samples = []  # (host time, line)
+        self.reader = None
+        self.window = None
 
     def __enter__(self):
-        fd, self.path = tempfile.mkstemp(suffix=".csv")
-        os.close(fd)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", str(self.period)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
         except (OSError, FileNotFoundError):
             self.proc = None
+        if self.proc is not None:
+            def pump():
+                for line in self.proc.stdout:
+                    self.samples.append((time.time(), line))
+            self.reader = threading.Thread(target=pump, daemon=True)
+            self.reader.start()
         time.sleep(0.3)
         return self
 
+    def mark(self, t0: float, t1: float) -> None:
+        """Host-clock bounds of the timed region."""
+        self.window = (t0, t1)
+
     def __exit__(self, *exc):
+        time.sleep(2 * self.period / 1e3)
         if self.proc is not None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+        if self.reader is not None:
+            self.reader.join(timeout=2)
 
     def summary(self):
-        if not self.path or not os.path.exists(self.path):
+        if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
-        for line in open(self.path):
+        for t, line in self.samples:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), parts[5:9], parts[4]))
+                rows.append((t, float(parts[1]), float(parts[2]), parts[5:9]))
             except ValueError:
                 continue
-        os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        inside = rows
+        if self.window:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 <= r[0] <= t1 + self.period / 1e3]
+            if not inside:  # region shorter than one period: the sample right after it
+                after = [r for r in rows if r[0] >= t0]
+                inside = after[:1] or rows[-1:]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
-        smax = max(r[1] for r in rows)
-        loaded = [r[0] for r in rows]
-        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
-                "samples": len(rows)}
+        reasons = sorted({names[i] for r in inside for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in rows),
+                "reasons": reasons, "samples": len(inside), "period_ms": self.period}
 
 
 # ------------------------------------------------------------------ CPU side
@@ -293,6 +312,7 @@ def run_gpu(args):
     with ClockSampler(local) as clk:
         barrier()
         torch.cuda.synchronize()
+        t_host0 = time.time()
         start.record(stream)
         for s in range(args.steps):
             for i, (_, f) in enumerate(ops):
@@ -301,6 +321,7 @@ def run_gpu(args):
                 ev[s][i][1].record(stream)
         end.record(stream)
         torch.cuda.synchronize()
+        clk.mark(t_host0, time.time())
         barrier()
     launches = gbblas.kernel_launches() - launches0
     clocks = clk.summary()
@@ -319,7 +340,15 @@ def run_gpu(args):
     ob = op_bytes()
     achieved = ob[dom] / (per_op_ms[dom] / 1e3) / 1e9
     kernels = {name: {"ms": round(per_op_ms[name], 4), "GB_s": round(ob[name] / (per_op_ms[name] / 1e3) / 1e9, 1),
-                      "frac": round(ob[name] / (per_op_ms[name] / 1e3) / 1e9 / peak, 4)} for name in per_op_ms}
+                      "frac_of_hbm": round(ob[name] / (per_op_ms[name] / 1e3) / 1e9 / peak, 4)} for name in per_op_ms}
+    # FP64 kernels do one DFMA per 8 (mtv) or 16 (dot) bytes; GB300's FP64 rate (1.25 TFLOP/s
+    # nominal, not in MEASURED_PEAKS.json) caps mtv_f64 below HBM speed.
+    fp64_flops = {"mtv_f64": 2 * M * N, "dot_f64": 2 * NDOT}
+    for name, fl in fp64_flops.items():
+        tf = fl / (per_op_ms[name] / 1e3) / 1e12
+        kernels[name]["fp64_TFLOPs"] = round(tf, 3)
+        kernels[name]["frac_of_fp64_nominal"] = round(tf / FP64_NOMINAL_TFLOPS, 4)
+    kernels["mtv_f64"]["bound"] = "fp64"
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
@@ -434,10 +463,88 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """The precision configuration: C = A*B, M = N = K = 8192 from float32,
+    as split-BF16 (three tcgen05 products) and plain FP32 (FMA pipe), on two
+    input sets (U[-1,1) and wide-range s*m*2^e, e in [-10, 10]); TFLOP/s of
+    2*M*N*K algorithmic flops and max / mean relative error against
+    long-double dots on sampled entries.  One JSON line per (path, set)."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    n = args.gemm_n
+    flops = 2.0 * n ** 3
+    g = torch.Generator(device="cuda").manual_seed(2)
+    rng = np.random.default_rng(2)
+    sample = 4096
+    rows = rng.integers(0, n, sample)
+    cols = rng.integers(0, n, sample)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    for set_name in ("uniform", "wide"):
+        if set_name == "uniform":
+            A = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
+            B = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
+        else:
+            def wide():
+                s = torch.where(torch.rand(n, n, generator=g, device="cuda") < 0.5, -1.0, 1.0)
+                m = torch.rand(n, n, generator=g, device="cuda") + 1.0
+                e = torch.randint(-10, 11, (n, n), generator=g, device="cuda").float()
+                return s * m * torch.exp2(e)
+            A, B = wide(), wide()
+        An, Bn = A.cpu().numpy(), B.cpu().numpy()
+        exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
+        for path, acc in (("bf16x3", 1), ("fp32", 0)):
+            C = torch.zeros(n, n, device="cuda")
+            sp = torch.cuda.current_stream().cuda_stream or None
+
+            def call():
+                gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1,
+                            acc, sp)
+            for _ in range(args.warmup):
+                call()
+            torch.cuda.synchronize()
+            iters = args.gemm_iters
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(0) as clk:
+                t0 = time.time()
+                e0.record()
+                for _ in range(iters):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                clk.mark(t0, time.time())
+            gbblas.call("gbblas_check_stream", sp)
+            ms = e0.elapsed_time(e1) / iters
+            # one clean product for the error check
+            C.zero_()
+            call()
+            got = C.cpu().numpy()[rows, cols].astype(np.float64)
+            rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
+            normwise = np.abs(got - exact) / absx
+            tf = flops / (ms / 1e3) / 1e12
+            line = {"metric": "FP32-accurate GEMM TFLOP/s", "path": path, "input_set": set_name,
+                    "value": round(tf, 2), "unit": "TFLOP/s", "ms_per_gemm": round(ms, 3), "M": n, "N": n, "K": n,
+                    "flops": "2*M*N*K algorithmic", "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
+                    "max_normwise_err": float(normwise.max()), "error_sample": f"{sample} entries vs long double",
+                    "clocks": clk.summary()}
+            if path == "bf16x3" and peaks.get("bf16_tflops"):
+                line["tensor_frac"] = round(3 * tf / peaks["bf16_tflops"], 4)
+                line["tensor_peak"] = f"3 BF16 products per algorithmic flop vs bf16_tflops {peaks['bf16_tflops']} (measured)"
+            print(json.dumps(line), flush=True)
+        del A, B
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="bandwidth", choices=["bandwidth", "precision"])
+    ap.add_argument("--gemm-n", type=int, default=8192)
+    ap.add_argument("--gemm-iters", type=int, default=5)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -455,6 +562,8 @@ def main():
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "precision":
+        run_precision(args)
     else:
         run_gpu(args)
 

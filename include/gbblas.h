@@ -84,6 +84,13 @@ gbblas_status gbblas_init(void);
  * devices).  Benchmarks read it before and after a timed region. */
 uint64_t gbblas_kernel_launches(void);
 
+/* Wait for `stream` and report device-side failures of this library's
+ * kernels on it: the tensor-core kernels bound every wait on the GPU and, if
+ * one gives up, record GBBLAS_STATUS_TIMEOUT instead of hanging.  Returns
+ * that status once (and clears it), else SUCCESS.  The *_host entry points
+ * do this check themselves. */
+gbblas_status gbblas_check_stream(void* stream);
+
 /* Release cached device and pinned-host memory held by the library for the
  * current device.  Safe to call at any time no call is in flight. */
 gbblas_status gbblas_release_cache(void);

@@ -87,6 +87,26 @@ gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void*
   return GBBLAS_STATUS_SUCCESS;
 }
 
+gbblas_status check_stream_errors(DeviceCtx* c, cudaStream_t stream) {
+  GB_CUDA_TRY(cudaStreamSynchronize(stream));
+  void* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->scratch.find(stream);
+    if (it == c->scratch.end() || !it->second.ptr) return GBBLAS_STATUS_SUCCESS;
+    p = it->second.ptr;
+  }
+  int code = 0;
+  int* word = reinterpret_cast<int*>(static_cast<char*>(p) + kErrWordOffset);
+  GB_CUDA_TRY(cudaMemcpy(&code, word, sizeof(int), cudaMemcpyDeviceToHost));
+  if (code != 0) {
+    GB_CUDA_TRY(cudaMemset(word, 0, sizeof(int)));
+    set_error("a kernel on this stream gave up a bounded device-side wait (status %d)", code);
+    return static_cast<gbblas_status>(code);
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
 gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out) {
   if (!c->host_stream) GB_CUDA_TRY(cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking));
   if (c->stage_bytes < bytes) {
@@ -175,7 +195,14 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
                        const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc,
                        cudaStream_t s) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
-  (void)acc;
+  if constexpr (std::is_same_v<T, float>) {
+    if (acc == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm: FP8 accuracy is not available");
+    // AUTO: the tensor-core path once the work is large enough to fill the
+    // 128 x 256 tiles of all SMs several times over.
+    const bool big = M >= 256 && N >= 256 && K >= 256 && (double)M * N * K >= 1.0e9;
+    if (acc == GBBLAS_ACCURACY_BF16X3 || (acc == GBBLAS_ACCURACY_AUTO && big))
+      return launch_gemm_bf16x3(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+  }
   return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
 }
 
@@ -216,6 +243,7 @@ gbblas_status gemm_host(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa
   GB_TRY(h2d(dB, B, nb * sizeof(T), s));
   GB_TRY(h2d(dC, C, nc * sizeof(T), s));
   GB_TRY(gemm_any<T>(c, M, N, K, dA, rsa, csa, dB, rsb, csb, dC, rsc, csc, acc, s));
+  GB_TRY(check_stream_errors(c, s));  // C on the host stays untouched if the GEMM gave up
   GB_TRY(d2h(C, dC, nc * sizeof(T), s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GBBLAS_STATUS_SUCCESS;
@@ -326,6 +354,12 @@ uint64_t gbblas_kernel_launches(void) { return gbblas::g_launches.load(); }
 gbblas_status gbblas_init(void) {
   DeviceCtx* c;
   return get_ctx(&c);
+}
+
+gbblas_status gbblas_check_stream(void* stream) {
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return check_stream_errors(c, as_stream(stream));
 }
 
 gbblas_status gbblas_release_cache(void) {

@@ -84,6 +84,9 @@ gbblas_status get_ctx(DeviceCtx** out);
 // fresh buffer are zeroed on the stream (reduction kernels keep their
 // completion counters there and return them to zero themselves).
 constexpr size_t kScratchZeroBytes = 256;
+// Byte offset, inside that zeroed header, of the stream's device error word:
+// kernels with bounded waits store a gbblas_status there when a wait gives up.
+constexpr size_t kErrWordOffset = 64;
 gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void** out);
 
 // Staging arena of at least `bytes` for the *_host paths (caller holds host_mu).
@@ -114,6 +117,16 @@ template <typename T>
 gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
                               int64_t csc, cudaStream_t stream);
+
+// C += A*B, FP32 operands split into BF16 hi+lo, three tcgen05 products
+// (gemm_tc.cu).
+gbblas_status launch_gemm_bf16x3(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
+                                 int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
+                                 int64_t csc, cudaStream_t stream);
+
+// Synchronise `stream` and report (then clear) any device-side error its
+// kernels recorded in the stream's scratch error word.
+gbblas_status check_stream_errors(DeviceCtx* c, cudaStream_t stream);
 
 }  // namespace gbblas
 
