@@ -57,12 +57,15 @@ typedef enum gbblas_layout {
 /* Arithmetic used by single-precision GEMM. */
 typedef enum gbblas_accuracy {
   GBBLAS_ACCURACY_FP32 = 0,   /* FP32 FMA on the CUDA cores (the reference's arithmetic) */
-  GBBLAS_ACCURACY_BF16X3 = 1, /* FP32-accurate: a = hi + lo in BF16, hi*hi + hi*lo + lo*hi
-                                 on tcgen05 tensor cores, FP32 accumulation in TMEM */
+  GBBLAS_ACCURACY_BF16X3 = 1, /* a = hi + lo in BF16, hi*hi + hi*lo + lo*hi on tcgen05
+                                 tensor cores, FP32 accumulation in TMEM: ~16 significand
+                                 bits per product, fastest FP32-input path */
   GBBLAS_ACCURACY_FP8 = 2,    /* low accuracy: E4M3 operands with one scale per 128
                                  elements along K, FP32 accumulation */
-  GBBLAS_ACCURACY_AUTO = 3    /* BF16X3 where the shape suits the tensor-core tiles,
+  GBBLAS_ACCURACY_AUTO = 3,   /* BF16X6 where the shape suits the tensor-core tiles,
                                  FP32 otherwise */
+  GBBLAS_ACCURACY_BF16X6 = 4  /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
+                                 the six products p_i*p_j with i + j < 3 on tcgen05 */
 } gbblas_accuracy;
 
 /* ---------------------------------------------------------------- library */

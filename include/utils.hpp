@@ -86,6 +86,7 @@ enum class accuracy : int {
   bf16x3 = GBBLAS_ACCURACY_BF16X3,
   fp8 = GBBLAS_ACCURACY_FP8,
   automatic = GBBLAS_ACCURACY_AUTO,
+  bf16x6 = GBBLAS_ACCURACY_BF16X6,
 };
 
 /// Throw std::runtime_error for a failed C-ABI call (the reference reports

@@ -197,11 +197,13 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if constexpr (std::is_same_v<T, float>) {
     if (acc == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm: FP8 accuracy is not available");
-    // AUTO: the tensor-core path once the work is large enough to fill the
-    // 128 x 256 tiles of all SMs several times over.
+    if (acc == GBBLAS_ACCURACY_BF16X3)
+      return launch_gemm_split_bf16(c, 2, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    // AUTO: the FP32-accurate tensor-core path once the work is large enough
+    // to fill the 128-row tiles of all SMs several times over.
     const bool big = M >= 256 && N >= 256 && K >= 256 && (double)M * N * K >= 1.0e9;
-    if (acc == GBBLAS_ACCURACY_BF16X3 || (acc == GBBLAS_ACCURACY_AUTO && big))
-      return launch_gemm_bf16x3(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    if (acc == GBBLAS_ACCURACY_BF16X6 || (acc == GBBLAS_ACCURACY_AUTO && big))
+      return launch_gemm_split_bf16(c, 3, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
   }
   return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
 }
@@ -318,7 +320,7 @@ template <typename T>
 gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
                        int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc, void* stream) {
   GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
-  if ((int)acc < 0 || (int)acc > 3) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+  if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
   return gemm_any<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, acc, as_stream(stream));

@@ -118,11 +118,11 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
                               int64_t csc, cudaStream_t stream);
 
-// C += A*B, FP32 operands split into BF16 hi+lo, three tcgen05 products
-// (gemm_tc.cu).
-gbblas_status launch_gemm_bf16x3(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
-                                 int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
-                                 int64_t csc, cudaStream_t stream);
+// C += A*B with FP32 operands split into `pieces` (2 or 3) BF16 parts and
+// the piece products summed on the tcgen05 tensor cores (gemm_tc.cu).
+gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_t N, int64_t K, const float* A,
+                                     int64_t rsa, int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C,
+                                     int64_t rsc, int64_t csc, cudaStream_t stream);
 
 // Synchronise `stream` and report (then clear) any device-side error its
 // kernels recorded in the stream's scratch error word.

@@ -22,6 +22,7 @@ ACCURACY_FP32 = 0
 ACCURACY_BF16X3 = 1
 ACCURACY_FP8 = 2
 ACCURACY_AUTO = 3
+ACCURACY_BF16X6 = 4
 
 STATUS = {
     0: "SUCCESS", 1: "INVALID_VALUE", 2: "SHAPE_MISMATCH", 3: "ALLOC_FAILED",
