@@ -540,9 +540,166 @@ def run_precision(args):
         del A, B
 
 
+def batching_shapes(seed=3):
+    """512 GEMM shapes (M, N, K log-uniform in [32, 2048], multiples of 8) and
+    4096 GEMV shapes (rows, cols log-uniform in [256, 16384])."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+
+    def lu(lo, hi, n):
+        return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+    g = np.maximum(8, np.round(lu(32, 2048, (512, 3)) / 8) * 8).astype(np.int64)
+    r = np.round(lu(256, 16384, 4096)).astype(np.int64)
+    c = np.round(lu(256, 16384, 4096)).astype(np.int64)
+    return g, r, c, rng
+
+
+def run_batching(args):
+    """The batching configuration: one graph-captured batch of 512 GEMMs
+    (float32 in, split-BF16 on the tensor cores) and 4096 row-major GEMVs,
+    U[-1,1) from seed 3.  The GEMV matrices (243.5 GB in total) are windows
+    at random 16-byte-aligned offsets of one pool of U[-1,1) data (--pool-gb),
+    so the batch fits next to other users on the GPU; every GEMV still
+    streams its whole matrix from HBM.  Reports the batch time, its
+    roofline (sum of each problem's roofline time: tensor peak for GEMMs,
+    HBM for GEMVs), sampled errors, and the CPU oracle on a sample."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    acc = {"bf16x3": 1, "bf16x6": 4}[args.batch_accuracy]
+    products = {1: 3, 4: 6}[acc]
+    g, r, c, rng = batching_shapes()
+    gen = torch.Generator(device=dev).manual_seed(3)
+
+    def U(*shape):
+        return torch.rand(*shape, generator=gen, device=dev).mul_(2).sub_(1)
+
+    gemms, gemm_t = [], []
+    for (M, N, K) in g:
+        A, B, C = U(M, K), U(K, N), torch.zeros(M, N, device=dev)
+        gemms.append(gbblas.gemm_desc(A, B, C))
+        gemm_t.append((A, B, C))
+    pool_elems = int(args.pool_gb * (1 << 30)) // 4
+    pool = torch.empty(pool_elems, device=dev)
+    step = 1 << 28
+    for s0 in range(0, pool_elems, step):
+        pool[s0:s0 + step].uniform_(-1, 1, generator=gen)
+    gemvs, gemv_t = [], []
+    for rows, cols in zip(r, c):
+        n = int(rows * cols)
+        off = int(rng.integers(0, (pool_elems - n) // 4)) * 4
+        A = pool[off:off + n].view(int(rows), int(cols))
+        x, y = U(int(cols)), torch.zeros(int(rows), device=dev)
+        gemvs.append(gbblas.gemv_desc(1, 0, int(rows), int(cols), A, x, y))
+        gemv_t.append((A, x, y))
+    gemm_flops = float((2 * g.prod(1)).sum())
+    gemv_bytes = float(((r * c + r + c) * 4).sum())
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+    t_gemm_roof = gemm_flops * products / (peaks["bf16_tflops"] * 1e12)
+    t_gemv_roof = gemv_bytes / (peaks["hbm_gbs"] * 1e9)
+
+    def time_batch(batch, iters):
+        s = torch.cuda.current_stream()
+        for _ in range(args.warmup):
+            batch.run(s)
+        batch.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(iters):
+            batch.run(s)
+        e1.record(s)
+        batch.sync()
+        return e0.elapsed_time(e1) / iters
+
+    launches0 = gbblas.kernel_launches()
+    t0 = time.perf_counter()
+    b_all = gbblas.Batch(gemms, gemvs, accuracy=acc)
+    plan_s = time.perf_counter() - t0
+    b_gemm = gbblas.Batch(gemms, [], accuracy=acc)
+    b_gemv = gbblas.Batch([], gemvs, accuracy=acc)
+    with ClockSampler(0) as clk:
+        t_wall0 = time.time()
+        ms_all = time_batch(b_all, args.steps)
+        clk.mark(t_wall0, time.time())
+    ms_gemm = time_batch(b_gemm, args.steps)
+    ms_gemv = time_batch(b_gemv, args.steps)
+    launches = gbblas.kernel_launches() - launches0
+
+    # sampled errors: fresh C (the timed runs accumulated into it)
+    pick_g = rng.choice(len(gemms), 8, replace=False)
+    pick_v = rng.choice(len(gemvs), 16, replace=False)
+    for A, B, C in gemm_t:
+        C.zero_()
+    b_gemm.run()
+    b_gemm.sync()
+    gemm_err = 0.0
+    for i in pick_g:
+        A, B, C = gemm_t[i]
+        ref = A.double() @ B.double()
+        scale = A.abs().double() @ B.abs().double()
+        gemm_err = max(gemm_err, float(((C.double() - ref).abs() / scale).max()))
+    gemv_err = 0.0
+    for i in pick_v:
+        A, x, y = gemv_t[i]
+        ref = A.double() @ x.double()
+        scale = A.abs().double() @ x.abs().double()
+        gemv_err = max(gemv_err, float(((y.double() - ref).abs() / scale).max()))
+
+    # CPU oracle on a sample (serial per problem, all host cores each)
+    cpu = None
+    if not args.no_cpu:
+        O.set_threads(os.cpu_count() or 1)
+        sg = rng.choice(len(gemms), 24, replace=False)
+        sv = rng.choice(len(gemvs), 48, replace=False)
+        hg = [(gemm_t[i][0].cpu().numpy(), gemm_t[i][1].cpu().numpy()) for i in sg]
+        hv = [(gemv_t[i][0].cpu().numpy(), gemv_t[i][1].cpu().numpy()) for i in sv]
+        t0 = time.perf_counter()
+        for A, B in hg:
+            M, K = A.shape
+            N = B.shape[1]
+            Cc = np.zeros((M, N), np.float32)
+            O.gemm_raw(M, N, K, A, K, 1, B, N, 1, Cc, N, 1)
+        tg = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for A, x in hv:
+            yy = np.zeros(A.shape[0], np.float32)
+            O.mtv_raw(1, A.shape[0], A.shape[1], np.ascontiguousarray(A), x, yy)
+        tv = time.perf_counter() - t0
+        fl_s = float(sum(2 * g[i].prod() for i in sg))
+        by_s = float(sum((r[i] * c[i] + r[i] + c[i]) * 4 for i in sv))
+        est = gemm_flops / (fl_s / tg) + gemv_bytes / (by_s / tv)
+        cpu = {"value": round(est * 1e3, 1), "unit": "ms per batch (estimated)", "cores": os.cpu_count(),
+               "kind": cpu_kind(), "sample": f"{len(sg)} GEMMs + {len(sv)} GEMVs of the batch run serially on the "
+                                              f"oracle ({tg:.2f} s + {tv:.2f} s), scaled by flops and bytes"}
+    line = {"metric": "batch ms (512 GEMM + 4096 GEMV, one graph)", "value": round(ms_all, 3), "unit": "ms",
+            "higher_is_better": False, "accuracy": args.batch_accuracy,
+            "ms_gemm_only": round(ms_gemm, 3), "ms_gemv_only": round(ms_gemv, 3),
+            "gemm_TFLOPs": round(gemm_flops / (ms_gemm / 1e3) / 1e12, 1),
+            "gemv_GBs": round(gemv_bytes / (ms_gemv / 1e3) / 1e9, 1),
+            "roofline": {"ms": round((t_gemm_roof + t_gemv_roof) * 1e3, 3),
+                         "frac": round((t_gemm_roof + t_gemv_roof) / (ms_all / 1e3), 4),
+                         "gemm_ms": round(t_gemm_roof * 1e3, 3), "gemv_ms": round(t_gemv_roof * 1e3, 3),
+                         "peaks": "MEASURED_PEAKS.json bf16_tflops (x products) and hbm_gbs"},
+            "plan_s": round(plan_s, 2), "gemm_flops": gemm_flops, "gemv_bytes": gemv_bytes,
+            "max_normwise_err": {"gemm": gemm_err, "gemv": gemv_err}, "cpu_baseline": cpu,
+            "gpu_launches_incl_graphs": int(launches), "clocks": clk.summary(),
+            "config": {"workload": "512 GEMM log-uniform [32,2048] + 4096 GEMV log-uniform [256,16384], seed 3",
+                       "gemv_pool_GiB": args.pool_gb}}
+    print(json.dumps(line), flush=True)
+    for b in (b_all, b_gemm, b_gemv):
+        b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="bandwidth", choices=["bandwidth", "precision"])
+    ap.add_argument("--workload", default="bandwidth", choices=["bandwidth", "precision", "batching"])
+    ap.add_argument("--pool-gb", type=float, default=48.0)
+    ap.add_argument("--batch-accuracy", default="bf16x3", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--gemm-n", type=int, default=8192)
     ap.add_argument("--gemm-iters", type=int, default=5)
     ap.add_argument("--gpus", type=int, default=1)
@@ -566,6 +723,8 @@ def main():
         run_reference(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "batching":
+        run_batching(args)
     else:
         run_gpu(args)
 

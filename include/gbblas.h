@@ -190,6 +190,63 @@ gbblas_status gbblas_sdot_tuning(int64_t n, const float* a, const float* b, int6
 gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, int64_t b1, int64_t b2,
                                  int64_t b3, double* result, void* stream);
 
+/* ------------------------------------------------------------- batching
+ * Many independent problems in one launch.  No counterpart in the reference,
+ * which runs one call at a time; these serve callers that would otherwise
+ * loop over amt::mtm / amt::mtv (reference src/mtm.cpp:189-214,
+ * src/mtv.cpp:173-201 call them once per size). */
+
+/* One GEMM of a group: C += A * B with the strides of gbblas_sgemm
+ * (DEVICE pointers). */
+typedef struct gbblas_gemm_desc {
+  int64_t M, N, K;
+  const float* A;
+  int64_t rsa, csa;
+  const float* B;
+  int64_t rsb, csb;
+  float* C;
+  int64_t rsc, csc;
+} gbblas_gemm_desc;
+
+/* One GEMV of a group: y = op(A) x (+ y if accumulate), A dense M x N of
+ * layout `layout`, op(A) = A (transpose = 0, y has M entries) or A^T
+ * (transpose = 1, y has N entries).  DEVICE pointers. */
+typedef struct gbblas_gemv_desc {
+  int32_t layout;
+  int32_t transpose;
+  int32_t accumulate;
+  int32_t reserved;
+  int64_t M, N;
+  const float* A;
+  const float* x;
+  float* y;
+} gbblas_gemv_desc;
+
+/* All GEMMs in one persistent tensor-core launch (accuracy BF16X3, BF16X6 or
+ * AUTO = BF16X6; FP32 runs them one by one on the CUDA cores).  Problems may
+ * not overlap their C. */
+gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count, gbblas_accuracy accuracy,
+                                   void* stream);
+
+/* All GEMVs in one persistent launch (row-streaming forms); column-streaming
+ * forms run as per-problem launches on the same stream. */
+gbblas_status gbblas_sgemv_grouped(const gbblas_gemv_desc* descs, int64_t count, void* stream);
+
+/* A batch: a fixed set of GEMMs and GEMVs planned once (tables uploaded,
+ * tile schedule chosen by the autotuner) and captured into a CUDA graph whose
+ * two branches - the grouped tensor-core GEMM and the grouped GEMV - run
+ * concurrently.  gbblas_batch_run replays the graph on `stream`; operand
+ * pointers are fixed at creation.  Like every GEMM here, each run
+ * ACCUMULATES into the C matrices (and into y where accumulate is set). */
+typedef struct gbblas_batch_s* gbblas_batch;
+gbblas_status gbblas_batch_create(const gbblas_gemm_desc* gemms, int64_t ngemm, gbblas_accuracy accuracy,
+                                  const gbblas_gemv_desc* gemvs, int64_t ngemv, gbblas_batch* out);
+gbblas_status gbblas_batch_run(gbblas_batch batch, void* stream);
+/* Wait for the batch's last run; GBBLAS_STATUS_TIMEOUT if one of its
+ * tensor-core kernels gave up a bounded device-side wait. */
+gbblas_status gbblas_batch_sync(gbblas_batch batch);
+gbblas_status gbblas_batch_destroy(gbblas_batch batch);
+
 /* ------------------------------------------------ host-buffer entry points
  * Same operations on HOST pointers: inputs are copied to the device, the
  * kernel runs, outputs come back, and the call returns when host memory

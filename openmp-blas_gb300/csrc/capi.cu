@@ -87,6 +87,14 @@ gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void*
   return GBBLAS_STATUS_SUCCESS;
 }
 
+void release_scratch(DeviceCtx* c, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->scratch.find(stream);
+  if (it == c->scratch.end()) return;
+  if (it->second.ptr) cudaFreeAsync(it->second.ptr, stream);
+  c->scratch.erase(it);
+}
+
 gbblas_status check_stream_errors(DeviceCtx* c, cudaStream_t stream) {
   GB_CUDA_TRY(cudaStreamSynchronize(stream));
   void* p = nullptr;
@@ -199,10 +207,9 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
     if (acc == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm: FP8 accuracy is not available");
     if (acc == GBBLAS_ACCURACY_BF16X3)
       return launch_gemm_split_bf16(c, 2, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
-    // AUTO: the FP32-accurate tensor-core path once the work is large enough
-    // to fill the 128-row tiles of all SMs several times over.
-    const bool big = M >= 256 && N >= 256 && K >= 256 && (double)M * N * K >= 1.0e9;
-    if (acc == GBBLAS_ACCURACY_BF16X6 || (acc == GBBLAS_ACCURACY_AUTO && big))
+    // AUTO: whichever FP32-accurate path the autotuner measured faster for
+    // this shape bucket (FMA kernel or split-BF16 with six products).
+    if (acc == GBBLAS_ACCURACY_BF16X6 || (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1))
       return launch_gemm_split_bf16(c, 3, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
   }
   return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
@@ -436,6 +443,37 @@ gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, in
                                  double* result, void* stream) {
   if (b1 <= 0 || b2 <= 0 || b3 <= 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "dot_tuning: block sizes must be > 0");
   return dot_dev<double>(n, a, b, result, stream);
+}
+
+gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count, gbblas_accuracy accuracy,
+                                   void* stream) {
+  if (count < 0 || (count > 0 && !descs)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: bad arguments");
+  if ((int)accuracy < 0 || (int)accuracy > 4)
+    return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: unknown accuracy %d", (int)accuracy);
+  if (accuracy == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm_grouped: FP8 is not available");
+  for (int64_t i = 0; i < count; ++i) {
+    const gbblas_gemm_desc& g = descs[i];
+    GB_TRY(check_gemm<float>(g.M, g.N, g.K, g.A, g.rsa, g.csa, g.B, g.rsb, g.csb, g.C, g.rsc, g.csc));
+  }
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  cudaStream_t s = as_stream(stream);
+  if (accuracy == GBBLAS_ACCURACY_FP32) {
+    for (int64_t i = 0; i < count; ++i) {
+      const gbblas_gemm_desc& g = descs[i];
+      GB_TRY(gemm_any<float>(c, g.M, g.N, g.K, g.A, g.rsa, g.csa, g.B, g.rsb, g.csb, g.C, g.rsc, g.csc,
+                             GBBLAS_ACCURACY_FP32, s));
+    }
+    return GBBLAS_STATUS_SUCCESS;
+  }
+  return launch_gemm_split_bf16_group(c, accuracy == GBBLAS_ACCURACY_BF16X3 ? 2 : 3, descs, count, s);
+}
+
+gbblas_status gbblas_sgemv_grouped(const gbblas_gemv_desc* descs, int64_t count, void* stream) {
+  if (count < 0 || (count > 0 && !descs)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemv_grouped: bad arguments");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return launch_gemv_group(c, descs, count, as_stream(stream));
 }
 
 gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa,

@@ -87,7 +87,12 @@ constexpr size_t kScratchZeroBytes = 256;
 // Byte offset, inside that zeroed header, of the stream's device error word:
 // kernels with bounded waits store a gbblas_status there when a wait gives up.
 constexpr size_t kErrWordOffset = 64;
+// Byte offset of the persistent kernels' tile counter (reset before each launch).
+constexpr size_t kTileCounterOffset = 128;
 gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void** out);
+
+// Free the scratch of `stream` (stream-ordered) and forget it.
+void release_scratch(DeviceCtx* c, cudaStream_t stream);
 
 // Staging arena of at least `bytes` for the *_host paths (caller holds host_mu).
 gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out);
@@ -123,6 +128,30 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
 gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_t N, int64_t K, const float* A,
                                      int64_t rsa, int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C,
                                      int64_t rsc, int64_t csc, cudaStream_t stream);
+
+// The same for a group of independent problems in one persistent launch
+// (tables and BF16 arena in the stream's scratch).
+gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
+                                           cudaStream_t stream);
+
+// A group bound to its own device memory, for repeated (graph-captured)
+// launches: create uploads the tables once; launch only enqueues kernels.
+struct TcGroupPlan;
+gbblas_status tc_group_create(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
+                              TcGroupPlan** out);
+gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream);
+void tc_group_destroy(TcGroupPlan* plan);
+int* tc_group_error_word(const TcGroupPlan* plan);
+
+// Set the tensor-core kernels' launch attributes (before any stream capture).
+void tc_prepare(DeviceCtx* c);
+
+// Grouped GEMV: row-streaming problems in one persistent launch, the rest
+// per problem (batch.cu).
+gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s);
+
+// Autotuner (tune.cu): AUTO accuracy -> 1 = split-BF16 six products, 0 = FMA.
+int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 
 // Synchronise `stream` and report (then clear) any device-side error its
 // kernels recorded in the stream's scratch error word.

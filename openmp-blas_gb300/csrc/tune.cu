@@ -1,0 +1,224 @@
+// tune.cu - the autotuner.
+//
+// The reference picks its blocking once per process from the CPU's cache
+// geometry and a hard-coded FMA latency table (include/mtm.hpp:19-81,
+// include/cpuinfo.hpp:167-223, include/cache_manager.hpp:107-150).  On the
+// GPU the choices are kernel variants, and they are picked by measurement:
+// the first time a (device, operation, shape bucket, dtype, accuracy) key is
+// seen, every candidate is timed with CUDA events on scratch outputs and the
+// fastest is remembered - in memory, and in a JSON file so later processes
+// start tuned.
+//
+//   GBBLAS_AUTOTUNE=0      use the built-in defaults, time nothing
+//   GBBLAS_TUNE_CACHE=path cache file (default $XDG_CACHE_HOME/gbblas/tune.json
+//                          or ~/.cache/gbblas/tune.json); unwritable = memory only
+//
+// Tuned choices:
+//   gemv_group_rows  rows per warp item of the grouped row-streaming GEMV
+//                    (1, 2, 4, 8), bucketed by median log2 rows / cols;
+//   gemm_auto        for GBBLAS_ACCURACY_AUTO, FP32 FMA kernel or split-BF16
+//                    (six products) - both FP32-accurate - bucketed by
+//                    log2 M, N, K.
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <regex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gbblas {
+
+gbblas_status time_gemv_group_variant(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, int R, float* ms);
+
+namespace {
+
+class Tuner {
+ public:
+  static Tuner& get() {
+    static Tuner t;
+    return t;
+  }
+
+  bool enabled() const { return enabled_; }
+
+  // Cached choice for `key`, or -1.
+  int lookup(const std::string& key) {
+    std::lock_guard<std::mutex> lk(mu_);
+    load_locked();
+    auto it = cache_.find(key);
+    return it == cache_.end() ? -1 : it->second;
+  }
+
+  void store(const std::string& key, int value) {
+    std::lock_guard<std::mutex> lk(mu_);
+    load_locked();
+    cache_[key] = value;
+    save_locked();
+  }
+
+ private:
+  Tuner() {
+    const char* e = std::getenv("GBBLAS_AUTOTUNE");
+    enabled_ = !(e && std::string(e) == "0");
+    if (const char* p = std::getenv("GBBLAS_TUNE_CACHE")) {
+      path_ = p;
+    } else if (const char* x = std::getenv("XDG_CACHE_HOME")) {
+      path_ = std::string(x) + "/gbblas/tune.json";
+    } else if (const char* h = std::getenv("HOME")) {
+      path_ = std::string(h) + "/.cache/gbblas/tune.json";
+    }
+  }
+
+  void load_locked() {
+    if (loaded_) return;
+    loaded_ = true;
+    if (path_.empty()) return;
+    std::ifstream f(path_);
+    if (!f) return;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string text = ss.str();
+    static const std::regex kv("\"([^\"]+)\"\\s*:\\s*(-?[0-9]+)");
+    for (auto it = std::sregex_iterator(text.begin(), text.end(), kv); it != std::sregex_iterator(); ++it) {
+      const std::string key = (*it)[1];
+      if (key == "version") continue;
+      cache_[key] = std::atoi((*it)[2].str().c_str());
+    }
+  }
+
+  void save_locked() {
+    if (path_.empty()) return;
+    const auto slash = path_.find_last_of('/');
+    if (slash != std::string::npos) {
+      std::string dir = path_.substr(0, slash);
+      for (size_t i = 1; i <= dir.size(); ++i)
+        if (i == dir.size() || dir[i] == '/') ::mkdir(dir.substr(0, i).c_str(), 0755);
+    }
+    const std::string tmp = path_ + ".tmp";
+    std::ofstream f(tmp);
+    if (!f) return;
+    f << "{\n  \"version\": 1";
+    for (const auto& kv : cache_) f << ",\n  \"" << kv.first << "\": " << kv.second;
+    f << "\n}\n";
+    f.close();
+    std::rename(tmp.c_str(), path_.c_str());
+  }
+
+  std::mutex mu_;
+  std::map<std::string, int> cache_;
+  bool loaded_ = false;
+  bool enabled_ = true;
+  std::string path_;
+};
+
+std::string device_tag(DeviceCtx* c) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, c->device) != cudaSuccess) return "unknown";
+  std::string name = p.name;
+  std::replace(name.begin(), name.end(), ' ', '_');
+  return name + "_sm" + std::to_string(c->num_sms);
+}
+
+int log2_bucket(int64_t v) { return v <= 1 ? 0 : (int)std::lround(std::log2((double)v)); }
+
+}  // namespace
+
+int tuned_gemv_group_rows(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count) {
+  constexpr int kDefault = 4;
+  Tuner& t = Tuner::get();
+  std::vector<int64_t> rows, cols;
+  for (int64_t i = 0; i < count; ++i) {
+    const bool tr = d[i].transpose != 0;
+    const bool rows_contig = (d[i].layout == GBBLAS_LAST_ORDER) != tr;
+    if (!rows_contig || d[i].M <= 0 || d[i].N <= 0) continue;
+    rows.push_back(tr ? d[i].N : d[i].M);
+    cols.push_back(tr ? d[i].M : d[i].N);
+  }
+  if (rows.empty()) return kDefault;
+  std::nth_element(rows.begin(), rows.begin() + rows.size() / 2, rows.end());
+  std::nth_element(cols.begin(), cols.begin() + cols.size() / 2, cols.end());
+  const std::string key = "gemv_group_rows|" + device_tag(c) + "|r" + std::to_string(log2_bucket(rows[rows.size() / 2])) +
+                          "|c" + std::to_string(log2_bucket(cols[cols.size() / 2])) + "|n" +
+                          std::to_string(log2_bucket((int64_t)rows.size())) + "|f32";
+  int v = t.lookup(key);
+  if (v > 0) return v;
+  if (!t.enabled()) return kDefault;
+  int best = kDefault;
+  float best_ms = 1e30f;
+  for (int R : {1, 2, 4, 8}) {
+    float ms = 0.f;
+    if (time_gemv_group_variant(c, d, count, R, &ms) != GBBLAS_STATUS_SUCCESS) return kDefault;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = R;
+    }
+  }
+  t.store(key, best);
+  return best;
+}
+
+// 1 = split-BF16 (six products), 0 = FP32 FMA, for an AUTO-accuracy GEMM of
+// this shape.  Without tuning: the tensor cores once the work fills them.
+int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
+  const int fallback = (M >= 256 && N >= 256 && K >= 256 && (double)M * N * K >= 1.0e9) ? 1 : 0;
+  Tuner& t = Tuner::get();
+  const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
+  const std::string key = "gemm_auto|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
+                          "|k" + std::to_string(bk) + "|f32";
+  int v = t.lookup(key);
+  if (v >= 0) return v;
+  if (!t.enabled()) return fallback;
+  // representative shape of the bucket, capped so tuning stays cheap
+  const int64_t m = std::min<int64_t>(int64_t(1) << bm, 8192), n = std::min<int64_t>(int64_t(1) << bn, 8192),
+                k = std::min<int64_t>(int64_t(1) << bk, 8192);
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return fallback;
+  void* mem = nullptr;
+  const size_t bytes = sizeof(float) * (size_t)(m * k + k * n + m * n);
+  if (cudaMallocAsync(&mem, bytes, s) != cudaSuccess) {
+    cudaStreamDestroy(s);
+    return fallback;
+  }
+  cudaMemsetAsync(mem, 0, bytes, s);
+  float* A = static_cast<float*>(mem);
+  float* B = A + m * k;
+  float* C = B + k * n;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best_ms[2] = {1e30f, 1e30f};
+  for (int choice = 0; choice < 2; ++choice) {
+    auto run = [&]() {
+      return choice == 1 ? launch_gemm_split_bf16(c, 3, m, n, k, A, k, 1, B, n, 1, C, n, 1, s)
+                         : launch_gemm_fma<float>(c, m, n, k, A, k, 1, B, n, 1, C, n, 1, s);
+    };
+    if (run() != GBBLAS_STATUS_SUCCESS) continue;  // warm-up
+    cudaEventRecord(e0, s);
+    bool ok = true;
+    for (int i = 0; i < 3 && ok; ++i) ok = run() == GBBLAS_STATUS_SUCCESS;
+    cudaEventRecord(e1, s);
+    if (!ok || cudaEventSynchronize(e1) != cudaSuccess) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best_ms[choice] = ms;
+  }
+  cudaFreeAsync(mem, s);
+  cudaStreamSynchronize(s);
+  release_scratch(c, s);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  if (best_ms[0] >= 1e30f && best_ms[1] >= 1e30f) return fallback;
+  const int best = best_ms[1] < best_ms[0] ? 1 : 0;
+  t.store(key, best);
+  return best;
+}
+
+}  // namespace gbblas

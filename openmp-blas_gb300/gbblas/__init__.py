@@ -56,6 +56,12 @@ SIGNATURES = {
     "gbblas_sdot_noalloc": (_int, [_i64, _vp, _vp, _vp, _vp]),
     "gbblas_sdot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
     "gbblas_ddot_tuning": (_int, [_i64, _vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "gbblas_sgemm_grouped": (_int, [_vp, _i64, _int, _vp]),
+    "gbblas_sgemv_grouped": (_int, [_vp, _i64, _vp]),
+    "gbblas_batch_create": (_int, [_vp, _i64, _int, _vp, _i64, _vp]),
+    "gbblas_batch_run": (_int, [_vp, _vp]),
+    "gbblas_batch_sync": (_int, [_vp]),
+    "gbblas_batch_destroy": (_int, [_vp]),
     "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
     "gbblas_dgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
     "gbblas_smtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
@@ -173,6 +179,70 @@ def dot(a, b, out, stream=None):
     """out[0] = a . b (out is a 1-element device tensor)."""
     call(f"gbblas_{_pfx(a)}dot", a.numel(), _dev(a), _dev(b), _dev(out), _stream_ptr(stream))
     return out
+
+
+# ---------------------------------------------------------------- batching
+
+class GemmDesc(ctypes.Structure):
+    """gbblas_gemm_desc: C += A*B with element strides (device pointers)."""
+    _fields_ = [("M", _i64), ("N", _i64), ("K", _i64), ("A", _vp), ("rsa", _i64), ("csa", _i64),
+                ("B", _vp), ("rsb", _i64), ("csb", _i64), ("C", _vp), ("rsc", _i64), ("csc", _i64)]
+
+
+class GemvDesc(ctypes.Structure):
+    """gbblas_gemv_desc: y = op(A) x (+ y); A dense M x N in `layout` (device pointers)."""
+    _fields_ = [("layout", ctypes.c_int32), ("transpose", ctypes.c_int32), ("accumulate", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("M", _i64), ("N", _i64), ("A", _vp), ("x", _vp), ("y", _vp)]
+
+
+def gemm_desc(A, B, C) -> GemmDesc:
+    """Descriptor of C += A @ B for 2-D float32 CUDA tensors (any strides)."""
+    return GemmDesc(A.shape[0], B.shape[1], A.shape[1], _dev(A), A.stride(0), A.stride(1),
+                    _dev(B), B.stride(0), B.stride(1), _dev(C), C.stride(0), C.stride(1))
+
+
+def gemv_desc(layout, transpose, M, N, A, x, y, accumulate=False) -> GemvDesc:
+    return GemvDesc(layout, int(transpose), int(accumulate), 0, M, N, _dev(A), _dev(x), _dev(y))
+
+
+def gemm_grouped(descs, accuracy: int = ACCURACY_BF16X6, stream=None):
+    arr = (GemmDesc * len(descs))(*descs)
+    call("gbblas_sgemm_grouped", ctypes.addressof(arr), len(descs), accuracy, _stream_ptr(stream))
+
+
+def gemv_grouped(descs, stream=None):
+    arr = (GemvDesc * len(descs))(*descs)
+    call("gbblas_sgemv_grouped", ctypes.addressof(arr), len(descs), _stream_ptr(stream))
+
+
+class Batch:
+    """A batch of GEMMs and GEMVs captured into one CUDA graph
+    (gbblas_batch_create / run / sync / destroy)."""
+
+    def __init__(self, gemms=(), gemvs=(), accuracy: int = ACCURACY_BF16X6):
+        ga = (GemmDesc * max(1, len(gemms)))(*gemms)
+        va = (GemvDesc * max(1, len(gemvs)))(*gemvs)
+        h = ctypes.c_void_p()
+        call("gbblas_batch_create", ctypes.addressof(ga), len(gemms), accuracy, ctypes.addressof(va), len(gemvs),
+             ctypes.byref(h))
+        self.handle = h
+
+    def run(self, stream=None):
+        call("gbblas_batch_run", self.handle, _stream_ptr(stream))
+
+    def sync(self):
+        call("gbblas_batch_sync", self.handle)
+
+    def close(self):
+        if self.handle:
+            call("gbblas_batch_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------- numpy (host) helpers

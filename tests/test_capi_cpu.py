@@ -67,3 +67,26 @@ def test_no_cpu_fallback_without_gpu():
     assert out[0] == 0
     with pytest.raises(gbblas.GbblasError):
         gbblas.dot_host(a, a)
+
+
+def test_descriptor_structs_match_the_c_layout(tmp_path):
+    """The ctypes mirrors of gbblas_gemm_desc / gbblas_gemv_desc have the C
+    sizes and field offsets (checked with the C compiler)."""
+    import ctypes
+    import subprocess
+    src = tmp_path / "layout.c"
+    fields_g = [f for f, _ in gbblas.GemmDesc._fields_]
+    fields_v = [f for f, _ in gbblas.GemvDesc._fields_]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbblas.h"', "int main(void){",
+             'printf("%zu\\n", sizeof(gbblas_gemm_desc));', 'printf("%zu\\n", sizeof(gbblas_gemv_desc));']
+    lines += [f'printf("%zu\\n", offsetof(gbblas_gemm_desc, {f}));' for f in fields_g]
+    lines += [f'printf("%zu\\n", offsetof(gbblas_gemv_desc, {f}));' for f in fields_v]
+    lines += ["return 0;}"]
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [ctypes.sizeof(gbblas.GemmDesc), ctypes.sizeof(gbblas.GemvDesc)]
+    want += [getattr(gbblas.GemmDesc, f).offset for f in fields_g]
+    want += [getattr(gbblas.GemvDesc, f).offset for f in fields_v]
+    assert out == want
