@@ -247,6 +247,75 @@ gbblas_status gbblas_batch_run(gbblas_batch batch, void* stream);
 gbblas_status gbblas_batch_sync(gbblas_batch batch);
 gbblas_status gbblas_batch_destroy(gbblas_batch batch);
 
+/* -------------------------------------------------------------- serving
+ * A request loop with continuous batching.  No counterpart in the
+ * reference (it has no serving path); it serves callers that issue many
+ * mtm / mtv / dot calls of mixed sizes and precisions concurrently.
+ *
+ * Requests are submitted from any host thread.  A scheduler thread admits
+ * them in arrival order while their working set fits the free-HBM budget
+ * and a stream slot is free, coalesces everything admitted in one round
+ * into grouped launches (split-BF16 GEMMs in one persistent tensor-core
+ * launch, float GEMVs in one grouped launch; FP64, FP32-FMA and dot
+ * requests as their own kernels) on one of `streams` CUDA streams, so work
+ * of successive rounds overlaps on the device.  A host function queued
+ * behind each round stamps its requests complete.  Operands and results are
+ * DEVICE memory, normally taken from the server's pool (gbblas_server_alloc).
+ * Each result is identical whether a request runs alone or in a mix: every
+ * kernel used reduces in an order fixed by the request's own shape. */
+
+typedef enum gbblas_op {
+  GBBLAS_OP_MTM = 0, /* C += A * B   (A M x K, B K x N, C M x N; all of layout `layout`) */
+  GBBLAS_OP_MTV = 1, /* y  = A * x   (amt::mtv semantics; A M x N of layout `layout`) */
+  GBBLAS_OP_VTM = 2, /* y  = v^T A   (amt::vtm semantics) */
+  GBBLAS_OP_DOT = 3  /* *C = A . B   (n = M elements) */
+} gbblas_op;
+
+typedef enum gbblas_dtype { GBBLAS_F32 = 0, GBBLAS_F64 = 1 } gbblas_dtype;
+
+typedef struct gbblas_request {
+  int32_t op;       /* gbblas_op */
+  int32_t dtype;    /* gbblas_dtype */
+  int32_t accuracy; /* gbblas_accuracy, float MTM only (AUTO = six-product split-BF16) */
+  int32_t layout;   /* gbblas_layout of the matrices */
+  int64_t M, N, K;
+  const void* A; /* MTM: A;  MTV/VTM: matrix;  DOT: a */
+  const void* B; /* MTM: B;  MTV/VTM: x or v;  DOT: b */
+  void* C;       /* MTM: C;  MTV/VTM: y;       DOT: 1-element result */
+} gbblas_request;
+
+typedef struct gbblas_server_config {
+  int32_t streams;       /* rounds in flight at once (default 4) */
+  int32_t max_group;     /* requests per round (default 256) */
+  int64_t budget_bytes;  /* admission budget: operands + results + scratch of
+                            requests in flight (default 64 GiB) */
+  int64_t scratch_bytes; /* per-stream scratch reserved at start (default 1 GiB) */
+} gbblas_server_config;
+
+typedef struct gbblas_server_stats {
+  int64_t submitted, completed, rejected, rounds;
+  int64_t peak_inflight_bytes;
+  double mean_round_size;
+} gbblas_server_stats;
+
+typedef struct gbblas_server_s* gbblas_server;
+
+/* cfg may be NULL (defaults).  The server belongs to the current device. */
+gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_server* out);
+/* Device memory from the server's pool (stream-ordered, kept resident). */
+gbblas_status gbblas_server_alloc(gbblas_server s, int64_t bytes, void** ptr);
+gbblas_status gbblas_server_free(gbblas_server s, void* ptr);
+/* Enqueue; returns at once with a ticket.  Shape errors are reported here. */
+gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uint64_t* ticket);
+/* Block until the ticket's request is done; latency = completion - submit. */
+gbblas_status gbblas_server_wait(gbblas_server s, uint64_t ticket, double* latency_s);
+/* Submit reqs[i] at arrival_s[i] seconds after the call (non-decreasing),
+ * from a native thread, wait for all, and write each latency (seconds). */
+gbblas_status gbblas_server_run_trace(gbblas_server s, const gbblas_request* reqs, const double* arrival_s,
+                                      int64_t n, double* latency_s);
+gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out);
+gbblas_status gbblas_server_destroy(gbblas_server s);
+
 /* ------------------------------------------------ host-buffer entry points
  * Same operations on HOST pointers: inputs are copied to the device, the
  * kernel runs, outputs come back, and the call returns when host memory

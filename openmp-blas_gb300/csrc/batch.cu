@@ -218,9 +218,10 @@ gbblas_status launch_gemv_group_plan(DeviceCtx* c, const GemvGroupPlan& pl, cuda
 // Rows per warp item for a set of GEMVs, from the autotuner.
 int tuned_gemv_group_rows(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count);
 
-gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s) {
+gbblas_status launch_gemv_group_rows_fixed(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s,
+                                           int R) {
   GemvGroupPlan pl;
-  GB_TRY(plan_gemv_group(d, count, tuned_gemv_group_rows(c, d, count), pl));
+  GB_TRY(plan_gemv_group(d, count, R, pl));
   if (!pl.rows.empty()) {
     void* scratch = nullptr;
     GB_TRY(get_scratch(c, s, kScratchZeroBytes + sizeof(GemvRowsProblem) * pl.rows.size(), &scratch));
@@ -229,6 +230,10 @@ gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t
                                 cudaMemcpyHostToDevice, s));
   }
   return launch_gemv_group_plan(c, pl, s);
+}
+
+gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s) {
+  return launch_gemv_group_rows_fixed(c, d, count, s, tuned_gemv_group_rows(c, d, count));
 }
 
 // Time the row-streaming group kernel with R rows per item on the given

@@ -1,0 +1,441 @@
+// serve.cu - request loop with continuous batching (gbblas_server_*).
+//
+// Threads:
+//   callers    gbblas_server_submit (any thread) appends to the pending FIFO;
+//   scheduler  one native thread: admits pending requests in arrival order
+//              while their working set fits the HBM budget and one of the
+//              `streams` slots is free, coalesces the admitted ones into a
+//              round - split-BF16 GEMMs in one grouped tensor-core launch,
+//              float GEMVs in one grouped launch, FP64 / FMA GEMMs and dots
+//              as their own kernels - and enqueues the round on a free
+//              stream followed by a host function;
+//   CUDA       the host function runs when the round's work is done, stamps
+//              its requests complete and hands the round back.
+// Rounds on different streams overlap on the device; a request that arrives
+// while others run joins the next round as soon as a slot and memory free up.
+// Operands come from a CUDA memory pool owned by the server (kept resident).
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gbblas {
+
+gbblas_status launch_gemv_group_rows_fixed(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s,
+                                           int R);
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+  gbblas_request r{};
+  int64_t bytes = 0;
+  Clock::time_point t_submit, t_done;
+  bool done = false;
+  gbblas_status status = GBBLAS_STATUS_SUCCESS;
+};
+
+struct Round {
+  void* srv = nullptr;  // the owning gbblas_server_s
+  std::vector<Req*> reqs;
+  int64_t bytes = 0;
+  int stream_slot = 0;
+  gbblas_status status = GBBLAS_STATUS_SUCCESS;
+};
+
+int64_t round_up64(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Device bytes a request holds while in flight: operands, result, and the
+// split-BF16 arena of a tensor-core GEMM.
+int64_t working_set(const gbblas_request& r) {
+  const int64_t s = r.dtype == GBBLAS_F64 ? 8 : 4;
+  switch (r.op) {
+    case GBBLAS_OP_MTM: {
+      int64_t b = (r.M * r.K + r.K * r.N + r.M * r.N) * s;
+      if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32) {
+        const int64_t pieces = r.accuracy == GBBLAS_ACCURACY_BF16X3 ? 2 : 3;
+        b += pieces * 2 * (round_up64(r.M, 128) + round_up64(r.N, 128)) * round_up64(r.K, 64);
+      }
+      return b;
+    }
+    case GBBLAS_OP_MTV:
+    case GBBLAS_OP_VTM:
+      return (r.M * r.N + r.M + r.N) * s;
+    default:
+      return 2 * r.M * s + s;
+  }
+}
+
+}  // namespace
+}  // namespace gbblas
+
+using namespace gbblas;
+
+struct gbblas_server_s {
+  DeviceCtx* ctx = nullptr;
+  int device = 0;
+  gbblas_server_config cfg{};
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t alloc_stream = nullptr;
+  std::vector<cudaStream_t> streams;
+  std::vector<bool> slot_busy;
+
+  std::mutex mu;
+  std::condition_variable cv;       // scheduler wake-ups
+  std::condition_variable cv_done;  // waiters
+  std::deque<Req*> pending;
+  std::vector<std::unique_ptr<Req>> all;  // ticket -> request
+  std::vector<Round*> finished;
+  int inflight_rounds = 0;
+  int64_t inflight_bytes = 0;
+  bool budget_blocked = false;
+  bool stop = false;
+  std::thread scheduler;
+  gbblas_server_stats stats{};
+  int64_t round_reqs_total = 0;
+};
+
+namespace {
+
+void CUDART_CB on_round_done(void* p) {
+  Round* rd = static_cast<Round*>(p);
+  const auto now = Clock::now();
+  gbblas_server_s* s = static_cast<gbblas_server_s*>(rd->srv);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Req* q : rd->reqs) q->t_done = now;
+    s->finished.push_back(rd);
+  }
+  s->cv.notify_one();
+}
+
+// Enqueue one round on `st` (scheduler thread, no lock held).
+gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
+  DeviceCtx* c = s->ctx;
+  std::vector<gbblas_gemm_desc> split3, split2;
+  std::vector<gbblas_gemv_desc> gemv;
+  gbblas_status first_err = GBBLAS_STATUS_SUCCESS;
+  auto note = [&](gbblas_status e) {
+    if (e != GBBLAS_STATUS_SUCCESS && first_err == GBBLAS_STATUS_SUCCESS) first_err = e;
+  };
+  for (Req* q : rd->reqs) {
+    const gbblas_request& r = q->r;
+    const bool row = r.layout == GBBLAS_LAST_ORDER;
+    if (r.op == GBBLAS_OP_MTM) {
+      const int64_t rsa = row ? r.K : 1, csa = row ? 1 : r.M, rsb = row ? r.N : 1, csb = row ? 1 : r.K,
+                    rsc = row ? r.N : 1, csc = row ? 1 : r.M;
+      if (r.dtype == GBBLAS_F64) {
+        note(launch_gemm_fma<double>(c, r.M, r.N, r.K, static_cast<const double*>(r.A), rsa, csa,
+                                     static_cast<const double*>(r.B), rsb, csb, static_cast<double*>(r.C), rsc,
+                                     csc, st));
+      } else if (r.accuracy == GBBLAS_ACCURACY_FP32) {
+        note(launch_gemm_fma<float>(c, r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa,
+                                    static_cast<const float*>(r.B), rsb, csb, static_cast<float*>(r.C), rsc, csc,
+                                    st));
+      } else {
+        gbblas_gemm_desc d{r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa, static_cast<const float*>(r.B),
+                           rsb, csb, static_cast<float*>(r.C), rsc, csc};
+        (r.accuracy == GBBLAS_ACCURACY_BF16X3 ? split2 : split3).push_back(d);
+      }
+    } else if (r.op == GBBLAS_OP_MTV || r.op == GBBLAS_OP_VTM) {
+      const bool tr = r.op == GBBLAS_OP_VTM;
+      // amt::mtv: column-major accumulates; amt::vtm: row-major accumulates
+      const bool acc = tr ? row : !row;
+      if (r.dtype == GBBLAS_F32) {
+        gbblas_gemv_desc d{r.layout, tr ? 1 : 0, acc ? 1 : 0, 0, r.M, r.N, static_cast<const float*>(r.A),
+                           static_cast<const float*>(r.B), static_cast<float*>(r.C)};
+        gemv.push_back(d);
+      } else {
+        const int64_t out_len = tr ? r.N : r.M, red_len = tr ? r.M : r.N, lda = row ? r.N : r.M;
+        const bool rows_contig = row != tr;
+        const double* A = static_cast<const double*>(r.A);
+        const double* x = static_cast<const double*>(r.B);
+        double* y = static_cast<double*>(r.C);
+        note(rows_contig ? launch_gemv_rows<double>(c, out_len, red_len, A, lda, x, y, acc, st)
+                         : launch_gemv_cols<double>(c, out_len, red_len, A, lda, x, y, acc, st));
+      }
+    } else {
+      if (r.dtype == GBBLAS_F64)
+        note(launch_dot<double>(c, r.M, static_cast<const double*>(r.A), static_cast<const double*>(r.B),
+                                static_cast<double*>(r.C), st));
+      else
+        note(launch_dot<float>(c, r.M, static_cast<const float*>(r.A), static_cast<const float*>(r.B),
+                               static_cast<float*>(r.C), st));
+    }
+  }
+  if (!split3.empty()) note(launch_gemm_split_bf16_group(c, 3, split3.data(), (int64_t)split3.size(), st));
+  if (!split2.empty()) note(launch_gemm_split_bf16_group(c, 2, split2.data(), (int64_t)split2.size(), st));
+  // fixed rows-per-item: no autotuning (timing) inside the serving loop
+  if (!gemv.empty()) note(launch_gemv_group_rows_fixed(c, gemv.data(), (int64_t)gemv.size(), st, 4));
+  rd->status = first_err;
+  cudaError_t e = cudaLaunchHostFunc(st, on_round_done, rd);
+  if (e != cudaSuccess) {
+    set_error("server: cudaLaunchHostFunc failed: %s", cudaGetErrorString(e));
+    return GBBLAS_STATUS_CUDA_ERROR;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+void scheduler_main(gbblas_server_s* s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv.wait(lk, [&] {
+      return !s->finished.empty() ||
+             (!s->pending.empty() && s->inflight_rounds < (int)s->streams.size() && !s->budget_blocked) ||
+             (s->stop && s->pending.empty() && s->inflight_rounds == 0);
+    });
+    // completions: release memory and slots, wake waiters
+    if (!s->finished.empty()) {
+      for (Round* rd : s->finished) {
+        s->inflight_bytes -= rd->bytes;
+        s->inflight_rounds--;
+        s->slot_busy[rd->stream_slot] = false;
+        for (Req* q : rd->reqs) {
+          q->status = rd->status;
+          q->done = true;
+        }
+        s->stats.completed += (int64_t)rd->reqs.size();
+        delete rd;
+      }
+      s->finished.clear();
+      s->budget_blocked = false;
+      s->cv_done.notify_all();
+    }
+    if (s->stop && s->pending.empty() && s->inflight_rounds == 0) break;
+    // admit a round while a stream slot is free
+    while (!s->pending.empty() && s->inflight_rounds < (int)s->streams.size()) {
+      Round* rd = new Round();
+      rd->srv = s;
+      while (!s->pending.empty() && (int)rd->reqs.size() < s->cfg.max_group) {
+        Req* q = s->pending.front();
+        if (s->inflight_bytes + q->bytes > s->cfg.budget_bytes) break;  // wait for memory
+        s->pending.pop_front();
+        rd->reqs.push_back(q);
+        rd->bytes += q->bytes;
+        s->inflight_bytes += q->bytes;
+      }
+      if (rd->reqs.empty()) {
+        delete rd;
+        s->budget_blocked = true;
+        break;
+      }
+      int slot = 0;
+      while (s->slot_busy[slot]) ++slot;
+      s->slot_busy[slot] = true;
+      rd->stream_slot = slot;
+      s->inflight_rounds++;
+      s->stats.rounds++;
+      s->round_reqs_total += (int64_t)rd->reqs.size();
+      if (s->inflight_bytes > s->stats.peak_inflight_bytes) s->stats.peak_inflight_bytes = s->inflight_bytes;
+      cudaStream_t st = s->streams[slot];
+      lk.unlock();
+      gbblas_status e = launch_round(s, rd, st);
+      lk.lock();
+      if (e != GBBLAS_STATUS_SUCCESS) {  // the host function never runs: finish here
+        rd->status = e;
+        s->finished.push_back(rd);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_server* out) {
+  if (!out) {
+    set_error("gbblas_server_create: null output");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  auto s = std::make_unique<gbblas_server_s>();
+  s->ctx = c;
+  s->device = c->device;
+  s->cfg.streams = 4;
+  s->cfg.max_group = 256;
+  s->cfg.budget_bytes = int64_t(64) << 30;
+  s->cfg.scratch_bytes = int64_t(1) << 30;
+  if (cfg) {
+    if (cfg->streams > 0) s->cfg.streams = cfg->streams;
+    if (cfg->max_group > 0) s->cfg.max_group = cfg->max_group;
+    if (cfg->budget_bytes > 0) s->cfg.budget_bytes = cfg->budget_bytes;
+    if (cfg->scratch_bytes > 0) s->cfg.scratch_bytes = cfg->scratch_bytes;
+  }
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = c->device;
+  GB_CUDA_TRY(cudaMemPoolCreate(&s->pool, &props));
+  uint64_t keep = UINT64_MAX;  // never trim: operands stay resident
+  GB_CUDA_TRY(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s->alloc_stream, cudaStreamNonBlocking));
+  tc_prepare(c);
+  for (int i = 0; i < s->cfg.streams; ++i) {
+    cudaStream_t st;
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    s->streams.push_back(st);
+    s->slot_busy.push_back(false);
+    void* scr = nullptr;
+    GB_TRY(get_scratch(c, st, (size_t)s->cfg.scratch_bytes, &scr));
+  }
+  for (cudaStream_t st : s->streams) GB_CUDA_TRY(cudaStreamSynchronize(st));
+  s->scheduler = std::thread(scheduler_main, s.get());
+  *out = s.release();
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_alloc(gbblas_server s, int64_t bytes, void** ptr) {
+  if (!s || !ptr || bytes < 0) {
+    set_error("gbblas_server_alloc: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  cudaError_t e = cudaMallocFromPoolAsync(ptr, (size_t)(bytes ? bytes : 1), s->pool, s->alloc_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->alloc_stream);
+  if (e != cudaSuccess) {
+    set_error("gbblas_server_alloc of %lld bytes failed: %s", (long long)bytes, cudaGetErrorString(e));
+    return GBBLAS_STATUS_ALLOC_FAILED;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_free(gbblas_server s, void* ptr) {
+  if (!s) {
+    set_error("gbblas_server_free: null server");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  if (!ptr) return GBBLAS_STATUS_SUCCESS;
+  GB_CUDA_TRY(cudaFreeAsync(ptr, s->alloc_stream));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->alloc_stream));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uint64_t* ticket) {
+  if (!s || !r || !ticket) {
+    set_error("gbblas_server_submit: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  if (r->op < GBBLAS_OP_MTM || r->op > GBBLAS_OP_DOT || (r->dtype != GBBLAS_F32 && r->dtype != GBBLAS_F64) ||
+      (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 || r->accuracy > 4 ||
+      r->accuracy == GBBLAS_ACCURACY_FP8) {
+    set_error("gbblas_server_submit: bad op, dtype, layout or accuracy");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  if (r->M < 0 || r->N < 0 || r->K < 0 || !r->A || !r->B || !r->C) {
+    set_error("gbblas_server_submit: negative size or null operand");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  auto q = std::make_unique<Req>();
+  q->r = *r;
+  q->bytes = working_set(*r);
+  if (q->bytes > s->cfg.budget_bytes) {
+    set_error("gbblas_server_submit: request needs %lld bytes, the budget is %lld", (long long)q->bytes,
+              (long long)s->cfg.budget_bytes);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stats.rejected++;
+    return GBBLAS_STATUS_ALLOC_FAILED;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    q->t_submit = Clock::now();
+    *ticket = (uint64_t)s->all.size();
+    s->pending.push_back(q.get());
+    s->all.push_back(std::move(q));
+    s->stats.submitted++;
+  }
+  s->cv.notify_one();
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_wait(gbblas_server s, uint64_t ticket, double* latency_s) {
+  if (!s) {
+    set_error("gbblas_server_wait: null server");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (ticket >= s->all.size()) {
+    set_error("gbblas_server_wait: unknown ticket");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  Req* q = s->all[ticket].get();
+  s->cv_done.wait(lk, [&] { return q->done; });
+  if (latency_s) latency_s[0] = std::chrono::duration<double>(q->t_done - q->t_submit).count();
+  if (q->status != GBBLAS_STATUS_SUCCESS) set_error("gbblas_server: request %llu failed", (unsigned long long)ticket);
+  return q->status;
+}
+
+gbblas_status gbblas_server_run_trace(gbblas_server s, const gbblas_request* reqs, const double* arrival_s, int64_t n,
+                                      double* latency_s) {
+  if (!s || n < 0 || (n > 0 && (!reqs || !arrival_s))) {
+    set_error("gbblas_server_run_trace: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  std::vector<uint64_t> tickets((size_t)n);
+  std::vector<gbblas_status> sub((size_t)n, GBBLAS_STATUS_SUCCESS);
+  const auto t0 = Clock::now();
+  std::thread submitter([&] {
+    cudaSetDevice(s->device);
+    for (int64_t i = 0; i < n; ++i) {
+      const auto target = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
+      if (Clock::now() + std::chrono::microseconds(200) < target)
+        std::this_thread::sleep_until(target - std::chrono::microseconds(100));
+      while (Clock::now() < target) {
+      }
+      sub[(size_t)i] = gbblas_server_submit(s, &reqs[i], &tickets[(size_t)i]);
+    }
+  });
+  submitter.join();
+  gbblas_status st = GBBLAS_STATUS_SUCCESS;
+  for (int64_t i = 0; i < n; ++i) {
+    double lat = -1.0;
+    gbblas_status e = sub[(size_t)i];
+    if (e == GBBLAS_STATUS_SUCCESS) e = gbblas_server_wait(s, tickets[(size_t)i], &lat);
+    if (latency_s) latency_s[i] = e == GBBLAS_STATUS_SUCCESS ? lat : -1.0;
+    if (e != GBBLAS_STATUS_SUCCESS && st == GBBLAS_STATUS_SUCCESS) st = e;
+  }
+  return st;
+}
+
+gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out) {
+  if (!s || !out) {
+    set_error("gbblas_server_get_stats: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  *out = s->stats;
+  out->mean_round_size = s->stats.rounds ? (double)s->round_reqs_total / (double)s->stats.rounds : 0.0;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_destroy(gbblas_server s) {
+  if (!s) return GBBLAS_STATUS_SUCCESS;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  if (s->scheduler.joinable()) s->scheduler.join();
+  for (cudaStream_t st : s->streams) {
+    cudaStreamSynchronize(st);
+    release_scratch(s->ctx, st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  if (s->alloc_stream) {
+    cudaStreamSynchronize(s->alloc_stream);
+    cudaStreamDestroy(s->alloc_stream);
+  }
+  if (s->pool) cudaMemPoolDestroy(s->pool);
+  delete s;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+}  // extern "C"

@@ -62,6 +62,14 @@ SIGNATURES = {
     "gbblas_batch_run": (_int, [_vp, _vp]),
     "gbblas_batch_sync": (_int, [_vp]),
     "gbblas_batch_destroy": (_int, [_vp]),
+    "gbblas_server_create": (_int, [_vp, _vp]),
+    "gbblas_server_alloc": (_int, [_vp, _i64, _vp]),
+    "gbblas_server_free": (_int, [_vp, _vp]),
+    "gbblas_server_submit": (_int, [_vp, _vp, _vp]),
+    "gbblas_server_wait": (_int, [_vp, ctypes.c_uint64, _vp]),
+    "gbblas_server_run_trace": (_int, [_vp, _vp, _vp, _i64, _vp]),
+    "gbblas_server_get_stats": (_int, [_vp, _vp]),
+    "gbblas_server_destroy": (_int, [_vp]),
     "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
     "gbblas_dgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
     "gbblas_smtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
@@ -236,6 +244,82 @@ class Batch:
     def close(self):
         if self.handle:
             call("gbblas_batch_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- serving
+
+OP_MTM, OP_MTV, OP_VTM, OP_DOT = 0, 1, 2, 3
+F32, F64 = 0, 1
+
+
+class Request(ctypes.Structure):
+    """gbblas_request (device pointers)."""
+    _fields_ = [("op", ctypes.c_int32), ("dtype", ctypes.c_int32), ("accuracy", ctypes.c_int32),
+                ("layout", ctypes.c_int32), ("M", _i64), ("N", _i64), ("K", _i64),
+                ("A", _vp), ("B", _vp), ("C", _vp)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("streams", ctypes.c_int32), ("max_group", ctypes.c_int32), ("budget_bytes", _i64),
+                ("scratch_bytes", _i64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", _i64), ("completed", _i64), ("rejected", _i64), ("rounds", _i64),
+                ("peak_inflight_bytes", _i64), ("mean_round_size", ctypes.c_double)]
+
+
+class Server:
+    """gbblas_server_*: continuous-batching request loop on the current device."""
+
+    def __init__(self, streams=0, max_group=0, budget_bytes=0, scratch_bytes=0):
+        cfg = ServerConfig(streams, max_group, budget_bytes, scratch_bytes)
+        h = ctypes.c_void_p()
+        call("gbblas_server_create", ctypes.byref(cfg), ctypes.byref(h))
+        self.handle = h
+
+    def alloc(self, nbytes: int) -> int:
+        p = ctypes.c_void_p()
+        call("gbblas_server_alloc", self.handle, nbytes, ctypes.byref(p))
+        return p.value
+
+    def free(self, ptr: int) -> None:
+        call("gbblas_server_free", self.handle, ptr)
+
+    def submit(self, req: Request) -> int:
+        t = ctypes.c_uint64()
+        call("gbblas_server_submit", self.handle, ctypes.byref(req), ctypes.byref(t))
+        return t.value
+
+    def wait(self, ticket: int) -> float:
+        lat = ctypes.c_double()
+        call("gbblas_server_wait", self.handle, ticket, ctypes.byref(lat))
+        return lat.value
+
+    def run_trace(self, reqs, arrivals):
+        import numpy as np
+        n = len(reqs)
+        arr = (Request * max(1, n))(*reqs)
+        t = np.ascontiguousarray(arrivals, dtype=np.float64)
+        lat = np.zeros(max(1, n), np.float64)
+        call("gbblas_server_run_trace", self.handle, ctypes.addressof(arr), t.ctypes.data, n, lat.ctypes.data)
+        return lat[:n]
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        call("gbblas_server_get_stats", self.handle, ctypes.byref(st))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            call("gbblas_server_destroy", self.handle)
             self.handle = None
 
     def __del__(self):
