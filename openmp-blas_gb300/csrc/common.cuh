@@ -118,10 +118,12 @@ gbblas_status launch_gemv_cols(DeviceCtx* c, int64_t rows, int64_t cols, const T
 template <typename T>
 gbblas_status launch_dot(DeviceCtx* c, int64_t n, const T* a, const T* b, T* result, cudaStream_t stream);
 
+// max_ctas > 0 caps the grid (the kernel loops over tiles), leaving SMs to
+// other streams.
 template <typename T>
 gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
-                              int64_t csc, cudaStream_t stream);
+                              int64_t csc, cudaStream_t stream, int max_ctas = 0);
 
 // C += A*B with FP32 operands split into `pieces` (2 or 3) BF16 parts and
 // the piece products summed on the tcgen05 tensor cores (gemm_tc.cu).
@@ -132,14 +134,14 @@ gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_
 // The same for a group of independent problems in one persistent launch
 // (tables and BF16 arena in the stream's scratch).
 gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
-                                           cudaStream_t stream);
+                                           cudaStream_t stream, int max_ctas = 0);
 
 // A group bound to its own device memory, for repeated (graph-captured)
 // launches: create uploads the tables once; launch only enqueues kernels.
 struct TcGroupPlan;
 gbblas_status tc_group_create(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
                               TcGroupPlan** out);
-gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream);
+gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream, int max_ctas = 0);
 void tc_group_destroy(TcGroupPlan* plan);
 int* tc_group_error_word(const TcGroupPlan* plan);
 

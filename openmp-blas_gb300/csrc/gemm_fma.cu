@@ -66,7 +66,7 @@ template <typename T, int BM, int BN, int BK, int TM, int TN, int LA, int LB>
 __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
     gemm_fma_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t rsa, int64_t csa,
                     const T* __restrict__ B, int64_t rsb, int64_t csb, T* __restrict__ C, int64_t rsc,
-                    int64_t csc) {
+                    int64_t csc, int64_t tiles_n, int64_t ntiles) {
   using CF = Cfg<T, BM, BN, BK, TM, TN>;
   using VT = typename Vec16<T>::t;
   constexpr int W = CF::W, NT = CF::NT, PAD = CF::PAD;
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
 
   const int tid = threadIdx.x;
   const int tx = tid % (BN / TN), ty = tid / (BN / TN);
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  int64_t m0 = 0, n0 = 0;  // current output tile (set per tile below)
 
   T ra[CF::AR], rb[CF::BR];
 
@@ -207,6 +207,11 @@ __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
     }
   };
 
+  // Tiles are handed out grid-stride, so a grid capped below the tile count
+  // (a caller sharing the GPU with latency-sensitive work) still covers C.
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  m0 = (tile / tiles_n) * BM;
+  n0 = (tile % tiles_n) * BN;
   T acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
@@ -270,17 +275,23 @@ __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
       }
     }
   }
+  }  // tile loop
 }
 
 template <typename T, int BM, int BN, int BK, int TM, int TN>
 gbblas_status launch_cfg(int la, int lb, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa,
                          const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, int max_ctas) {
   using CF = Cfg<T, BM, BN, BK, TM, TN>;
-  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
+  const int64_t tiles_n = (N + BN - 1) / BN, ntiles = tiles_n * ((M + BM - 1) / BM);
+  int64_t g = ntiles;
+  if (max_ctas > 0 && g > max_ctas) g = max_ctas;
+  if (g > 0x7fffffff) g = 0x7fffffff;
+  const unsigned grid = (unsigned)g;
 #define GB_L(LA_, LB_)                                                                                   \
   gemm_fma_kernel<T, BM, BN, BK, TM, TN, LA_, LB_><<<grid, CF::NT, 0, stream>>>(M, N, K, A, rsa, csa, B, \
-                                                                                rsb, csb, C, rsc, csc)
+                                                                                rsb, csb, C, rsc, csc,  \
+                                                                                tiles_n, ntiles)
   if (la == kScalar || lb == kScalar)
     GB_L(kScalar, kScalar);
   else if (la == kVecMN && lb == kVecMN)
@@ -300,7 +311,7 @@ gbblas_status launch_cfg(int la, int lb, int64_t M, int64_t N, int64_t K, const 
 template <typename T>
 gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, int max_ctas) {
   constexpr int W = Vec16<T>::w;
   // Which loader each operand can use.
   int la = kScalar, lb = kScalar;
@@ -313,25 +324,24 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
     else if (rsb == 1 && csb % W == 0) lb = kVecK;
   }
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
-  if ((M + 63) / 64 > 65535) {
-    set_error("gemm: M=%lld exceeds the grid limit", (long long)M);
-    return GBBLAS_STATUS_NOT_SUPPORTED;
-  }
   if constexpr (sizeof(T) == 4) {
     const int64_t big_tiles = ((M + 127) / 128) * ((N + 127) / 128);
     if (big_tiles >= 2 * (int64_t)c->num_sms)
-      return launch_cfg<float, 128, 128, 16, 8, 8>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream);
-    return launch_cfg<float, 64, 64, 16, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream);
+      return launch_cfg<float, 128, 128, 16, 8, 8>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
+                                                   max_ctas);
+    return launch_cfg<float, 64, 64, 16, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
+                                               max_ctas);
   } else {
-    return launch_cfg<double, 64, 64, 8, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream);
+    return launch_cfg<double, 64, 64, 8, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
+                                               max_ctas);
   }
 }
 
 template gbblas_status launch_gemm_fma<float>(DeviceCtx*, int64_t, int64_t, int64_t, const float*, int64_t,
                                               int64_t, const float*, int64_t, int64_t, float*, int64_t, int64_t,
-                                              cudaStream_t);
+                                              cudaStream_t, int);
 template gbblas_status launch_gemm_fma<double>(DeviceCtx*, int64_t, int64_t, int64_t, const double*, int64_t,
                                                int64_t, const double*, int64_t, int64_t, double*, int64_t,
-                                               int64_t, cudaStream_t);
+                                               int64_t, cudaStream_t, int);
 
 }  // namespace gbblas

@@ -591,7 +591,7 @@ gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
 }
 
 template <int P>
-gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream) {
+gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
   using CF = TcCfg<P>;
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   int* err = reinterpret_cast<int*>(pl.base + kErrWordOffset);
@@ -611,7 +611,8 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                                      (int)CF::kSmem));
     attr_set[c->device & 63] = true;
   }
-  const int grid = (int)std::min<int64_t>(pl.tiles, c->num_sms);
+  int grid = (int)std::min<int64_t>(pl.tiles, c->num_sms);
+  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
   gemm_split_kernel<P><<<grid, kThreads, CF::kSmem, stream>>>(pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
                                                              (int)pl.a_rows, (int)pl.b_rows, counter, err);
   return check_launch("gemm_split_kernel");
@@ -625,8 +626,8 @@ void tc_prepare(DeviceCtx* c) {
   cudaFuncSetAttribute(gemm_split_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<3>::kSmem);
 }
 
-gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream) {
-  return pl->pieces == 3 ? launch_bound<3>(c, *pl, stream) : launch_bound<2>(c, *pl, stream);
+gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas) {
+  return pl->pieces == 3 ? launch_bound<3>(c, *pl, stream, max_ctas) : launch_bound<2>(c, *pl, stream, max_ctas);
 }
 
 gbblas_status tc_group_create(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
@@ -673,14 +674,14 @@ int* tc_group_error_word(const TcGroupPlan* pl) {
 }
 
 gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
-                                           cudaStream_t stream) {
+                                           cudaStream_t stream, int max_ctas) {
   TcGroupPlan pl;
   GB_TRY(plan_group(pieces, descs, count, pl));
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   void* s = nullptr;
   GB_TRY(get_scratch(c, stream, pl.bytes, &s));
   GB_TRY(bind_group(pl, static_cast<char*>(s), stream));
-  return tc_group_launch(c, &pl, stream);
+  return tc_group_launch(c, &pl, stream, max_ctas);
 }
 
 gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_t N, int64_t K, const float* A,

@@ -14,6 +14,7 @@
 // Rounds on different streams overlap on the device; a request that arrives
 // while others run joins the next round as soon as a slot and memory free up.
 // Operands come from a CUDA memory pool owned by the server (kept resident).
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -36,6 +37,8 @@ using Clock = std::chrono::steady_clock;
 struct Req {
   gbblas_request r{};
   int64_t bytes = 0;
+  double est_us = 0.0;  // estimated GPU time
+  bool heavy = false;
   Clock::time_point t_submit, t_done;
   bool done = false;
   gbblas_status status = GBBLAS_STATUS_SUCCESS;
@@ -46,6 +49,8 @@ struct Round {
   std::vector<Req*> reqs;
   int64_t bytes = 0;
   int stream_slot = 0;
+  bool heavy = false;
+  int max_ctas = 0;  // grid cap for the round's GEMMs (0 = whole GPU)
   gbblas_status status = GBBLAS_STATUS_SUCCESS;
 };
 
@@ -72,6 +77,35 @@ int64_t working_set(const gbblas_request& r) {
   }
 }
 
+// Estimated GPU time (us) of a request from its flops / bytes and the rate of
+// the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP32
+// FMA ~50, FP64 ~0.8 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1 TFLOP/s).
+double estimate_us(const gbblas_request& r) {
+  const double launch = 5.0;
+  switch (r.op) {
+    case GBBLAS_OP_MTM: {
+      const double fl = 2.0 * (double)r.M * (double)r.N * (double)r.K;
+      double rate;  // flop per us
+      if (r.dtype == GBBLAS_F64)
+        rate = 0.8e6;
+      else if (r.accuracy == GBBLAS_ACCURACY_FP32)
+        rate = 50e6;
+      else if (r.accuracy == GBBLAS_ACCURACY_BF16X3)
+        rate = 430e6;
+      else
+        rate = 260e6;
+      return launch + fl / rate;
+    }
+    case GBBLAS_OP_MTV:
+    case GBBLAS_OP_VTM: {
+      const double mn = (double)r.M * (double)r.N;
+      return launch + (r.dtype == GBBLAS_F64 ? std::max(mn * 8 / 6e6, 2 * mn / 1.1e6) : mn * 4 / 6e6);
+    }
+    default:
+      return launch + 2.0 * (double)r.M * (r.dtype == GBBLAS_F64 ? 8 : 4) / 6e6;
+  }
+}
+
 }  // namespace
 }  // namespace gbblas
 
@@ -83,16 +117,20 @@ struct gbblas_server_s {
   gbblas_server_config cfg{};
   cudaMemPool_t pool = nullptr;
   cudaStream_t alloc_stream = nullptr;
-  std::vector<cudaStream_t> streams;
+  std::vector<cudaStream_t> streams;        // light rounds, high priority
   std::vector<bool> slot_busy;
+  std::vector<cudaStream_t> heavy_streams;  // heavy requests, low priority
+  std::vector<bool> heavy_busy;
 
   std::mutex mu;
   std::condition_variable cv;       // scheduler wake-ups
   std::condition_variable cv_done;  // waiters
-  std::deque<Req*> pending;
+  std::deque<Req*> pending;        // light requests, arrival order
+  std::deque<Req*> heavy_pending;  // heavy requests, arrival order
   std::vector<std::unique_ptr<Req>> all;  // ticket -> request
   std::vector<Round*> finished;
   int inflight_rounds = 0;
+  int inflight_heavy = 0;
   int64_t inflight_bytes = 0;
   bool budget_blocked = false;
   bool stop = false;
@@ -118,6 +156,7 @@ void CUDART_CB on_round_done(void* p) {
 // Enqueue one round on `st` (scheduler thread, no lock held).
 gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
   DeviceCtx* c = s->ctx;
+  const int cap = rd->max_ctas;
   std::vector<gbblas_gemm_desc> split3, split2;
   std::vector<gbblas_gemv_desc> gemv;
   gbblas_status first_err = GBBLAS_STATUS_SUCCESS;
@@ -133,11 +172,11 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
       if (r.dtype == GBBLAS_F64) {
         note(launch_gemm_fma<double>(c, r.M, r.N, r.K, static_cast<const double*>(r.A), rsa, csa,
                                      static_cast<const double*>(r.B), rsb, csb, static_cast<double*>(r.C), rsc,
-                                     csc, st));
+                                     csc, st, cap));
       } else if (r.accuracy == GBBLAS_ACCURACY_FP32) {
         note(launch_gemm_fma<float>(c, r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa,
                                     static_cast<const float*>(r.B), rsb, csb, static_cast<float*>(r.C), rsc, csc,
-                                    st));
+                                    st, cap));
       } else {
         gbblas_gemm_desc d{r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa, static_cast<const float*>(r.B),
                            rsb, csb, static_cast<float*>(r.C), rsc, csc};
@@ -169,8 +208,8 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
                                static_cast<float*>(r.C), st));
     }
   }
-  if (!split3.empty()) note(launch_gemm_split_bf16_group(c, 3, split3.data(), (int64_t)split3.size(), st));
-  if (!split2.empty()) note(launch_gemm_split_bf16_group(c, 2, split2.data(), (int64_t)split2.size(), st));
+  if (!split3.empty()) note(launch_gemm_split_bf16_group(c, 3, split3.data(), (int64_t)split3.size(), st, cap));
+  if (!split2.empty()) note(launch_gemm_split_bf16_group(c, 2, split2.data(), (int64_t)split2.size(), st, cap));
   // fixed rows-per-item: no autotuning (timing) inside the serving loop
   if (!gemv.empty()) note(launch_gemv_group_rows_fixed(c, gemv.data(), (int64_t)gemv.size(), st, 4));
   rd->status = first_err;
@@ -185,18 +224,29 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
 void scheduler_main(gbblas_server_s* s) {
   cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
+  auto light_ready = [&] {
+    return !s->pending.empty() && s->inflight_rounds < (int)s->streams.size() && !s->budget_blocked;
+  };
+  auto heavy_ready = [&] {
+    return !s->heavy_pending.empty() && s->inflight_heavy < (int)s->heavy_streams.size() && !s->budget_blocked;
+  };
   for (;;) {
     s->cv.wait(lk, [&] {
-      return !s->finished.empty() ||
-             (!s->pending.empty() && s->inflight_rounds < (int)s->streams.size() && !s->budget_blocked) ||
-             (s->stop && s->pending.empty() && s->inflight_rounds == 0);
+      return !s->finished.empty() || light_ready() || heavy_ready() ||
+             (s->stop && s->pending.empty() && s->heavy_pending.empty() && s->inflight_rounds == 0 &&
+              s->inflight_heavy == 0);
     });
     // completions: release memory and slots, wake waiters
     if (!s->finished.empty()) {
       for (Round* rd : s->finished) {
         s->inflight_bytes -= rd->bytes;
-        s->inflight_rounds--;
-        s->slot_busy[rd->stream_slot] = false;
+        if (rd->heavy) {
+          s->inflight_heavy--;
+          s->heavy_busy[rd->stream_slot] = false;
+        } else {
+          s->inflight_rounds--;
+          s->slot_busy[rd->stream_slot] = false;
+        }
         for (Req* q : rd->reqs) {
           q->status = rd->status;
           q->done = true;
@@ -208,39 +258,64 @@ void scheduler_main(gbblas_server_s* s) {
       s->budget_blocked = false;
       s->cv_done.notify_all();
     }
-    if (s->stop && s->pending.empty() && s->inflight_rounds == 0) break;
-    // admit a round while a stream slot is free
-    while (!s->pending.empty() && s->inflight_rounds < (int)s->streams.size()) {
-      Round* rd = new Round();
-      rd->srv = s;
-      while (!s->pending.empty() && (int)rd->reqs.size() < s->cfg.max_group) {
-        Req* q = s->pending.front();
-        if (s->inflight_bytes + q->bytes > s->cfg.budget_bytes) break;  // wait for memory
-        s->pending.pop_front();
-        rd->reqs.push_back(q);
-        rd->bytes += q->bytes;
-        s->inflight_bytes += q->bytes;
-      }
-      if (rd->reqs.empty()) {
-        delete rd;
-        s->budget_blocked = true;
-        break;
-      }
-      int slot = 0;
-      while (s->slot_busy[slot]) ++slot;
-      s->slot_busy[slot] = true;
-      rd->stream_slot = slot;
-      s->inflight_rounds++;
-      s->stats.rounds++;
-      s->round_reqs_total += (int64_t)rd->reqs.size();
-      if (s->inflight_bytes > s->stats.peak_inflight_bytes) s->stats.peak_inflight_bytes = s->inflight_bytes;
-      cudaStream_t st = s->streams[slot];
-      lk.unlock();
-      gbblas_status e = launch_round(s, rd, st);
-      lk.lock();
-      if (e != GBBLAS_STATUS_SUCCESS) {  // the host function never runs: finish here
-        rd->status = e;
-        s->finished.push_back(rd);
+    if (s->stop && s->pending.empty() && s->heavy_pending.empty() && s->inflight_rounds == 0 &&
+        s->inflight_heavy == 0)
+      break;
+    // Form rounds while slots are free.  Light rounds take requests in
+    // arrival order up to max_group and up to heavy_us of estimated work;
+    // a heavy request is a round by itself.
+    bool progress = true;
+    while (progress) {
+      progress = false;
+      for (int kind = 0; kind < 2; ++kind) {
+        const bool heavy = kind == 1;
+        std::deque<Req*>& q = heavy ? s->heavy_pending : s->pending;
+        const int cap = heavy ? (int)s->heavy_streams.size() : (int)s->streams.size();
+        int& inflight = heavy ? s->inflight_heavy : s->inflight_rounds;
+        if (q.empty() || inflight >= cap || s->budget_blocked) continue;
+        Round* rd = new Round();
+        rd->srv = s;
+        rd->heavy = heavy;
+        double est = 0.0;
+        while (!q.empty() && (int)rd->reqs.size() < (heavy ? 1 : s->cfg.max_group)) {
+          Req* r = q.front();
+          if (s->inflight_bytes + r->bytes > s->cfg.budget_bytes) break;  // wait for memory
+          if (!rd->reqs.empty() && est + r->est_us > (double)s->cfg.heavy_us) break;
+          q.pop_front();
+          rd->reqs.push_back(r);
+          rd->bytes += r->bytes;
+          est += r->est_us;
+          s->inflight_bytes += r->bytes;
+        }
+        if (rd->reqs.empty()) {
+          delete rd;
+          s->budget_blocked = true;
+          continue;
+        }
+        std::vector<bool>& busy = heavy ? s->heavy_busy : s->slot_busy;
+        int slot = 0;
+        while (busy[slot]) ++slot;
+        busy[slot] = true;
+        rd->stream_slot = slot;
+        inflight++;
+        s->stats.rounds++;
+        s->round_reqs_total += (int64_t)rd->reqs.size();
+        if (s->inflight_bytes > s->stats.peak_inflight_bytes) s->stats.peak_inflight_bytes = s->inflight_bytes;
+        // A heavy round's CTAs run for milliseconds and are not preempted by
+        // higher-priority streams: while light work is waiting or running,
+        // cap its grid at three quarters of the SMs so light rounds keep a
+        // quarter of the GPU; on an otherwise idle GPU it gets every SM.
+        if (heavy && (!s->pending.empty() || s->inflight_rounds > 0))
+          rd->max_ctas = std::max(1, s->ctx->num_sms * 3 / 4);
+        cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
+        lk.unlock();
+        gbblas_status e = launch_round(s, rd, st);
+        lk.lock();
+        if (e != GBBLAS_STATUS_SUCCESS) {  // the host function never runs: finish here
+          rd->status = e;
+          s->finished.push_back(rd);
+        }
+        progress = true;
       }
     }
   }
@@ -264,7 +339,11 @@ gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_serve
   s->cfg.max_group = 256;
   s->cfg.budget_bytes = int64_t(64) << 30;
   s->cfg.scratch_bytes = int64_t(1) << 30;
+  s->cfg.heavy_streams = 2;
+  s->cfg.heavy_us = 1000;
   if (cfg) {
+    if (cfg->heavy_streams > 0) s->cfg.heavy_streams = cfg->heavy_streams;
+    if (cfg->heavy_us > 0) s->cfg.heavy_us = cfg->heavy_us;
     if (cfg->streams > 0) s->cfg.streams = cfg->streams;
     if (cfg->max_group > 0) s->cfg.max_group = cfg->max_group;
     if (cfg->budget_bytes > 0) s->cfg.budget_bytes = cfg->budget_bytes;
@@ -279,15 +358,19 @@ gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_serve
   GB_CUDA_TRY(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s->alloc_stream, cudaStreamNonBlocking));
   tc_prepare(c);
-  for (int i = 0; i < s->cfg.streams; ++i) {
+  int prio_low = 0, prio_high = 0;  // numerically: low priority >= high priority
+  GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  for (int i = 0; i < s->cfg.streams + s->cfg.heavy_streams; ++i) {
+    const bool heavy = i >= s->cfg.streams;
     cudaStream_t st;
-    GB_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    s->streams.push_back(st);
-    s->slot_busy.push_back(false);
+    GB_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, heavy ? prio_low : prio_high));
+    (heavy ? s->heavy_streams : s->streams).push_back(st);
+    (heavy ? s->heavy_busy : s->slot_busy).push_back(false);
     void* scr = nullptr;
     GB_TRY(get_scratch(c, st, (size_t)s->cfg.scratch_bytes, &scr));
   }
   for (cudaStream_t st : s->streams) GB_CUDA_TRY(cudaStreamSynchronize(st));
+  for (cudaStream_t st : s->heavy_streams) GB_CUDA_TRY(cudaStreamSynchronize(st));
   s->scheduler = std::thread(scheduler_main, s.get());
   *out = s.release();
   return GBBLAS_STATUS_SUCCESS;
@@ -336,6 +419,8 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
   auto q = std::make_unique<Req>();
   q->r = *r;
   q->bytes = working_set(*r);
+  q->est_us = estimate_us(*r);
+  q->heavy = q->est_us > (double)s->cfg.heavy_us;
   if (q->bytes > s->cfg.budget_bytes) {
     set_error("gbblas_server_submit: request needs %lld bytes, the budget is %lld", (long long)q->bytes,
               (long long)s->cfg.budget_bytes);
@@ -347,7 +432,7 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
     std::lock_guard<std::mutex> lk(s->mu);
     q->t_submit = Clock::now();
     *ticket = (uint64_t)s->all.size();
-    s->pending.push_back(q.get());
+    (q->heavy ? s->heavy_pending : s->pending).push_back(q.get());
     s->all.push_back(std::move(q));
     s->stats.submitted++;
   }
@@ -423,7 +508,9 @@ gbblas_status gbblas_server_destroy(gbblas_server s) {
   }
   s->cv.notify_all();
   if (s->scheduler.joinable()) s->scheduler.join();
-  for (cudaStream_t st : s->streams) {
+  std::vector<cudaStream_t> all_streams = s->streams;
+  all_streams.insert(all_streams.end(), s->heavy_streams.begin(), s->heavy_streams.end());
+  for (cudaStream_t st : all_streams) {
     cudaStreamSynchronize(st);
     release_scratch(s->ctx, st);
     cudaStreamSynchronize(st);
