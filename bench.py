@@ -465,7 +465,8 @@ def run_reference(args):
 
 def run_precision(args):
     """The precision configuration: C = A*B, M = N = K = 8192 from float32,
-    as split-BF16 (three tcgen05 products) and plain FP32 (FMA pipe), on two
+    as split-BF16 (three or six tcgen05 products), FP8-E4M3 with per-128
+    K-block scales (tcgen05 kind::f8f6f4) and plain FP32 (FMA pipe), on two
     input sets (U[-1,1) and wide-range s*m*2^e, e in [-10, 10]); TFLOP/s of
     2*M*N*K algorithmic flops and max / mean relative error against
     long-double dots on sampled entries.  One JSON line per (path, set)."""
@@ -485,6 +486,8 @@ def run_precision(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     for set_name in ("uniform", "wide"):
+        if set_name not in args.sets.split(","):
+            continue
         if set_name == "uniform":
             A = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
             B = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
@@ -497,7 +500,9 @@ def run_precision(args):
             A, B = wide(), wide()
         An, Bn = A.cpu().numpy(), B.cpu().numpy()
         exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
-        for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp32", 0)):
+        for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp8", 2), ("fp32", 0)):
+            if path not in args.paths.split(","):
+                continue
             C = torch.zeros(n, n, device="cuda")
             sp = torch.cuda.current_stream().cuda_stream or None
 
@@ -526,7 +531,7 @@ def run_precision(args):
             rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
             normwise = np.abs(got - exact) / absx
             tf = flops / (ms / 1e3) / 1e12
-            line = {"metric": "FP32-accurate GEMM TFLOP/s", "path": path, "input_set": set_name,
+            line = {"metric": "GEMM TFLOP/s (float32 operands)", "path": path, "input_set": set_name,
                     "value": round(tf, 2), "unit": "TFLOP/s", "ms_per_gemm": round(ms, 3), "M": n, "N": n, "K": n,
                     "flops": "2*M*N*K algorithmic", "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
                     "max_normwise_err": float(normwise.max()), "error_sample": f"{sample} entries vs long double",
@@ -536,6 +541,10 @@ def run_precision(args):
                 line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
                 line["tensor_peak"] = (f"{products} BF16 products per algorithmic flop vs bf16_tflops "
                                        f"{peaks['bf16_tflops']} (measured, burst)")
+            if path == "fp8" and peaks.get("bf16_tflops"):
+                line["tensor_frac"] = round(tf / (2 * peaks["bf16_tflops"]), 4)
+                line["tensor_peak"] = (f"2 x bf16_tflops {peaks['bf16_tflops']} (measured BF16 burst times the "
+                                       "nominal FP8/BF16 ratio; no FP8 peak is measured)")
             print(json.dumps(line), flush=True)
         del A, B
 
@@ -810,6 +819,9 @@ def main():
     ap.add_argument("--batch-accuracy", default="bf16x3", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--gemm-n", type=int, default=8192)
     ap.add_argument("--gemm-iters", type=int, default=5)
+    ap.add_argument("--paths", default="bf16x3,bf16x6,fp8,fp32",
+                    help="precision workload: comma-separated GEMM paths to run")
+    ap.add_argument("--sets", default="uniform,wide", help="precision workload: input sets to run")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)

@@ -60,8 +60,11 @@ typedef enum gbblas_accuracy {
   GBBLAS_ACCURACY_BF16X3 = 1, /* a = hi + lo in BF16, hi*hi + hi*lo + lo*hi on tcgen05
                                  tensor cores, FP32 accumulation in TMEM: ~16 significand
                                  bits per product, fastest FP32-input path */
-  GBBLAS_ACCURACY_FP8 = 2,    /* low accuracy: E4M3 operands with one scale per 128
-                                 elements along K, FP32 accumulation */
+  GBBLAS_ACCURACY_FP8 = 2,    /* low accuracy: E4M3 operands with one power-of-two
+                                 scale per 128 elements along K (per row of A, per
+                                 column of B), kind::f8f6f4 tcgen05 products, FP32
+                                 accumulation; ~3 significand bits per operand and
+                                 values below 2^-9 of their block's max flush to 0 */
   GBBLAS_ACCURACY_AUTO = 3,   /* BF16X6 where the shape suits the tensor-core tiles,
                                  FP32 otherwise */
   GBBLAS_ACCURACY_BF16X6 = 4  /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
@@ -222,9 +225,9 @@ typedef struct gbblas_gemv_desc {
   float* y;
 } gbblas_gemv_desc;
 
-/* All GEMMs in one persistent tensor-core launch (accuracy BF16X3, BF16X6 or
- * AUTO = BF16X6; FP32 runs them one by one on the CUDA cores).  Problems may
- * not overlap their C. */
+/* All GEMMs in one persistent tensor-core launch (accuracy BF16X3, BF16X6,
+ * FP8 or AUTO = BF16X6; FP32 runs them one by one on the CUDA cores).
+ * Problems may not overlap their C. */
 gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count, gbblas_accuracy accuracy,
                                    void* stream);
 

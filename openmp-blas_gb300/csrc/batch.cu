@@ -334,9 +334,9 @@ gbblas_status gbblas_batch_create(const gbblas_gemm_desc* gemms, int64_t ngemm, 
     set_error("gbblas_batch_create: bad arguments");
     return GBBLAS_STATUS_INVALID_VALUE;
   }
-  if ((int)accuracy < 0 || (int)accuracy > 4 || accuracy == GBBLAS_ACCURACY_FP8) {
-    set_error("gbblas_batch_create: accuracy %d is not available for batches", (int)accuracy);
-    return GBBLAS_STATUS_NOT_SUPPORTED;
+  if ((int)accuracy < 0 || (int)accuracy > 4) {
+    set_error("gbblas_batch_create: unknown accuracy %d", (int)accuracy);
+    return GBBLAS_STATUS_INVALID_VALUE;
   }
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
@@ -351,8 +351,9 @@ gbblas_status gbblas_batch_create(const gbblas_gemm_desc* gemms, int64_t ngemm, 
     if (accuracy == GBBLAS_ACCURACY_FP32) {
       b->fma_gemms.assign(gemms, gemms + ngemm);
     } else {
-      const int pieces = accuracy == GBBLAS_ACCURACY_BF16X3 ? 2 : 3;
-      if ((st = tc_group_create(c, pieces, gemms, ngemm, &b->gemm)) != GBBLAS_STATUS_SUCCESS) return fail(st);
+      // AUTO in a batch: the FP32-accurate six-product split
+      const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode(accuracy);
+      if ((st = tc_group_create(c, mode, gemms, ngemm, &b->gemm)) != GBBLAS_STATUS_SUCCESS) return fail(st);
     }
   }
   if (ngemv > 0) {

@@ -204,13 +204,12 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
                        cudaStream_t s) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if constexpr (std::is_same_v<T, float>) {
-    if (acc == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm: FP8 accuracy is not available");
-    if (acc == GBBLAS_ACCURACY_BF16X3)
-      return launch_gemm_split_bf16(c, 2, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
-    // AUTO: whichever FP32-accurate path the autotuner measured faster for
-    // this shape bucket (FMA kernel or split-BF16 with six products).
-    if (acc == GBBLAS_ACCURACY_BF16X6 || (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1))
-      return launch_gemm_split_bf16(c, 3, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    // BF16X3 / BF16X6 / FP8 always take the tensor cores.  AUTO: whichever
+    // FP32-accurate path the autotuner measured faster for this shape bucket
+    // (FMA kernel or split-BF16 with six products).
+    int mode = tc_mode(acc);
+    if (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1) mode = tc_mode(GBBLAS_ACCURACY_BF16X6);
+    if (mode != 0) return launch_gemm_tc(c, mode, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
   }
   return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
 }
@@ -450,7 +449,6 @@ gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count,
   if (count < 0 || (count > 0 && !descs)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: bad arguments");
   if ((int)accuracy < 0 || (int)accuracy > 4)
     return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: unknown accuracy %d", (int)accuracy);
-  if (accuracy == GBBLAS_ACCURACY_FP8) return bad(GBBLAS_STATUS_NOT_SUPPORTED, "gemm_grouped: FP8 is not available");
   for (int64_t i = 0; i < count; ++i) {
     const gbblas_gemm_desc& g = descs[i];
     GB_TRY(check_gemm<float>(g.M, g.N, g.K, g.A, g.rsa, g.csa, g.B, g.rsb, g.csb, g.C, g.rsc, g.csc));
@@ -466,7 +464,9 @@ gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count,
     }
     return GBBLAS_STATUS_SUCCESS;
   }
-  return launch_gemm_split_bf16_group(c, accuracy == GBBLAS_ACCURACY_BF16X3 ? 2 : 3, descs, count, s);
+  // AUTO in a group: the six-product split (FP32-accurate on the tensor cores)
+  const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode(accuracy);
+  return launch_gemm_tc_group(c, mode, descs, count, s);
 }
 
 gbblas_status gbblas_sgemv_grouped(const gbblas_gemv_desc* descs, int64_t count, void* stream) {

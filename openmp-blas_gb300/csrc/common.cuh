@@ -125,21 +125,26 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
                               int64_t csc, cudaStream_t stream, int max_ctas = 0);
 
-// C += A*B with FP32 operands split into `pieces` (2 or 3) BF16 parts and
-// the piece products summed on the tcgen05 tensor cores (gemm_tc.cu).
-gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_t N, int64_t K, const float* A,
-                                     int64_t rsa, int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C,
-                                     int64_t rsc, int64_t csc, cudaStream_t stream);
+// C += A*B on the tcgen05 tensor cores (gemm_tc.cu).  mode = tc_mode(acc):
+// 2 / 3 = FP32 operands split into that many BF16 pieces, 8 = FP8-E4M3 with
+// per-128-K-block power-of-two scales; 0 = not a tensor-core accuracy.
+int tc_mode(gbblas_accuracy acc);
+// Device bytes of the operand arena one problem needs in `mode`.
+size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K);
+
+gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
+                             int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
+                             int64_t csc, cudaStream_t stream);
 
 // The same for a group of independent problems in one persistent launch
-// (tables and BF16 arena in the stream's scratch).
-gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
-                                           cudaStream_t stream, int max_ctas = 0);
+// (tables and operand arena in the stream's scratch).
+gbblas_status launch_gemm_tc_group(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
+                                   cudaStream_t stream, int max_ctas = 0);
 
 // A group bound to its own device memory, for repeated (graph-captured)
 // launches: create uploads the tables once; launch only enqueues kernels.
 struct TcGroupPlan;
-gbblas_status tc_group_create(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
+gbblas_status tc_group_create(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
                               TcGroupPlan** out);
 gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream, int max_ctas = 0);
 void tc_group_destroy(TcGroupPlan* plan);

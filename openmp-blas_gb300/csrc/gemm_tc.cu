@@ -1,53 +1,64 @@
-// gemm_tc.cu - FP32-accurate GEMM on the 5th-generation tensor cores
-// (split-BF16), single and grouped.  C += A * B for float A, B, C of any
-// layout; a group is any number of independent problems of any shapes.
+// gemm_tc.cu - GEMM on the 5th-generation tensor cores, single and grouped:
+// FP32-accurate (split-BF16) and low-accuracy (FP8-E4M3, block-scaled).
+// C += A * B for float A, B, C of any layout; a group is any number of
+// independent problems of any shapes.
 //
-//   1. split_group_kernel: every FP32 operand element a becomes P BF16 pieces
-//      p0 = bf16_rn(a), p1 = bf16_rn(a - p0), p2 = bf16_rn(a - p0 - p1),
-//      written K-major (A as M x K, B as its transpose N x K) into one arena
-//      per operand kind: all problems' rows stacked, one common K pitch,
-//      piece planes one after another.  One pair of TMA tensor maps then
-//      covers every problem of the group.
+//   1. Operand preparation, written K-major (A as M x K, B as its transpose
+//      N x K) into one arena per operand kind: all problems' rows stacked,
+//      one common K pitch.  One pair of TMA tensor maps then covers every
+//      problem of the group.
+//      prep_group_kernel, split-BF16: every FP32 element a becomes P BF16 pieces
+//        p0 = bf16_rn(a), p1 = bf16_rn(a - p0), p2 = bf16_rn(a - p0 - p1),
+//        piece planes one after another.
+//      prep_group_kernel, FP8: every 128-element K-block of a row becomes
+//        128 E4M3 values and one power-of-two FP32 scale (scale planes stored
+//        K-block-major beside the arena).
 //   2. gemm_split_kernel (persistent, one CTA per SM): a device-side tile
 //      scheduler hands out 128 x 128 output tiles of all problems (largest K
-//      first) through an atomic counter.  Per tile: C += sum of the piece
-//      products p_i(A) p_j(B) with i + j < P by tcgen05.mma (kind::f16, BF16
-//      in, FP32 accumulate) into two TMEM accumulators - p0*p0 alone, and
-//      every smaller product together (so small terms are summed at their own
-//      scale).  K is walked in chunks of 512: each chunk accumulates in one of
-//      two TMEM buffers while the epilogue warps fold the previous chunk into
-//      FP32 registers with round-to-nearest adds (the tensor core's own
-//      accumulation over long K is measurably less accurate than FP32); the
+//      first) through an atomic counter.  K is walked in chunks: each chunk
+//      accumulates in one of two TMEM buffers while the epilogue warps fold
+//      the previous chunk into FP32 registers with round-to-nearest adds; the
 //      registers go into C once per tile.  The chunk buffers carry over from
 //      tile to tile, so a tile's epilogue overlaps the next tile's MMAs.
+//      Split-BF16 (tcgen05.mma kind::f16, BF16 in, FP32 accumulate): C += sum
+//      of the piece products p_i(A) p_j(B) with i + j < P, into two TMEM
+//      accumulators - p0*p0 alone, and every smaller product together (so
+//      small terms are summed at their own scale); chunks of 512 K (the
+//      tensor core's own accumulation over long K is measurably less accurate
+//      than FP32).
 //        P = 2 ("bf16x3"):  p0p0 + (p0p1 + p1p0)                     3 MMAs
 //        P = 3 ("bf16x6"):  p0p0 + (p0p1 + p1p0 + p0p2 + p1p1 + p2p0) 6 MMAs
 //      Three pieces hold all 24 significand bits of an FP32 value and the
 //      dropped products are below 2^-23 of |a||b|: bf16x6 is at least as
 //      accurate as FP32 FMA arithmetic.  bf16x3 keeps about 16 bits.
+//      FP8 (tcgen05.mma kind::f8f6f4, E4M3 in, FP32 accumulate): one chunk
+//      per 128-K scale block; the epilogue adds partial * sa(row) * sb(col).
 //
-// Warp roles (192 threads):
+// Warp roles (192 threads; FP8: 320):
 //   warp 0      tile scheduler + TMA producer: takes the next tile from the
 //               global counter, publishes it in a shared-memory tile ring,
-//               then streams its K slices (2P tiles of 64 K each) into a
-//               stage ring with 2-D tiled bulk copies (128-byte swizzle);
+//               then streams its K slices (2P tiles of 128 bytes of K each)
+//               into a stage ring with 2-D tiled bulk copies (128-byte
+//               swizzle);
 //   warp 1      allocates TMEM and issues the MMAs (one elected lane);
 //               tcgen05.commit frees a stage once its MMAs have read it and
 //               signals a TMEM chunk buffer as full;
 //   warps 2-5   epilogue: tcgen05.ld each finished chunk (warp w reads TMEM
-//               lanes 32*(w%4)..+31 = tile rows) into 128 FP32 registers per
-//               thread, release the buffer, add the registers into C.
+//   (FP8: 2-9)  lanes 32*(w%4)..+31 = tile rows; with 8 warps, warps 6-9 take
+//               the upper 64 columns) into FP32 registers, release the
+//               buffer, add the registers into C.
 // Every mbarrier wait is bounded (2 s by %globaltimer); a wait that gives up
 // records GBBLAS_STATUS_TIMEOUT in the stream's error word, the CTA drains
 // its in-flight copies (bounded again), lets its MMAs finish, frees TMEM and
 // returns.
 //
 // Replaces the FP32 path of the reference's mtm (include/mtm.hpp:116-206)
-// when the caller asks for GBBLAS_ACCURACY_BF16X3 / BF16X6, and runs the
-// batched form of it.  Roofline: tensor pipe; (number of products) *
-// 2*M*N*K BF16 flops per problem, reported as 2*M*N*K algorithmic flops.
+// when the caller asks for GBBLAS_ACCURACY_BF16X3 / BF16X6 / FP8, and runs
+// the batched form of it.  Roofline: tensor pipe; 2*M*N*K algorithmic flops
+// per problem (split-BF16 issues 3 or 6 times that in BF16 products).
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -65,21 +76,51 @@ using namespace tc;
 constexpr int kBM = 128;
 constexpr int kBN = 128;
 constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
-constexpr int kThreads = 192;
 constexpr int kChunkTiles = 8;   // K slices folded into registers per chunk (512 of K)
 constexpr int kTileRing = 4;     // tiles in flight between scheduler and consumers
+// FP8: chunks of scales in flight between producer and epilogue.  The ring
+// couples the producer to the epilogue, so it is deep enough (16 x 1 KB) that
+// the operand stages, not the scales, bound how far the copies run ahead.
+constexpr int kScaleSlots = 16;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
 
-template <int P>
+// Kernel modes: 2 / 3 = FP32 split into that many BF16 pieces; kModeFp8 =
+// E4M3 operands with one power-of-two scale per 128 elements along K.
+constexpr int kModeFp8 = 8;
+
+template <int MODE>
+struct ModeTraits {
+  static constexpr bool fp8 = MODE == kModeFp8;
+  static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
+  static constexpr int kBKe = fp8 ? 128 : kBK;  // K elements per slice (128 bytes either way)
+  static constexpr int kChunk = fp8 ? 1 : kChunkTiles;  // slices per TMEM chunk (FP8: one scale block)
+  // Epilogue warps: 4 (each 32 tile rows x 128 columns) or, for FP8, whose
+  // chunks are four times shorter, 8 (32 rows x 64 columns each).
+  static constexpr int kEpiWarps = fp8 ? 8 : 4;
+  static constexpr int kCols = kBN * 4 / kEpiWarps;  // tile columns per epilogue thread
+  static constexpr int kThreads = 64 + 32 * kEpiWarps;
+  // TMEM chunk buffers (512 columns in all): 2 x (main + correction) for the
+  // split, 4 x main for FP8 (the MMAs may run three chunks ahead).
+  static constexpr int kBufs = fp8 ? 4 : 2;
+  static constexpr uint32_t kBufCols = 512 / kBufs;
+};
+
+template <int MODE>
 struct TcCfg {
-  static constexpr uint32_t kABytes = kBM * kBK * 2;  // one bf16 piece tile of A
-  static constexpr uint32_t kBBytes = kBN * kBK * 2;
+  static constexpr int P = ModeTraits<MODE>::P;
+  static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A
+  static constexpr uint32_t kBBytes = kBN * 128;
   static constexpr uint32_t kStageBytes = P * (kABytes + kBBytes);
-  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - 512) / kStageBytes);
-  static constexpr int kStages = kStagesFit > 4 ? 4 : kStagesFit;
-  static constexpr uint32_t kTmemCols = 4 * kBN;  // two chunk buffers x (main + correction)
-  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + 512 /*barriers, ring*/;
+  static constexpr uint32_t kTmemCols = 512;  // the chunk buffers (ModeTraits::kBufs x kBufCols)
+  // FP8: ring of per-chunk scales (128 row scales of A, 128 column scales of B)
+  static constexpr uint32_t kScaleBytes = ModeTraits<MODE>::fp8 ? kScaleSlots * 2 * 128 * 4 : 0;
+  static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
+  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kScaleBytes) / kStageBytes);
+  static constexpr int kStages = kStagesFit > 6 ? 6 : kStagesFit;
+  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kScaleBytes + kBarBytes;
+  static_assert((2 * 6 + 2 * 4 + 2 * kTileRing + 2 * kScaleSlots + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
+                "barrier area too small");
   static_assert(kStages >= 2, "need at least a double-buffered stage ring");
   static_assert(kSmem <= kSmemLimit, "exceeds the 227 KB per-CTA shared memory limit");
   static_assert(kStageBytes % 1024 == 0 && kABytes % 1024 == 0 && kBBytes % 1024 == 0,
@@ -90,7 +131,7 @@ struct TcCfg {
 // One GEMM of a group, as the kernel sees it (device memory).
 struct TcProblem {
   int M, N;
-  int num_kt;      // K slices: padded K / 64
+  int num_kt;      // K slices of 128 bytes: padded K / 64 (BF16) or / 128 (FP8)
   int a_row;       // first row of this problem in the A arena (piece 0)
   int b_row;       // first row in the B^T arena (piece 0)
   int tiles_m, tiles_n;
@@ -99,26 +140,47 @@ struct TcProblem {
   int64_t rsc, csc;
 };
 
-// One operand matrix to split (device memory).
+// One operand matrix to split or quantise (device memory).
 struct SplitJob {
   const float* src;
   int64_t rows, K, rs, cs;  // logical rows x K, element (r, k) at src[r*rs + k*cs]
   int64_t dst_row;          // first row in the arena
-  int tiles_r, tiles_k;     // 32 x 32 tiles covering padded rows x padded K
+  int tiles_r, tiles_k;     // preparation tiles (PrepTile) covering padded rows x padded K
   int tile_start;
 };
 
-// ---------------------------------------------------------------- split
-// For every job, writes P pieces of rows_pad x k_pad into the arena (piece p
-// at out + p * piece_stride, row pitch `pitch`), zero outside rows x K.
-template <int P>
-__global__ void __launch_bounds__(256) split_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
-                                                          __nv_bfloat16* __restrict__ out, int64_t piece_stride,
-                                                          int64_t pitch) {
-  __shared__ float tile[32][33];
+// ------------------------------------------------------ operand preparation
+// Tile of one preparation CTA: TR rows x TK along K (16 KB of FP32).
+template <int MODE>
+struct PrepTile {
+  static constexpr int TK = MODE == kModeFp8 ? 128 : 64;  // one FP8 scale block / one BF16 slice
+  static constexpr int TR = 4096 / TK;                    // 32 / 64 rows
+  static constexpr int LD = TK + 4;                       // shared row pitch (floats), 16-byte multiple
+};
+
+// For every job, writes its rows_pad x k_pad operand into the arena (row pitch
+// `pitch` elements), zero outside rows x K:
+//  * split-BF16 (MODE 2, 3): MODE pieces p0 = bf16_rn(a), p1 = bf16_rn(a - p0),
+//    ... (piece p at out + p * piece_stride);
+//  * FP8: E4M3 bytes and one power-of-two scale per (row, 128-K block) at
+//    scales[kb * scale_stride + arena row].  Block scale s = 2^e with e the
+//    smallest integer such that amax * 2^-e <= 448 (the largest finite E4M3),
+//    so v * 2^-e is exact and only the E4M3 rounding (nearest-even,
+//    saturating) loses bits.  All-zero (and padding) blocks get s = 1.
+// One CTA per tile.  Interior tiles of 16-byte-aligned sources are read with
+// 128-bit loads along whichever dimension is contiguous; edge tiles and other
+// strides element by element (still coalesced along the contiguous side).
+template <int MODE>
+__global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
+                                                         void* __restrict__ out, int64_t piece_stride, int64_t pitch,
+                                                         float* __restrict__ scales, int64_t scale_stride) {
+  using PT = PrepTile<MODE>;
+  constexpr int TK = PT::TK, TR = PT::TR, LD = PT::LD;
+  __shared__ __align__(16) float tile[TR * LD];
   __shared__ int sjob;
   const int t = blockIdx.x;
-  if (threadIdx.x == 0 && threadIdx.y == 0) {  // job = last with tile_start <= t
+  const int tid = threadIdx.x;
+  if (tid == 0) {  // job = last with tile_start <= t
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -132,31 +194,90 @@ __global__ void __launch_bounds__(256) split_group_kernel(const SplitJob* __rest
   __syncthreads();
   const SplitJob& j = jobs[sjob];
   const int local = t - j.tile_start;
-  const int64_t r0 = (int64_t)(local / j.tiles_k) * 32, k0 = (int64_t)(local % j.tiles_k) * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  if (j.cs == 1) {  // K contiguous: threads along k
+  const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
+  const bool full = r0 + TR <= j.rows && k0 + TK <= j.K;
+  const bool al16 = (reinterpret_cast<uintptr_t>(j.src) & 15) == 0;
+  if (full && al16 && j.cs == 1 && (j.rs & 3) == 0) {  // 128-bit loads along K
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int64_t r = r0 + ty + 8 * i, k = k0 + tx;
-      tile[ty + 8 * i][tx] = (r < j.rows && k < j.K) ? __ldg(j.src + r * j.rs + k) : 0.f;
+      const int idx = tid + 256 * i, r = idx / (TK / 4), k4 = idx % (TK / 4);
+      const float4 v = dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + r) * j.rs + k0 + 4 * k4));
+      *reinterpret_cast<float4*>(&tile[r * LD + 4 * k4]) = v;
     }
-  } else {  // rows contiguous (or general): threads along r
+  } else if (full && al16 && j.rs == 1 && (j.cs & 3) == 0) {  // 128-bit loads along rows
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int64_t r = r0 + tx, k = k0 + ty + 8 * i;
-      tile[tx][ty + 8 * i] = (r < j.rows && k < j.K) ? __ldg(j.src + r * j.rs + k * j.cs) : 0.f;
+      const int idx = tid + 256 * i, k = idx / (TR / 4), r4 = idx % (TR / 4);
+      const float4 v = dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + k) * j.cs + r0 + 4 * r4));
+      tile[(4 * r4 + 0) * LD + k] = v.x;
+      tile[(4 * r4 + 1) * LD + k] = v.y;
+      tile[(4 * r4 + 2) * LD + k] = v.z;
+      tile[(4 * r4 + 3) * LD + k] = v.w;
+    }
+  } else if (j.cs == 1) {  // K contiguous: consecutive threads along k
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+      const int idx = tid + 256 * i, r = idx / TK, k = idx % TK;
+      tile[r * LD + k] = (r0 + r < j.rows && k0 + k < j.K) ? __ldg(j.src + (r0 + r) * j.rs + k0 + k) : 0.f;
+    }
+  } else {  // rows contiguous (or general): consecutive threads along r
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+      const int idx = tid + 256 * i, r = idx % TR, k = idx / TR;
+      tile[r * LD + k] =
+          (r0 + r < j.rows && k0 + k < j.K) ? __ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs) : 0.f;
     }
   }
   __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  if constexpr (MODE == kModeFp8) {
+    // warp w: rows 4w..4w+3, lane: 4 consecutive K of the row's 128
+    uint8_t* q8 = static_cast<uint8_t*>(out);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int64_t r = j.dst_row + r0 + ty + 8 * i, k = k0 + tx;
-    float v = tile[ty + 8 * i][tx];
+    for (int rr = 0; rr < 4; ++rr) {
+      const int r = warp * 4 + rr;
+      const float4 v = *reinterpret_cast<const float4*>(&tile[r * LD + lane * 4]);
+      float amax = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
 #pragma unroll
-    for (int p = 0; p < P; ++p) {
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      out[p * piece_stride + r * pitch + k] = h;
-      v = v - __bfloat162float(h);  // exact in FP32
+      for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      int e = 0;
+      if (amax > 0.f) {
+        int ex;
+        const float m = frexpf(amax, &ex);  // amax = m * 2^ex, m in [0.5, 1); 448 = 0.875 * 2^9
+        e = ex - 9 + (m > 0.875f ? 1 : 0);
+        e = e < -126 ? -126 : (e > 126 ? 126 : e);
+      }
+      const float inv = __int_as_float((127 - e) << 23);  // 2^-e, a normal float for |e| <= 126
+      const __nv_fp8x2_storage_t lo =
+          __nv_cvt_float2_to_fp8x2(make_float2(v.x * inv, v.y * inv), __NV_SATFINITE, __NV_E4M3);
+      const __nv_fp8x2_storage_t hi =
+          __nv_cvt_float2_to_fp8x2(make_float2(v.z * inv, v.w * inv), __NV_SATFINITE, __NV_E4M3);
+      const int64_t row = j.dst_row + r0 + r;
+      *reinterpret_cast<uint32_t*>(q8 + row * pitch + k0 + lane * 4) = (uint32_t)lo | ((uint32_t)hi << 16);
+      if (lane == 0) scales[(k0 >> 7) * scale_stride + row] = __int_as_float((127 + e) << 23);
+    }
+  } else {
+    // half-warp per row: rows 8w + 2i + (lane / 16), lane % 16: 4 consecutive K of 64
+    __nv_bfloat16* pb = static_cast<__nv_bfloat16*>(out);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = warp * 8 + 2 * i + (lane >> 4), kk = (lane & 15) * 4;
+      float4 v = *reinterpret_cast<const float4*>(&tile[r * LD + kk]);
+      const int64_t base = (j.dst_row + r0 + r) * pitch + k0 + kk;
+#pragma unroll
+      for (int p = 0; p < MODE; ++p) {
+        const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+        const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+        uint2 w;
+        w.x = *reinterpret_cast<const uint32_t*>(&h01);
+        w.y = *reinterpret_cast<const uint32_t*>(&h23);
+        *reinterpret_cast<uint2*>(pb + p * piece_stride + base) = w;
+        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+        v.x -= f01.x;  // exact in FP32
+        v.y -= f01.y;
+        v.z -= f23.x;
+        v.w -= f23.y;
+      }
     }
   }
 }
@@ -188,12 +309,15 @@ __device__ __forceinline__ void tile_coords(const TcProblem& p, int t, int& m0, 
   n0 = (in_g / gm) * kBN;
 }
 
-template <int P>
-__global__ void __launch_bounds__(kThreads, 1)
+template <int MODE>
+__global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                       const TcProblem* __restrict__ probs, int nprob, int total_tiles, int a_piece_rows,
-                      int b_piece_rows, int* __restrict__ tile_counter, int* __restrict__ err) {
-  using CF = TcCfg<P>;
+                      int b_piece_rows, int* __restrict__ tile_counter, int* __restrict__ err,
+                      const float* __restrict__ sa, const float* __restrict__ sb) {
+  using MT = ModeTraits<MODE>;
+  using CF = TcCfg<MODE>;
+  constexpr int P = MT::P;
   constexpr int ST = CF::kStages;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
@@ -203,14 +327,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   auto b_tile = [&](int s, int p) {
     return smem + (size_t)s * CF::kStageBytes + (size_t)P * CF::kABytes + (size_t)p * CF::kBBytes;
   };
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
+  float* scale_ring = reinterpret_cast<float*>(smem + (size_t)ST * CF::kStageBytes);  // [kScaleSlots][256] (FP8)
+  auto scale_slot = [&](int i) { return scale_ring + i * 256; };  // sa[0..127] then sb[0..127]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes + CF::kScaleBytes);
   uint64_t* full = bars;                   // [ST]  TMA -> MMA
   uint64_t* empty = full + ST;             // [ST]  MMA -> TMA
-  uint64_t* tfull = empty + ST;            // [2]   MMA -> epilogue: chunk in TMEM buffer b
-  uint64_t* tempty = tfull + 2;            // [2]   epilogue -> MMA: TMEM buffer b drained
-  uint64_t* ring_full = tempty + 2;        // [kTileRing] scheduler -> consumers
+  uint64_t* tfull = empty + ST;            // [kBufs] MMA -> epilogue: chunk in TMEM buffer b
+  uint64_t* tempty = tfull + 4;            // [kBufs] epilogue -> MMA: TMEM buffer b drained
+  uint64_t* ring_full = tempty + 4;        // [kTileRing] scheduler -> consumers
   uint64_t* ring_empty = ring_full + kTileRing;  // [kTileRing] consumers -> scheduler
-  uint64_t* accf = ring_empty + kTileRing;  // [1] every MMA of this CTA finished
+  uint64_t* sfull = ring_empty + kTileRing;     // [kScaleSlots] producer -> epilogue (FP8 scales landed)
+  uint64_t* sempty = sfull + kScaleSlots;       // [kScaleSlots] epilogue -> producer (scales read)
+  uint64_t* accf = sempty + kScaleSlots;        // [1] every MMA of this CTA finished
   int* ring = reinterpret_cast<int*>(accf + 1);  // [kTileRing] tile ids, -1 = no more work
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kTileRing);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -222,13 +350,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < MT::kBufs; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+      mbar_init(&tempty[b], MT::kEpiWarps);  // one arrival per epilogue warp
     }
     for (int r = 0; r < kTileRing; ++r) {
       mbar_init(&ring_full[r], 1);
-      mbar_init(&ring_empty[r], 5);  // MMA lane + four epilogue warps
+      mbar_init(&ring_empty[r], 1 + MT::kEpiWarps);  // MMA lane + the epilogue warps
+    }
+    for (int i = 0; i < kScaleSlots; ++i) {
+      mbar_init(&sfull[i], 1);
+      mbar_init(&sempty[i], MT::kEpiWarps);  // one arrival per epilogue warp
     }
     mbar_init(accf, 1);
     *abort_flag = 0;
@@ -250,7 +382,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
   };
 
-  int issued = 0;  // producer: K slices whose copies were issued (all tiles)
+  int issued = 0;   // producer: K slices whose copies were issued (all tiles)
+  int sissued = 0;  // producer (FP8): chunks whose scale copies were issued
   if (warp == 0) {
     if (lane == 0) {
       bool stop = false;
@@ -279,17 +412,31 @@ __global__ void __launch_bounds__(kThreads, 1)
           // piece p of A occupies rows [p*a_piece_rows, (p+1)*a_piece_rows) of the arena map
 #pragma unroll
           for (int p = 0; p < P; ++p)
-            tma_load_2d(a_tile(s, p), &tm_a, &full[s], kt * kBK, p * a_piece_rows + pr.a_row + m0);
+            tma_load_2d(a_tile(s, p), &tm_a, &full[s], kt * MT::kBKe, p * a_piece_rows + pr.a_row + m0);
 #pragma unroll
           for (int p = 0; p < P; ++p)
-            tma_load_2d(b_tile(s, p), &tm_b, &full[s], kt * kBK, p * b_piece_rows + pr.b_row + n0);
+            tma_load_2d(b_tile(s, p), &tm_b, &full[s], kt * MT::kBKe, p * b_piece_rows + pr.b_row + n0);
           ++issued;
+          if constexpr (MT::fp8) {
+            // this chunk's 128 row scales of A and 128 column scales of B
+            // (scale planes are K-block-major: both runs contiguous)
+            const int ss = sissued % kScaleSlots, sr = sissued / kScaleSlots;
+            if (sr > 0 && !mbar_wait_bounded(&sempty[ss], (sr - 1) & 1, abort_flag, kWaitLimitNs)) {
+              fail();
+              stop = true;
+              break;
+            }
+            mbar_arrive_expect_tx(&sfull[ss], 2 * 128 * 4);
+            bulk_load(scale_slot(ss), sa + (int64_t)kt * a_piece_rows + pr.a_row + m0, 128 * 4, &sfull[ss]);
+            bulk_load(scale_slot(ss) + 128, sb + (int64_t)kt * b_piece_rows + pr.b_row + n0, 128 * 4, &sfull[ss]);
+            ++sissued;
+          }
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(kBM, kBN);
+      constexpr uint32_t idesc = MT::fp8 ? idesc_e4m3_f32(kBM, kBN) : idesc_bf16_f32(kBM, kBN);
       int consumed = 0;  // K slices consumed (all tiles)
       int chunk_g = 0;   // chunks started (all tiles)
       bool stop = false;
@@ -305,12 +452,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int num_kt = probs[find_problem(probs, nprob, t)].num_kt;
         for (int kt = 0; kt < num_kt; ++kt) {
           const int s = consumed % ST, round = consumed / ST;
-          const bool chunk_first = (kt % kChunkTiles) == 0;
-          const bool chunk_last = ((kt + 1) % kChunkTiles) == 0 || kt + 1 == num_kt;
+          const bool chunk_first = (kt % MT::kChunk) == 0;
+          const bool chunk_last = ((kt + 1) % MT::kChunk) == 0 || kt + 1 == num_kt;
           if (chunk_first) ++chunk_g;
-          const int chunk = chunk_g - 1, b = chunk & 1;
-          if (chunk_first && chunk >= 2) {  // buffer b must have been drained by the epilogue
-            if (!mbar_wait_bounded(&tempty[b], ((chunk >> 1) - 1) & 1, abort_flag, kWaitLimitNs)) {
+          const int chunk = chunk_g - 1, b = chunk % MT::kBufs;
+          if (chunk_first && chunk >= MT::kBufs) {  // buffer b must have been drained by the epilogue
+            if (!mbar_wait_bounded(&tempty[b], ((chunk / MT::kBufs) - 1) & 1, abort_flag, kWaitLimitNs)) {
               fail();
               stop = true;
               break;
@@ -323,7 +470,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           tc_fence_after();
-          const uint32_t acc_main = tmem + (uint32_t)(b * 2 * kBN), acc_corr = acc_main + kBN;
+          const uint32_t acc_main = tmem + (uint32_t)b * MT::kBufCols, acc_corr = acc_main + kBN;
           uint32_t a[P], bb[P];
 #pragma unroll
           for (int p = 0; p < P; ++p) {
@@ -331,17 +478,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             bb[p] = smem_u32(b_tile(s, p));
           }
 #pragma unroll
-          for (int kk = 0; kk < kBK / 16; ++kk) {
-            const uint32_t off = kk * 32;  // 16 bf16 along K inside the swizzled row
+          for (int kk = 0; kk < 4; ++kk) {
+            // 32 bytes along K per MMA inside the swizzled 128-byte row:
+            // 16 bf16 (kind::f16) or 32 e4m3 (kind::f8f6f4)
+            const uint32_t off = kk * 32;
             const uint32_t acc = (chunk_first && kk == 0) ? 0u : 1u;
-            mma_f16(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc, acc);
-            // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
-            mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[1] + off), idesc, acc);
-            mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
-            if constexpr (P == 3) {
-              mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[2] + off), idesc, 1u);
-              mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[1] + off), idesc, 1u);
-              mma_f16(acc_corr, sw128_kmajor_desc(a[2] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
+            if constexpr (MT::fp8) {
+              mma_f8f6f4(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc, acc);
+            } else {
+              mma_f16(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc, acc);
+              // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
+              mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[1] + off), idesc, acc);
+              mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
+              if constexpr (P == 3) {
+                mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[2] + off), idesc, 1u);
+                mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[1] + off), idesc, 1u);
+                mma_f16(acc_corr, sw128_kmajor_desc(a[2] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
+              }
             }
           }
           mma_commit(&empty[s]);
@@ -359,9 +512,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quarter = warp % 4, one tile row per thread.
+    // epilogue warps 2..: TMEM lane quarter = warp % 4 (the lanes a warp may
+    // access), one tile row per thread; column slice (warp - 2) / 4 of kCols.
+    constexpr int kCols = MT::kCols;
     const int q = warp & 3;
-    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+    const int col0 = ((warp - 2) >> 2) * kCols;
+    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col0;
     int chunk_g = 0;
     for (int it = 0;; ++it) {
       const int slot = it % kTileRing, use = it / kTileRing;
@@ -378,31 +534,70 @@ __global__ void __launch_bounds__(kThreads, 1)
       const TcProblem& pr = probs[find_problem(probs, nprob, t)];
       int m0, n0;
       tile_coords(pr, t, m0, n0);
-      const int nchunks = (pr.num_kt + kChunkTiles - 1) / kChunkTiles;
-      float acc[kBN];
+      const int nchunks = (pr.num_kt + MT::kChunk - 1) / MT::kChunk;
+      float acc[kCols];
 #pragma unroll
-      for (int j = 0; j < kBN; ++j) acc[j] = 0.f;
+      for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
       bool ok = true;
       for (int c = 0; c < nchunks; ++c, ++chunk_g) {
-        const int b = chunk_g & 1;
+        const int b = chunk_g % MT::kBufs;
         // tcgen05.ld is warp-collective: make the decision warp-uniform.
         const bool ready =
-            __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[b], (chunk_g >> 1) & 1, abort_flag, kWaitLimitNs));
+            __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[b], (chunk_g / MT::kBufs) & 1, abort_flag, kWaitLimitNs));
         if (!ready) {
           if (lane == 0) fail();
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t tb = trow + (uint32_t)(b * 2 * kBN);
+        const uint32_t tb = trow + (uint32_t)b * MT::kBufCols;
+        if constexpr (MT::fp8) {
+          // chunk c is 128-K block c: C += partial * scale_a(row, c) * scale_b(col, c),
+          // the scales staged in shared memory by the producer (slot chunk_g % kScaleSlots).
+          const int ss = chunk_g % kScaleSlots;
+          const bool landed = __all_sync(
+              0xffffffffu, mbar_wait_bounded(&sfull[ss], (chunk_g / kScaleSlots) & 1, abort_flag, kWaitLimitNs));
+          if (!landed) {
+            if (lane == 0) fail();
+            ok = false;
+            break;
+          }
+          const float* sc = scale_slot(ss);
+          const float sr = sc[q * 32 + lane];
+          const float2 sr2 = make_float2(sr, sr);
 #pragma unroll
-        for (int c0 = 0; c0 < kBN; c0 += 16) {
-          float v0[16], v1[16];
-          tmem_ld16(tb + c0, v0);
-          tmem_ld16(tb + kBN + c0, v1);
-          tmem_ld_wait();
+          for (int h = 0; h < kCols; h += 64) {
+            float v[64];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[c0 + j] += v0[j] + v1[j];
+            for (int c0 = 0; c0 < 64; c0 += 16) tmem_ld16p(tb + h + c0, v + c0);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 64; j += 4) {
+              // column scales: the same address across the warp (broadcast)
+              const float4 s4 = *reinterpret_cast<const float4*>(sc + 128 + col0 + h + j);
+              const float2 c01 = __fmul2_rn(make_float2(s4.x, s4.y), sr2);
+              const float2 c23 = __fmul2_rn(make_float2(s4.z, s4.w), sr2);
+              const float2 a01 = __ffma2_rn(make_float2(v[j], v[j + 1]), c01, make_float2(acc[h + j], acc[h + j + 1]));
+              const float2 a23 =
+                  __ffma2_rn(make_float2(v[j + 2], v[j + 3]), c23, make_float2(acc[h + j + 2], acc[h + j + 3]));
+              acc[h + j] = a01.x;
+              acc[h + j + 1] = a01.y;
+              acc[h + j + 2] = a23.x;
+              acc[h + j + 3] = a23.y;
+            }
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sempty[ss]);
+        } else {
+#pragma unroll
+          for (int c0 = 0; c0 < kCols; c0 += 16) {
+            float v0[16], v1[16];
+            tmem_ld16(tb + c0, v0);
+            tmem_ld16(tb + kBN + c0, v1);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[c0 + j] += v0[j] + v1[j];
+          }
         }
         tc_fence_before();
         __syncwarp();
@@ -416,10 +611,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         float* crow = pr.C + (int64_t)row * pr.rsc;
         const bool vec =
             (pr.csc == 1) && ((pr.rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(pr.C) & 15) == 0);
-        if (vec && n0 + kBN <= pr.N) {
+        const int cn = n0 + col0;
+        if (vec && cn + kCols <= pr.N) {
 #pragma unroll
-          for (int j = 0; j < kBN; j += 4) {
-            float4* p = reinterpret_cast<float4*>(crow + n0 + j);
+          for (int j = 0; j < kCols; j += 4) {
+            float4* p = reinterpret_cast<float4*>(crow + cn + j);
             float4 cv = *p;
             cv.x += acc[j];
             cv.y += acc[j + 1];
@@ -429,8 +625,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < kBN; ++j)
-            if (n0 + j < pr.N) crow[(int64_t)(n0 + j) * pr.csc] += acc[j];
+          for (int j = 0; j < kCols; ++j)
+            if (cn + j < pr.N) crow[(int64_t)(cn + j) * pr.csc] += acc[j];
         }
       }
     }
@@ -442,6 +638,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     int never = 0;
     const int from = issued > ST ? issued - ST : 0;
     for (int k = from; k < issued; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
+    const int sfrom = sissued > kScaleSlots ? sissued - kScaleSlots : 0;
+    for (int k = sfrom; k < sissued; ++k)
+      (void)mbar_wait_bounded(&sfull[k % kScaleSlots], (k / kScaleSlots) & 1, &never, kWaitLimitNs / 2);
   }
   tc_fence_before();
   __syncthreads();
@@ -467,21 +666,23 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D bf16 tensor map over a rows x cols (cols contiguous) buffer, box of
-// box_rows x 64 with 128-byte swizzle.
-gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+// 2-D tensor map over a rows x cols (cols contiguous) buffer of BF16 or
+// 8-bit elements, box of box_rows x 128 bytes with 128-byte swizzle.
+gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows,
+                       bool bytes) {
   auto fn = encode_fn();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled is not available from the driver");
     return GBBLAS_STATUS_CUDA_ERROR;
   }
+  const uint64_t esize = bytes ? 1 : 2;
   cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
+  cuuint64_t strides[1] = {cols * esize};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esize), box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = fn(map, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d) for %llu x %llu", (int)r, (unsigned long long)rows,
               (unsigned long long)cols);
@@ -495,33 +696,42 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 }  // namespace
 
-// Everything one split-BF16 group launch needs: host tables, where they and
-// the BF16 arena live on the device, and the two arena tensor maps.
+// Everything one tensor-core group launch needs: host tables, where they and
+// the operand arena live on the device, and the two arena tensor maps.
 struct TcGroupPlan {
-  int pieces = 2;
+  int mode = 2;  // 2 / 3 BF16 pieces, kModeFp8
   int nprob = 0;
-  int64_t a_rows = 0, b_rows = 0, pitch = 0, tiles = 0;
+  int64_t a_rows = 0, b_rows = 0, pitch = 0, tiles = 0;  // pitch in elements (FP8: bytes)
   int a_tiles = 0, b_tiles = 0;
   std::vector<TcProblem> probs;
   std::vector<SplitJob> ajobs, bjobs;
-  size_t off_probs = 0, off_jobs = 0, off_arena = 0, bytes = 0;
-  char* base = nullptr;  // device: zeroed header | problems | jobs | arena
+  size_t off_probs = 0, off_jobs = 0, off_arena = 0, off_sa = 0, off_sb = 0, bytes = 0;
+  char* base = nullptr;  // device: zeroed header | problems | jobs | arena | FP8 scales
   bool owned = false;    // base allocated by the plan (graph plans)
   CUtensorMap map_a, map_b;
+  bool fp8() const { return mode == kModeFp8; }
+  int planes() const { return fp8() ? 1 : mode; }
+  int slice_k() const { return fp8() ? 128 : kBK; }  // K elements per 128-byte slice
+  int job_k() const { return fp8() ? 128 : 64; }     // K extent of one preparation tile (PrepTile::TK)
 };
 
 namespace {
 
 // Host-side planning (no device work): problem order (largest K first),
 // arena rows, tile numbering, split jobs, device layout.
-gbblas_status plan_group(int pieces, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl) {
-  pl.pieces = pieces;
+gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl) {
+  if (mode != 2 && mode != 3 && mode != kModeFp8) {
+    set_error("tensor-core gemm: unknown mode %d", mode);
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  pl.mode = mode;
+  const int64_t sk = pl.slice_k(), jk = pl.job_k(), jr = 4096 / jk;
   std::vector<int64_t> order;
   order.reserve(count);
   for (int64_t i = 0; i < count; ++i) {
     const gbblas_gemm_desc& g = d[i];
     if (g.M > (1 << 29) || g.N > (1 << 29) || g.K > (1 << 30)) {
-      set_error("split-bf16 gemm: problem %lld too large for the tile grid", (long long)i);
+      set_error("tensor-core gemm: problem %lld too large for the tile grid", (long long)i);
       return GBBLAS_STATUS_NOT_SUPPORTED;
     }
     if (g.M > 0 && g.N > 0 && g.K > 0) order.push_back(i);
@@ -531,14 +741,14 @@ gbblas_status plan_group(int pieces, const gbblas_gemm_desc* d, int64_t count, T
   pl.probs.resize(pl.nprob);
   pl.ajobs.resize(pl.nprob);
   pl.bjobs.resize(pl.nprob);
-  for (int i = 0; i < pl.nprob; ++i) pl.pitch = std::max<int64_t>(pl.pitch, round_up(d[order[i]].K, kBK));
+  for (int i = 0; i < pl.nprob; ++i) pl.pitch = std::max<int64_t>(pl.pitch, round_up(d[order[i]].K, sk));
   for (int i = 0; i < pl.nprob; ++i) {
     const gbblas_gemm_desc& g = d[order[i]];
-    const int64_t Mp = round_up(g.M, kBM), Np = round_up(g.N, kBN), Kp = round_up(g.K, kBK);
+    const int64_t Mp = round_up(g.M, kBM), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
     TcProblem& p = pl.probs[i];
     p.M = (int)g.M;
     p.N = (int)g.N;
-    p.num_kt = (int)(Kp / kBK);
+    p.num_kt = (int)(Kp / sk);
     p.a_row = (int)pl.a_rows;
     p.b_row = (int)pl.b_rows;
     p.tiles_m = (int)(Mp / kBM);
@@ -547,32 +757,39 @@ gbblas_status plan_group(int pieces, const gbblas_gemm_desc* d, int64_t count, T
     p.C = g.C;
     p.rsc = g.rsc;
     p.csc = g.csc;
-    pl.ajobs[i] = {g.A, g.M, g.K, g.rsa, g.csa, pl.a_rows, (int)(Mp / 32), (int)(Kp / 32), pl.a_tiles};
+    pl.ajobs[i] = {g.A, g.M, g.K, g.rsa, g.csa, pl.a_rows, (int)(Mp / jr), (int)(Kp / jk), pl.a_tiles};
     pl.a_tiles += pl.ajobs[i].tiles_r * pl.ajobs[i].tiles_k;
     // B^T: element (n, k) = B[k*rsb + n*csb]
-    pl.bjobs[i] = {g.B, g.N, g.K, g.csb, g.rsb, pl.b_rows, (int)(Np / 32), (int)(Kp / 32), pl.b_tiles};
+    pl.bjobs[i] = {g.B, g.N, g.K, g.csb, g.rsb, pl.b_rows, (int)(Np / jr), (int)(Kp / jk), pl.b_tiles};
     pl.b_tiles += pl.bjobs[i].tiles_r * pl.bjobs[i].tiles_k;
     pl.a_rows += Mp;
     pl.b_rows += Np;
     pl.tiles += (int64_t)p.tiles_m * p.tiles_n;
   }
-  if ((double)(pl.a_rows + pl.b_rows) * pieces >= 2.0e9 || pl.tiles >= (1ll << 31) ||
+  if ((double)(pl.a_rows + pl.b_rows) * pl.planes() >= 2.0e9 || pl.tiles >= (1ll << 31) ||
       (double)pl.a_tiles >= 2.0e9 || (double)pl.b_tiles >= 2.0e9) {
-    set_error("split-bf16 gemm: group too large for one launch");
+    set_error("tensor-core gemm: group too large for one launch");
     return GBBLAS_STATUS_NOT_SUPPORTED;
   }
+  const size_t esize = pl.fp8() ? 1 : sizeof(__nv_bfloat16);
   pl.off_probs = kScratchZeroBytes;
   pl.off_jobs = pl.off_probs + align256(sizeof(TcProblem) * pl.nprob);
   pl.off_arena = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.nprob);
-  const size_t a_piece = (size_t)(pl.a_rows * pl.pitch), b_piece = (size_t)(pl.b_rows * pl.pitch);
-  pl.bytes = pl.off_arena + (size_t)pieces * (a_piece + b_piece) * sizeof(__nv_bfloat16);
+  const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
+  pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
+  const size_t kb = pl.fp8() ? (size_t)(pl.pitch / 128) : 0;
+  pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(float));
+  pl.bytes = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(float));
   return GBBLAS_STATUS_SUCCESS;
 }
 
-__nv_bfloat16* arena_a(const TcGroupPlan& pl) { return reinterpret_cast<__nv_bfloat16*>(pl.base + pl.off_arena); }
-__nv_bfloat16* arena_b(const TcGroupPlan& pl) {
-  return arena_a(pl) + (size_t)pl.pieces * (size_t)(pl.a_rows * pl.pitch);
+char* arena_a(const TcGroupPlan& pl) { return pl.base + pl.off_arena; }
+char* arena_b(const TcGroupPlan& pl) {
+  const size_t esize = pl.fp8() ? 1 : sizeof(__nv_bfloat16);
+  return arena_a(pl) + (size_t)pl.planes() * (size_t)(pl.a_rows * pl.pitch) * esize;
 }
+float* scales_a(const TcGroupPlan& pl) { return reinterpret_cast<float*>(pl.base + pl.off_sa); }
+float* scales_b(const TcGroupPlan& pl) { return reinterpret_cast<float*>(pl.base + pl.off_sb); }
 
 // Point the plan at device memory `base` (>= pl.bytes, header zeroed), copy
 // the tables there on `stream`, and encode the arena tensor maps.
@@ -585,56 +802,81 @@ gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
                               cudaMemcpyHostToDevice, stream));
   GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs + sizeof(SplitJob) * pl.nprob, pl.bjobs.data(),
                               sizeof(SplitJob) * pl.nprob, cudaMemcpyHostToDevice, stream));
-  GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)(pl.pieces * pl.a_rows), (uint64_t)pl.pitch, kBM));
-  GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)(pl.pieces * pl.b_rows), (uint64_t)pl.pitch, kBN));
+  GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)(pl.planes() * pl.a_rows), (uint64_t)pl.pitch, kBM, pl.fp8()));
+  GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)(pl.planes() * pl.b_rows), (uint64_t)pl.pitch, kBN, pl.fp8()));
   return GBBLAS_STATUS_SUCCESS;
 }
 
-template <int P>
+template <int MODE>
 gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
-  using CF = TcCfg<P>;
+  using CF = TcCfg<MODE>;
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   int* err = reinterpret_cast<int*>(pl.base + kErrWordOffset);
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* dprobs = reinterpret_cast<const TcProblem*>(pl.base + pl.off_probs);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
-  split_group_kernel<P><<<pl.a_tiles, dim3(32, 8), 0, stream>>>(djobs, pl.nprob, arena_a(pl),
-                                                                (int64_t)(pl.a_rows * pl.pitch), pl.pitch);
-  GB_TRY(check_launch("split_group_kernel(A)"));
-  split_group_kernel<P><<<pl.b_tiles, dim3(32, 8), 0, stream>>>(djobs + pl.nprob, pl.nprob, arena_b(pl),
-                                                                (int64_t)(pl.b_rows * pl.pitch), pl.pitch);
-  GB_TRY(check_launch("split_group_kernel(B)"));
+  prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.nprob, arena_a(pl),
+                                                          (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
+                                                          pl.a_rows);
+  GB_TRY(check_launch("prep_group_kernel(A)"));
+  prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.nprob, pl.nprob, arena_b(pl),
+                                                          (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
+                                                          pl.b_rows);
+  GB_TRY(check_launch("prep_group_kernel(B)"));
   static bool attr_set[64] = {false};
   if (!attr_set[c->device & 63]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)CF::kSmem));
     attr_set[c->device & 63] = true;
   }
   int grid = (int)std::min<int64_t>(pl.tiles, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  gemm_split_kernel<P><<<grid, kThreads, CF::kSmem, stream>>>(pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                                                             (int)pl.a_rows, (int)pl.b_rows, counter, err);
+  gemm_split_kernel<MODE><<<grid, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(pl.map_a, pl.map_b, dprobs, pl.nprob,
+                                                                 (int)pl.tiles, (int)pl.a_rows, (int)pl.b_rows,
+                                                                 counter, err, scales_a(pl), scales_b(pl));
   return check_launch("gemm_split_kernel");
 }
 
 }  // namespace
 
+int tc_mode(gbblas_accuracy acc) {
+  switch (acc) {
+    case GBBLAS_ACCURACY_BF16X3: return 2;
+    case GBBLAS_ACCURACY_BF16X6: return 3;
+    case GBBLAS_ACCURACY_FP8: return kModeFp8;
+    default: return 0;
+  }
+}
+
+size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
+  const bool fp8 = mode == kModeFp8;
+  const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? 128 : kBK;
+  const int64_t rows = round_up(M, kBM) + round_up(N, kBN), Kp = round_up(K, sk);
+  return (size_t)(rows * Kp * planes * (fp8 ? 1 : 2) + (fp8 ? rows * (Kp / 128) * 4 : 0));
+}
+
 void tc_prepare(DeviceCtx* c) {
   (void)c;
   cudaFuncSetAttribute(gemm_split_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<2>::kSmem);
   cudaFuncSetAttribute(gemm_split_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<3>::kSmem);
+  cudaFuncSetAttribute(gemm_split_kernel<kModeFp8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)TcCfg<kModeFp8>::kSmem);
 }
 
 gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas) {
-  return pl->pieces == 3 ? launch_bound<3>(c, *pl, stream, max_ctas) : launch_bound<2>(c, *pl, stream, max_ctas);
+  switch (pl->mode) {
+    case 3: return launch_bound<3>(c, *pl, stream, max_ctas);
+    case kModeFp8: return launch_bound<kModeFp8>(c, *pl, stream, max_ctas);
+    default: return launch_bound<2>(c, *pl, stream, max_ctas);
+  }
 }
 
-gbblas_status tc_group_create(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
+gbblas_status tc_group_create(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
                               TcGroupPlan** out) {
   (void)c;
   TcGroupPlan* pl = new TcGroupPlan();
-  gbblas_status st = plan_group(pieces, descs, count, *pl);
+  gbblas_status st = plan_group(mode, descs, count, *pl);
   if (st != GBBLAS_STATUS_SUCCESS) {
     delete pl;
     return st;
@@ -673,10 +915,10 @@ int* tc_group_error_word(const TcGroupPlan* pl) {
   return pl->base ? reinterpret_cast<int*>(pl->base + kErrWordOffset) : nullptr;
 }
 
-gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbblas_gemm_desc* descs, int64_t count,
-                                           cudaStream_t stream, int max_ctas) {
+gbblas_status launch_gemm_tc_group(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
+                                   cudaStream_t stream, int max_ctas) {
   TcGroupPlan pl;
-  GB_TRY(plan_group(pieces, descs, count, pl));
+  GB_TRY(plan_group(mode, descs, count, pl));
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   void* s = nullptr;
   GB_TRY(get_scratch(c, stream, pl.bytes, &s));
@@ -684,12 +926,12 @@ gbblas_status launch_gemm_split_bf16_group(DeviceCtx* c, int pieces, const gbbla
   return tc_group_launch(c, &pl, stream, max_ctas);
 }
 
-gbblas_status launch_gemm_split_bf16(DeviceCtx* c, int pieces, int64_t M, int64_t N, int64_t K, const float* A,
-                                     int64_t rsa, int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C,
-                                     int64_t rsc, int64_t csc, cudaStream_t stream) {
+gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
+                             int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
+                             int64_t csc, cudaStream_t stream) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   gbblas_gemm_desc d{M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc};
-  return launch_gemm_split_bf16_group(c, pieces, &d, 1, stream);
+  return launch_gemm_tc_group(c, mode, &d, 1, stream);
 }
 
 }  // namespace gbblas

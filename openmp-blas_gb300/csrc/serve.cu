@@ -56,17 +56,21 @@ struct Round {
 
 int64_t round_up64(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
+// Tensor-core mode of an FP32 GEMM request that does not ask for the FMA
+// path (AUTO: the FP32-accurate six-product split).
+int server_mode(int32_t acc) {
+  return acc == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode((gbblas_accuracy)acc);
+}
+
 // Device bytes a request holds while in flight: operands, result, and the
-// split-BF16 arena of a tensor-core GEMM.
+// operand arena (BF16 pieces or FP8 values and scales) of a tensor-core GEMM.
 int64_t working_set(const gbblas_request& r) {
   const int64_t s = r.dtype == GBBLAS_F64 ? 8 : 4;
   switch (r.op) {
     case GBBLAS_OP_MTM: {
       int64_t b = (r.M * r.K + r.K * r.N + r.M * r.N) * s;
-      if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32) {
-        const int64_t pieces = r.accuracy == GBBLAS_ACCURACY_BF16X3 ? 2 : 3;
-        b += pieces * 2 * (round_up64(r.M, 128) + round_up64(r.N, 128)) * round_up64(r.K, 64);
-      }
+      if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32)
+        b += (int64_t)tc_arena_bytes(server_mode(r.accuracy), r.M, r.N, r.K);
       return b;
     }
     case GBBLAS_OP_MTV:
@@ -78,8 +82,9 @@ int64_t working_set(const gbblas_request& r) {
 }
 
 // Estimated GPU time (us) of a request from its flops / bytes and the rate of
-// the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP32
-// FMA ~50, FP64 ~0.8 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1 TFLOP/s).
+// the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP8
+// ~600, FP32 FMA ~50, FP64 ~0.8 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1
+// TFLOP/s).
 double estimate_us(const gbblas_request& r) {
   const double launch = 5.0;
   switch (r.op) {
@@ -92,6 +97,8 @@ double estimate_us(const gbblas_request& r) {
         rate = 50e6;
       else if (r.accuracy == GBBLAS_ACCURACY_BF16X3)
         rate = 430e6;
+      else if (r.accuracy == GBBLAS_ACCURACY_FP8)
+        rate = 600e6;
       else
         rate = 260e6;
       return launch + fl / rate;
@@ -157,7 +164,7 @@ void CUDART_CB on_round_done(void* p) {
 gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
   DeviceCtx* c = s->ctx;
   const int cap = rd->max_ctas;
-  std::vector<gbblas_gemm_desc> split3, split2;
+  std::vector<gbblas_gemm_desc> split3, split2, fp8;
   std::vector<gbblas_gemv_desc> gemv;
   gbblas_status first_err = GBBLAS_STATUS_SUCCESS;
   auto note = [&](gbblas_status e) {
@@ -180,7 +187,8 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
       } else {
         gbblas_gemm_desc d{r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa, static_cast<const float*>(r.B),
                            rsb, csb, static_cast<float*>(r.C), rsc, csc};
-        (r.accuracy == GBBLAS_ACCURACY_BF16X3 ? split2 : split3).push_back(d);
+        const int mode = server_mode(r.accuracy);
+        (mode == 2 ? split2 : mode == 3 ? split3 : fp8).push_back(d);
       }
     } else if (r.op == GBBLAS_OP_MTV || r.op == GBBLAS_OP_VTM) {
       const bool tr = r.op == GBBLAS_OP_VTM;
@@ -208,8 +216,10 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
                                static_cast<float*>(r.C), st));
     }
   }
-  if (!split3.empty()) note(launch_gemm_split_bf16_group(c, 3, split3.data(), (int64_t)split3.size(), st, cap));
-  if (!split2.empty()) note(launch_gemm_split_bf16_group(c, 2, split2.data(), (int64_t)split2.size(), st, cap));
+  if (!split3.empty()) note(launch_gemm_tc_group(c, 3, split3.data(), (int64_t)split3.size(), st, cap));
+  if (!split2.empty()) note(launch_gemm_tc_group(c, 2, split2.data(), (int64_t)split2.size(), st, cap));
+  if (!fp8.empty())
+    note(launch_gemm_tc_group(c, tc_mode(GBBLAS_ACCURACY_FP8), fp8.data(), (int64_t)fp8.size(), st, cap));
   // fixed rows-per-item: no autotuning (timing) inside the serving loop
   if (!gemv.empty()) note(launch_gemv_group_rows_fixed(c, gemv.data(), (int64_t)gemv.size(), st, 4));
   rd->status = first_err;
@@ -407,8 +417,7 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
     return GBBLAS_STATUS_INVALID_VALUE;
   }
   if (r->op < GBBLAS_OP_MTM || r->op > GBBLAS_OP_DOT || (r->dtype != GBBLAS_F32 && r->dtype != GBBLAS_F64) ||
-      (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 || r->accuracy > 4 ||
-      r->accuracy == GBBLAS_ACCURACY_FP8) {
+      (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 || r->accuracy > 4) {
     set_error("gbblas_server_submit: bad op, dtype, layout or accuracy");
     return GBBLAS_STATUS_INVALID_VALUE;
   }

@@ -196,7 +196,7 @@ int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
   float best_ms[2] = {1e30f, 1e30f};
   for (int choice = 0; choice < 2; ++choice) {
     auto run = [&]() {
-      return choice == 1 ? launch_gemm_split_bf16(c, 3, m, n, k, A, k, 1, B, n, 1, C, n, 1, s)
+      return choice == 1 ? launch_gemm_tc(c, tc_mode(GBBLAS_ACCURACY_BF16X6), m, n, k, A, k, 1, B, n, 1, C, n, 1, s)
                          : launch_gemm_fma<float>(c, m, n, k, A, k, 1, B, n, 1, C, n, 1, s);
     };
     if (run() != GBBLAS_STATUS_SUCCESS) continue;  // warm-up
