@@ -1,10 +1,11 @@
 /*
  * gbblas.h - C ABI of the GB300 (sm_103a) implementation of OpenMP-BLAS's
- * dense hot path: mtm (GEMM), mtv / vtm (GEMV) and dot.
+ * dense hot path: mtm (GEMM), mtv / vtm (GEMV) and dot, plus the streaming
+ * operations beside it: outer product, transpose and element-wise ops.
  *
- * The C++ drop-in headers include/mtm.hpp, include/mtv.hpp and
- * include/dot.hpp keep the reference's amt:: templates and call the
- * *_host entry points below; any other language binds these functions
+ * The C++ drop-in headers include/mtm.hpp, mtv.hpp, dot.hpp, outer.hpp,
+ * trans.hpp and el_wise_op.hpp keep the reference's amt:: templates and call
+ * the *_host entry points below; any other language binds these functions
  * directly (ctypes, cgo, JNI...).  No C++ or CUDA type appears in a
  * signature: sizes are int64_t, strides are in elements, streams are
  * `void*` holding a cudaStream_t (NULL = the legacy default stream).
@@ -17,12 +18,15 @@
  *     given stream.  *_host entry points take HOST pointers, stage through a
  *     library-owned device pool, and return after the result is back in host
  *     memory (the reference's "call the lambda and the result is there").
- *   - Shape rules are the reference's: matrices have both extents > 1, the
- *     inner dimensions must agree (reference include/mtm.hpp:234-250,
- *     include/mtv.hpp:126-144 and 189-208, include/dot.hpp:196-214).  A
- *     violation returns GBBLAS_STATUS_SHAPE_MISMATCH (the reference throws
- *     std::runtime_error; the drop-in headers turn the status back into that
- *     exception).
+ *   - Sizes are explicit, so the C ABI rejects only what it cannot run
+ *     (negative sizes, null pointers, output strides that would alias, an
+ *     unknown enum) with GBBLAS_STATUS_INVALID_VALUE.  The reference's shape
+ *     rules on tensors (operands are matrices / vectors, inner dimensions
+ *     agree: reference include/mtm.hpp:234-250, include/mtv.hpp:126-144 and
+ *     189-208, include/dot.hpp:196-214) are checked by the drop-in headers,
+ *     which throw std::runtime_error when the callable is created, as the
+ *     reference does.  GBBLAS_STATUS_SHAPE_MISMATCH is reserved for
+ *     bindings that pass tensor extents through.
  *   - Results are deterministic: reductions use a fixed order, no atomics.
  */
 #ifndef GBBLAS_H
@@ -193,6 +197,54 @@ gbblas_status gbblas_sdot_tuning(int64_t n, const float* a, const float* b, int6
 gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, int64_t b1, int64_t b2,
                                  int64_t b3, double* result, void* stream);
 
+/* -------------------------------------------------------- outer product */
+
+/* C += a b^T: C is the M x N matrix (dense, layout lc), a has M elements, b
+ * has N.  Replaces amt::outer_prod, reference include/outer.hpp:67-119
+ * (helper 14-65), which also accumulates into C.  Each element is one fused
+ * multiply-add, c = fma(a_i, b_j, c), as in the reference's inner loop
+ * (include/simd_loop.hpp:42-47).  DEVICE pointers. */
+gbblas_status gbblas_souter(gbblas_layout lc, int64_t M, int64_t N, const float* a, const float* b, float* C,
+                            void* stream);
+gbblas_status gbblas_douter(gbblas_layout lc, int64_t M, int64_t N, const double* a, const double* b,
+                            double* C, void* stream);
+
+/* ------------------------------------------------------------ transpose */
+
+/* C = A^T out of place: A is M x N with element (i, j) at A[i*rsa + j*csa];
+ * C is N x M with element (j, i) at C[j*rsc + i*csc].  Any strides (both
+ * layouts, padded leading dimensions); C must not overlap A.  Replaces
+ * amt::transpose(c, a, num_threads), reference include/trans.hpp:103-145
+ * (helper 33-65), which honours both tensors' strides the same way. */
+gbblas_status gbblas_stranspose(int64_t M, int64_t N, const float* A, int64_t rsa, int64_t csa, float* C,
+                                int64_t rsc, int64_t csc, void* stream);
+gbblas_status gbblas_dtranspose(int64_t M, int64_t N, const double* A, int64_t rsa, int64_t csa, double* C,
+                                int64_t rsc, int64_t csc, void* stream);
+
+/* In place, square n x n (either layout: the storage is transposed).
+ * Replaces amt::transpose(a, num_threads), reference include/trans.hpp:
+ * 147-169 (helper 67-101).  The reference's in-place form is only correct
+ * for square matrices (it swaps a[i*rows + j] with a[j*cols + i]); the drop-in
+ * header rejects other shapes. */
+gbblas_status gbblas_stranspose_inplace(int64_t n, float* A, void* stream);
+gbblas_status gbblas_dtranspose_inplace(int64_t n, double* A, void* stream);
+
+/* ---------------------------------------------------------- element-wise */
+
+typedef enum gbblas_ew_op {
+  GBBLAS_EW_ADD = 0, /* std::plus       */
+  GBBLAS_EW_SUB = 1, /* std::minus      */
+  GBBLAS_EW_MUL = 2, /* std::multiplies */
+  GBBLAS_EW_DIV = 3  /* std::divides (IEEE division) */
+} gbblas_ew_op;
+
+/* c[i] = a[i] op b[i] for i < n over the tensors' storage order.  Replaces
+ * amt::el_op::add / sub / mul / div / apply / apply_ops, reference
+ * include/el_wise_op.hpp:33-121 (which loops over c.size() elements of the
+ * three tensors' storage).  DEVICE pointers; c may equal a or b. */
+gbblas_status gbblas_sew(gbblas_ew_op op, int64_t n, const float* a, const float* b, float* c, void* stream);
+gbblas_status gbblas_dew(gbblas_ew_op op, int64_t n, const double* a, const double* b, double* c, void* stream);
+
 /* ------------------------------------------------------------- batching
  * Many independent problems in one launch.  No counterpart in the reference,
  * which runs one call at a time; these serve callers that would otherwise
@@ -346,6 +398,18 @@ gbblas_status gbblas_dvtm_host(gbblas_layout la, int64_t M, int64_t N, const dou
                                double* y);
 gbblas_status gbblas_sdot_host(int64_t n, const float* a, const float* b, float* result);
 gbblas_status gbblas_ddot_host(int64_t n, const double* a, const double* b, double* result);
+gbblas_status gbblas_souter_host(gbblas_layout lc, int64_t M, int64_t N, const float* a, const float* b,
+                                 float* C);
+gbblas_status gbblas_douter_host(gbblas_layout lc, int64_t M, int64_t N, const double* a, const double* b,
+                                 double* C);
+gbblas_status gbblas_stranspose_host(int64_t M, int64_t N, const float* A, int64_t rsa, int64_t csa, float* C,
+                                     int64_t rsc, int64_t csc);
+gbblas_status gbblas_dtranspose_host(int64_t M, int64_t N, const double* A, int64_t rsa, int64_t csa, double* C,
+                                     int64_t rsc, int64_t csc);
+gbblas_status gbblas_stranspose_inplace_host(int64_t n, float* A);
+gbblas_status gbblas_dtranspose_inplace_host(int64_t n, double* A);
+gbblas_status gbblas_sew_host(gbblas_ew_op op, int64_t n, const float* a, const float* b, float* c);
+gbblas_status gbblas_dew_host(gbblas_ew_op op, int64_t n, const double* a, const double* b, double* c);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -332,6 +332,169 @@ gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
   return gemm_any<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, acc, as_stream(stream));
 }
 
+// ---------------------------------------------- outer / transpose / element-wise
+template <typename T>
+gbblas_status check_outer(gbblas_layout lc, int64_t M, int64_t N, const T* a, const T* b, T* C) {
+  if (!layout_ok(lc)) return bad(GBBLAS_STATUS_INVALID_VALUE, "outer: layout must be 0 or 1");
+  if (M < 0 || N < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "outer: negative size");
+  if (M > 0 && N > 0 && (!a || !b || !C)) return bad(GBBLAS_STATUS_INVALID_VALUE, "outer: null pointer");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+// C (M x N, layout lc) += a b^T as a rank-1 update of contiguous rows:
+// row-major C: rows of length N, u = a, v = b; column-major C: columns of
+// length M, u = b, v = a (the operand swap of reference include/outer.hpp:110-114).
+template <typename T>
+gbblas_status outer_any(DeviceCtx* c, gbblas_layout lc, int64_t M, int64_t N, const T* a, const T* b, T* C,
+                        cudaStream_t s) {
+  if (lc == GBBLAS_LAST_ORDER) return launch_outer<T>(c, M, N, a, b, C, N, s);
+  return launch_outer<T>(c, N, M, b, a, C, M, s);
+}
+
+template <typename T>
+gbblas_status check_transpose(int64_t M, int64_t N, const T* A, int64_t rsa, int64_t csa, T* C, int64_t rsc,
+                              int64_t csc) {
+  if (M < 0 || N < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose: negative size");
+  if (rsa < 0 || csa < 0 || rsc < 0 || csc < 0)
+    return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose: strides must be non-negative");
+  if (M == 0 || N == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!A || !C) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose: null pointer");
+  if ((N > 1 && rsc == 0) || (M > 1 && csc == 0))
+    return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose: C strides must be non-zero (outputs would alias)");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status check_ew(gbblas_ew_op op, int64_t n, const T* a, const T* b, T* c) {
+  if ((int)op < 0 || (int)op > 3) return bad(GBBLAS_STATUS_INVALID_VALUE, "element-wise: unknown operation %d", (int)op);
+  if (n < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "element-wise: negative size");
+  if (n > 0 && (!a || !b || !c)) return bad(GBBLAS_STATUS_INVALID_VALUE, "element-wise: null pointer");
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status outer_dev(gbblas_layout lc, int64_t M, int64_t N, const T* a, const T* b, T* C, void* stream) {
+  GB_TRY(check_outer<T>(lc, M, N, a, b, C));
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return outer_any<T>(c, lc, M, N, a, b, C, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status transpose_dev(int64_t M, int64_t N, const T* A, int64_t rsa, int64_t csa, T* C, int64_t rsc,
+                            int64_t csc, void* stream) {
+  GB_TRY(check_transpose<T>(M, N, A, rsa, csa, C, rsc, csc));
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return launch_transpose<T>(c, M, N, A, rsa, csa, C, rsc, csc, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status transpose_inplace_dev(int64_t n, T* A, void* stream) {
+  if (n < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose in place: negative size");
+  if (n > 0 && !A) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose in place: null pointer");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return launch_transpose_square<T>(c, n, A, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status ew_dev(gbblas_ew_op op, int64_t n, const T* a, const T* b, T* out, void* stream) {
+  GB_TRY(check_ew<T>(op, n, a, b, out));
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  return launch_ew<T>(c, op, n, a, b, out, as_stream(stream));
+}
+
+template <typename T>
+gbblas_status outer_host(gbblas_layout lc, int64_t M, int64_t N, const T* a, const T* b, T* C) {
+  GB_TRY(check_outer<T>(lc, M, N, a, b, C));
+  if (M == 0 || N == 0) return GBBLAS_STATUS_SUCCESS;
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t nc = (size_t)(M * N) * sizeof(T), na = (size_t)M * sizeof(T), nb = (size_t)N * sizeof(T);
+  void* base;
+  GB_TRY(get_stage(c, round256(nc) + round256(na) + round256(nb), &base));
+  T* dC = static_cast<T*>(base);
+  T* da = reinterpret_cast<T*>(static_cast<char*>(base) + round256(nc));
+  T* db = reinterpret_cast<T*>(static_cast<char*>(base) + round256(nc) + round256(na));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(dC, C, nc, s));
+  GB_TRY(h2d(da, a, na, s));
+  GB_TRY(h2d(db, b, nb, s));
+  GB_TRY(outer_any<T>(c, lc, M, N, da, db, dC, s));
+  GB_TRY(d2h(C, dC, nc, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status transpose_host(int64_t M, int64_t N, const T* A, int64_t rsa, int64_t csa, T* C, int64_t rsc,
+                             int64_t csc) {
+  GB_TRY(check_transpose<T>(M, N, A, rsa, csa, C, rsc, csc));
+  if (M == 0 || N == 0) return GBBLAS_STATUS_SUCCESS;
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const int64_t sa = span(M, N, rsa, csa), sc = span(N, M, rsc, csc);
+  const size_t na = (size_t)sa * sizeof(T), nc = (size_t)sc * sizeof(T);
+  void* base;
+  GB_TRY(get_stage(c, round256(na) + round256(nc), &base));
+  T* dA = static_cast<T*>(base);
+  T* dC = reinterpret_cast<T*>(static_cast<char*>(base) + round256(na));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(dA, A, na, s));
+  // a C with gaps between its elements keeps them: bring it over first
+  if (sc != M * N) GB_TRY(h2d(dC, C, nc, s));
+  GB_TRY(launch_transpose<T>(c, M, N, dA, rsa, csa, dC, rsc, csc, s));
+  GB_TRY(d2h(C, dC, nc, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status transpose_inplace_host(int64_t n, T* A) {
+  if (n < 0) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose in place: negative size");
+  if (n == 0) return GBBLAS_STATUS_SUCCESS;
+  if (!A) return bad(GBBLAS_STATUS_INVALID_VALUE, "transpose in place: null pointer");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t bytes = (size_t)(n * n) * sizeof(T);
+  void* base;
+  GB_TRY(get_stage(c, round256(bytes), &base));
+  T* dA = static_cast<T*>(base);
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(dA, A, bytes, s));
+  GB_TRY(launch_transpose_square<T>(c, n, dA, s));
+  GB_TRY(d2h(A, dA, bytes, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+template <typename T>
+gbblas_status ew_host(gbblas_ew_op op, int64_t n, const T* a, const T* b, T* out) {
+  GB_TRY(check_ew<T>(op, n, a, b, out));
+  if (n == 0) return GBBLAS_STATUS_SUCCESS;
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  HostGuard g(c);
+  const size_t bytes = (size_t)n * sizeof(T);
+  void* base;
+  GB_TRY(get_stage(c, 3 * round256(bytes), &base));
+  T* da = static_cast<T*>(base);
+  T* db = reinterpret_cast<T*>(static_cast<char*>(base) + round256(bytes));
+  T* dc = reinterpret_cast<T*>(static_cast<char*>(base) + 2 * round256(bytes));
+  cudaStream_t s = c->host_stream;
+  GB_TRY(h2d(da, a, bytes, s));
+  GB_TRY(h2d(db, b, bytes, s));
+  GB_TRY(launch_ew<T>(c, op, n, da, db, dc, s));
+  GB_TRY(d2h(out, dc, bytes, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBBLAS_STATUS_SUCCESS;
+}
+
 }  // namespace
 }  // namespace gbblas
 
@@ -502,6 +665,58 @@ gbblas_status gbblas_sdot_host(int64_t n, const float* a, const float* b, float*
 }
 gbblas_status gbblas_ddot_host(int64_t n, const double* a, const double* b, double* result) {
   return dot_host<double>(n, a, b, result);
+}
+
+gbblas_status gbblas_souter(gbblas_layout lc, int64_t M, int64_t N, const float* a, const float* b, float* C,
+                            void* stream) {
+  return outer_dev<float>(lc, M, N, a, b, C, stream);
+}
+gbblas_status gbblas_douter(gbblas_layout lc, int64_t M, int64_t N, const double* a, const double* b, double* C,
+                            void* stream) {
+  return outer_dev<double>(lc, M, N, a, b, C, stream);
+}
+gbblas_status gbblas_stranspose(int64_t M, int64_t N, const float* A, int64_t rsa, int64_t csa, float* C,
+                                int64_t rsc, int64_t csc, void* stream) {
+  return transpose_dev<float>(M, N, A, rsa, csa, C, rsc, csc, stream);
+}
+gbblas_status gbblas_dtranspose(int64_t M, int64_t N, const double* A, int64_t rsa, int64_t csa, double* C,
+                                int64_t rsc, int64_t csc, void* stream) {
+  return transpose_dev<double>(M, N, A, rsa, csa, C, rsc, csc, stream);
+}
+gbblas_status gbblas_stranspose_inplace(int64_t n, float* A, void* stream) {
+  return transpose_inplace_dev<float>(n, A, stream);
+}
+gbblas_status gbblas_dtranspose_inplace(int64_t n, double* A, void* stream) {
+  return transpose_inplace_dev<double>(n, A, stream);
+}
+gbblas_status gbblas_sew(gbblas_ew_op op, int64_t n, const float* a, const float* b, float* c, void* stream) {
+  return ew_dev<float>(op, n, a, b, c, stream);
+}
+gbblas_status gbblas_dew(gbblas_ew_op op, int64_t n, const double* a, const double* b, double* c, void* stream) {
+  return ew_dev<double>(op, n, a, b, c, stream);
+}
+gbblas_status gbblas_souter_host(gbblas_layout lc, int64_t M, int64_t N, const float* a, const float* b, float* C) {
+  return outer_host<float>(lc, M, N, a, b, C);
+}
+gbblas_status gbblas_douter_host(gbblas_layout lc, int64_t M, int64_t N, const double* a, const double* b,
+                                 double* C) {
+  return outer_host<double>(lc, M, N, a, b, C);
+}
+gbblas_status gbblas_stranspose_host(int64_t M, int64_t N, const float* A, int64_t rsa, int64_t csa, float* C,
+                                     int64_t rsc, int64_t csc) {
+  return transpose_host<float>(M, N, A, rsa, csa, C, rsc, csc);
+}
+gbblas_status gbblas_dtranspose_host(int64_t M, int64_t N, const double* A, int64_t rsa, int64_t csa, double* C,
+                                     int64_t rsc, int64_t csc) {
+  return transpose_host<double>(M, N, A, rsa, csa, C, rsc, csc);
+}
+gbblas_status gbblas_stranspose_inplace_host(int64_t n, float* A) { return transpose_inplace_host<float>(n, A); }
+gbblas_status gbblas_dtranspose_inplace_host(int64_t n, double* A) { return transpose_inplace_host<double>(n, A); }
+gbblas_status gbblas_sew_host(gbblas_ew_op op, int64_t n, const float* a, const float* b, float* c) {
+  return ew_host<float>(op, n, a, b, c);
+}
+gbblas_status gbblas_dew_host(gbblas_ew_op op, int64_t n, const double* a, const double* b, double* c) {
+  return ew_host<double>(op, n, a, b, c);
 }
 
 }  // extern "C"

@@ -160,6 +160,22 @@ gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t
 // Autotuner (tune.cu): AUTO accuracy -> 1 = split-BF16 six products, 0 = FMA.
 int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 
+// Streaming operations beside the hot path (stream_ops.cu).
+// C[r*ld + l] += u[r] * v[l] (rows of C contiguous).
+template <typename T>
+gbblas_status launch_outer(DeviceCtx* c, int64_t R, int64_t L, const T* u, const T* v, T* C, int64_t ld,
+                           cudaStream_t s);
+// C(j, i) = A(i, j): A(i, j) at A[i*rsa + j*csa], C(j, i) at C[j*rsc + i*csc].
+template <typename T>
+gbblas_status launch_transpose(DeviceCtx* c, int64_t M, int64_t N, const T* A, int64_t rsa, int64_t csa, T* C,
+                               int64_t rsc, int64_t csc, cudaStream_t s);
+// Square n x n storage transposed in place.
+template <typename T>
+gbblas_status launch_transpose_square(DeviceCtx* c, int64_t n, T* A, cudaStream_t s);
+// out[i] = a[i] op b[i].
+template <typename T>
+gbblas_status launch_ew(DeviceCtx* c, gbblas_ew_op op, int64_t n, const T* a, const T* b, T* out, cudaStream_t s);
+
 // Synchronise `stream` and report (then clear) any device-side error its
 // kernels recorded in the stream's scratch error word.
 gbblas_status check_stream_errors(DeviceCtx* c, cudaStream_t stream);

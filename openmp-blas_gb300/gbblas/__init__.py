@@ -78,7 +78,25 @@ SIGNATURES = {
     "gbblas_dvtm_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
     "gbblas_sdot_host": (_int, [_i64, _vp, _vp, _vp]),
     "gbblas_ddot_host": (_int, [_i64, _vp, _vp, _vp]),
+    "gbblas_souter": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_douter": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_stranspose": (_int, [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp]),
+    "gbblas_dtranspose": (_int, [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp]),
+    "gbblas_stranspose_inplace": (_int, [_i64, _vp, _vp]),
+    "gbblas_dtranspose_inplace": (_int, [_i64, _vp, _vp]),
+    "gbblas_sew": (_int, [_int, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_dew": (_int, [_int, _i64, _vp, _vp, _vp, _vp]),
+    "gbblas_souter_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_douter_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
+    "gbblas_stranspose_host": (_int, [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
+    "gbblas_dtranspose_host": (_int, [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
+    "gbblas_stranspose_inplace_host": (_int, [_i64, _vp]),
+    "gbblas_dtranspose_inplace_host": (_int, [_i64, _vp]),
+    "gbblas_sew_host": (_int, [_int, _i64, _vp, _vp, _vp]),
+    "gbblas_dew_host": (_int, [_int, _i64, _vp, _vp, _vp]),
 }
+
+EW_ADD, EW_SUB, EW_MUL, EW_DIV = 0, 1, 2, 3
 
 _lib = None
 

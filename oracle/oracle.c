@@ -30,6 +30,12 @@
  *     overwrite/accumulate rule)         include/mtv.hpp:164-236
  *   - dot in three size regimes           include/dot.hpp:16-54,143-174
  *   - dot with caller-given blocks        include/dot.hpp:59-90
+ *   - outer product, C += a b^T           include/outer.hpp:14-119,
+ *                                          include/simd_loop.hpp:42-47
+ *   - transpose, out of place and square in place
+ *                                          include/trans.hpp:33-169,
+ *                                          include/simd_loop.hpp:194-238
+ *   - element-wise + - * /                include/el_wise_op.hpp:33-112
  *
  * Element layouts follow uBLAS: "first order" = column-major (strides
  * {1, rows}), "last order" = row-major (strides {cols, 1}).
@@ -244,6 +250,16 @@ void orc_set_threads(int n) {
 /* ------------------------------------------------------------------------ */
 /* Type-generic parts, instantiated for float and double.                   */
 /* ------------------------------------------------------------------------ */
+
+/* Fused multiply-add by element type (the contraction the reference's
+ * -ffast-math build applies to `c += a * b`). */
+static inline float fmas_(float a, float b, float c) { return fmaf(a, b, c); }
+static inline double fmad_(double a, double b, double c) { return fma(a, b, c); }
+
+/* Correctly rounded IEEE quotients, exempt from -ffast-math (which may turn
+ * a float division into a reciprocal estimate plus a Newton step). */
+__attribute__((optimize("no-fast-math"), noinline)) static float divs_(float a, float b) { return a / b; }
+__attribute__((optimize("no-fast-math"), noinline)) static double divd_(double a, double b) { return a / b; }
 
 #define ORC_T float
 #define ORC_S s

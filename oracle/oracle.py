@@ -78,6 +78,18 @@ def lib():
             f = getattr(L, f"orc_{s}dot_exact")
             f.argtypes = [_c_size, _vp, _vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             f.restype = None
+            f = getattr(L, f"orc_{s}outer")
+            f.argtypes = [ctypes.c_int, _c_size, _c_size, _vp, _vp, _vp]
+            f.restype = None
+            f = getattr(L, f"orc_{s}transpose")
+            f.argtypes = [_c_size, _c_size, _vp, _c_pd, _c_pd, _vp, _c_pd, _c_pd]
+            f.restype = None
+            f = getattr(L, f"orc_{s}transpose_inplace")
+            f.argtypes = [_c_size, _vp]
+            f.restype = None
+            f = getattr(L, f"orc_{s}ew")
+            f.argtypes = [ctypes.c_int, _c_size, _vp, _vp, _vp]
+            f.restype = None
         L.orc_sgemm_sample_exact.argtypes = [_c_size, _vp, _c_pd, _c_pd, _vp, _c_pd, _c_pd, _c_size, _vp, _vp, _vp, _vp]
         L.orc_sgemm_sample_exact.restype = None
         L.orc_cache_info.argtypes = [_vp, _vp, _vp]
@@ -109,6 +121,18 @@ def ref():
                 f = getattr(R, f"ref_{s}dot_tuning")
                 f.argtypes = [_c_size, _vp, _vp, _c_size, _c_size, _c_size]
                 f.restype = T
+                f = getattr(R, f"ref_{s}outer")
+                f.argtypes = [ctypes.c_int, _c_size, _c_size, _vp, _vp, _vp]
+                f.restype = ctypes.c_int
+                f = getattr(R, f"ref_{s}transpose")
+                f.argtypes = [ctypes.c_int, ctypes.c_int, _c_size, _c_size, _vp, _vp]
+                f.restype = ctypes.c_int
+                f = getattr(R, f"ref_{s}transpose_inplace")
+                f.argtypes = [_c_size, _vp]
+                f.restype = ctypes.c_int
+                f = getattr(R, f"ref_{s}ew")
+                f.argtypes = [ctypes.c_int, _c_size, _vp, _vp, _vp]
+                f.restype = ctypes.c_int
             R.ref_spack.argtypes = [_vp, _c_size, _vp, _vp, _c_size, _c_size, ctypes.c_int]
             R.ref_cache_info.argtypes = [_vp, _vp, _vp]
             _ref = R
@@ -257,6 +281,51 @@ def set_threads(n: int) -> None:
     lib().orc_set_threads(n)
 
 
+def outer(a, b, C, layout):
+    """C (M x N, logical) += a b^T computed in `layout`; returns the new C."""
+    M, N = C.shape
+    dt = C.dtype
+    c = to_layout(C, layout).copy()
+    aa = np.ascontiguousarray(a, dtype=dt)
+    bb = np.ascontiguousarray(b, dtype=dt)
+    getattr(lib(), f"orc_{_sfx(dt)}outer")(layout, M, N, _ptr(aa), _ptr(bb), _ptr(c))
+    return from_layout(c, M, N, layout).copy()
+
+
+def transpose_raw(M, N, a, rsa, csa, c, rsc, csc) -> None:
+    """C(j, i) = A(i, j) on raw buffers with element strides."""
+    getattr(lib(), f"orc_{_sfx(a.dtype)}transpose")(M, N, _ptr(a), rsa, csa, _ptr(c), rsc, csc)
+
+
+def transpose(A, la, lc):
+    """A^T of the logical matrix A, computed from A stored in layout la into a
+    dense C stored in layout lc; returns the logical N x M result."""
+    M, N = A.shape
+    a = to_layout(A, la)
+    c = np.zeros(M * N, A.dtype)
+    rsa, csa = strides(M, N, la)
+    rsc, csc = strides(N, M, lc)
+    transpose_raw(M, N, a, rsa, csa, c, rsc, csc)
+    return from_layout(c, N, M, lc).copy()
+
+
+def transpose_inplace(buf):
+    """Square n x n storage transposed in place (returns a new array)."""
+    b = np.ascontiguousarray(buf).copy()
+    n = int(round(np.sqrt(b.size)))
+    getattr(lib(), f"orc_{_sfx(b.dtype)}transpose_inplace")(n, _ptr(b))
+    return b
+
+
+def ew(op, a, b):
+    """a op b element by element: op 0 add, 1 sub, 2 mul, 3 div."""
+    aa = np.ascontiguousarray(a)
+    bb = np.ascontiguousarray(b, dtype=aa.dtype)
+    c = np.empty_like(aa)
+    getattr(lib(), f"orc_{_sfx(aa.dtype)}ew")(op, aa.size, _ptr(aa), _ptr(bb), _ptr(c))
+    return c
+
+
 # --------------------------------------------------------------------------
 # Reference (compiled from the reference's own headers)
 # --------------------------------------------------------------------------
@@ -321,3 +390,42 @@ def ref_pack(inp, wi, wo, m, n, out, offset_in=0, offset_out=0, trans=False):
     w = np.asarray(wi, dtype=np.uintp)
     isz = inp.itemsize
     ref().ref_spack(_ptr(out) + offset_out * isz, wo, _ptr(inp) + offset_in * isz, _ptr(w), m, n, 1 if trans else 0)
+
+
+def ref_outer(a, b, C, layout):
+    M, N = C.shape
+    dt = C.dtype
+    c = to_layout(C, layout).copy()
+    aa = np.ascontiguousarray(a, dtype=dt)
+    bb = np.ascontiguousarray(b, dtype=dt)
+    rc = getattr(ref(), f"ref_{_sfx(dt)}outer")(layout, M, N, _ptr(aa), _ptr(bb), _ptr(c))
+    if rc != 0:
+        raise RuntimeError("reference outer_prod threw")
+    return from_layout(c, M, N, layout).copy()
+
+
+def ref_transpose(A, la, lc):
+    M, N = A.shape
+    a = to_layout(A, la)
+    c = np.zeros(M * N, A.dtype)
+    rc = getattr(ref(), f"ref_{_sfx(A.dtype)}transpose")(la, lc, M, N, _ptr(a), _ptr(c))
+    if rc != 0:
+        raise RuntimeError("reference transpose threw")
+    return from_layout(c, N, M, lc).copy()
+
+
+def ref_transpose_inplace(buf):
+    b = np.ascontiguousarray(buf).copy()
+    n = int(round(np.sqrt(b.size)))
+    if getattr(ref(), f"ref_{_sfx(b.dtype)}transpose_inplace")(n, _ptr(b)) != 0:
+        raise RuntimeError("reference transpose threw")
+    return b
+
+
+def ref_ew(op, a, b):
+    aa = np.ascontiguousarray(a)
+    bb = np.ascontiguousarray(b, dtype=aa.dtype)
+    c = np.zeros_like(aa)
+    if getattr(ref(), f"ref_{_sfx(aa.dtype)}ew")(op, aa.size, _ptr(aa), _ptr(bb), _ptr(c)) != 0:
+        raise RuntimeError("reference element-wise op threw")
+    return c

@@ -1,7 +1,8 @@
 // ref_entry.cpp - C entry points over the reference's own hot-path headers.
 //
 // TEST INFRASTRUCTURE ONLY.  oracle/Makefile compiles this file together with
-// the reference's unmodified include/{mtm,mtv,dot}.hpp (read where they lie,
+// the reference's unmodified include/{mtm,mtv,dot,outer,trans,el_wise_op}.hpp
+// (read where they lie,
 // never copied) and the project's uBLAS-tensor compat shim into
 // oracle/_ref/libamt_ref.so.  Tests use it to pin the C restatement in
 // oracle/oracle.c and tests/golden/make_golden.py uses it to write golden
@@ -19,8 +20,11 @@
 #include <optional>
 
 #include <dot.hpp>
+#include <el_wise_op.hpp>
 #include <mtm.hpp>
 #include <mtv.hpp>
+#include <outer.hpp>
+#include <trans.hpp>
 
 namespace ub = boost::numeric::ublas;
 
@@ -112,9 +116,110 @@ T dot_tuning_any(std::size_t n, T const* a, T const* b, std::size_t b1, std::siz
   return r;
 }
 
+// a and b as (1, n) first_order vectors, as test/test.outer_prod.cpp:37-38 builds them.
+template <class T, class LC>
+int outer_case(std::size_t M, std::size_t N, T const* a, T const* b, T* C) {
+  auto av = load<T, ub::layout::first_order>(1, M, a);
+  auto bv = load<T, ub::layout::first_order>(1, N, b);
+  auto c = load<T, LC>(M, N, C);
+  amt::outer_prod(c, av, bv, std::nullopt)();
+  std::memcpy(C, c.data(), M * N * sizeof(T));
+  return 0;
+}
+
+template <class T>
+int outer_any(int lc, std::size_t M, std::size_t N, T const* a, T const* b, T* C) {
+  try {
+    return lc ? outer_case<T, ub::layout::last_order>(M, N, a, b, C)
+              : outer_case<T, ub::layout::first_order>(M, N, a, b, C);
+  } catch (std::exception const&) {
+    return 1;
+  }
+}
+
+// C = A^T for dense A (M x N, layout la) into dense C (N x M, layout lc).
+template <class T, class LA, class LC>
+int transpose_case(std::size_t M, std::size_t N, T const* A, T* C) {
+  auto a = load<T, LA>(M, N, A);
+  mat<T, LC> c(N, M);
+  amt::transpose(c, a, std::nullopt)();
+  std::memcpy(C, c.data(), M * N * sizeof(T));
+  return 0;
+}
+
+template <class T>
+int transpose_any(int la, int lc, std::size_t M, std::size_t N, T const* A, T* C) {
+  try {
+    if (la)
+      return lc ? transpose_case<T, ub::layout::last_order, ub::layout::last_order>(M, N, A, C)
+                : transpose_case<T, ub::layout::last_order, ub::layout::first_order>(M, N, A, C);
+    return lc ? transpose_case<T, ub::layout::first_order, ub::layout::last_order>(M, N, A, C)
+              : transpose_case<T, ub::layout::first_order, ub::layout::first_order>(M, N, A, C);
+  } catch (std::exception const&) {
+    return 1;
+  }
+}
+
+// In place on a square n x n (the only shape the reference handles in place).
+template <class T>
+int transpose_inplace_any(std::size_t n, T* A) {
+  try {
+    auto a = load<T, ub::layout::first_order>(n, n, A);
+    amt::transpose(a, std::nullopt)();
+    std::memcpy(A, a.data(), n * n * sizeof(T));
+    return 0;
+  } catch (std::exception const&) {
+    return 1;
+  }
+}
+
+template <class T>
+int ew_case(int op, std::size_t n, T const* a, T const* b, T* c) {
+  auto av = load<T, ub::layout::first_order>(1, n, a);
+  auto bv = load<T, ub::layout::first_order>(1, n, b);
+  auto cv = load<T, ub::layout::first_order>(1, n, c);
+  switch (op) {
+    case 0: amt::el_op::add(cv, av, bv, std::nullopt); break;
+    case 1: amt::el_op::sub(cv, av, bv, std::nullopt); break;
+    case 2: amt::el_op::mul(cv, av, bv, std::nullopt); break;
+    default: amt::el_op::div(cv, av, bv, std::nullopt); break;
+  }
+  std::memcpy(c, cv.data(), n * sizeof(T));
+  return 0;
+}
+
+template <class T>
+int ew_any(int op, std::size_t n, T const* a, T const* b, T* c) {
+  try {
+    return ew_case(op, n, a, b, c);
+  } catch (std::exception const&) {
+    return 1;
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int ref_souter(int lc, std::size_t M, std::size_t N, float const* a, float const* b, float* C) {
+  return outer_any<float>(lc, M, N, a, b, C);
+}
+int ref_douter(int lc, std::size_t M, std::size_t N, double const* a, double const* b, double* C) {
+  return outer_any<double>(lc, M, N, a, b, C);
+}
+int ref_stranspose(int la, int lc, std::size_t M, std::size_t N, float const* A, float* C) {
+  return transpose_any<float>(la, lc, M, N, A, C);
+}
+int ref_dtranspose(int la, int lc, std::size_t M, std::size_t N, double const* A, double* C) {
+  return transpose_any<double>(la, lc, M, N, A, C);
+}
+int ref_stranspose_inplace(std::size_t n, float* A) { return transpose_inplace_any<float>(n, A); }
+int ref_dtranspose_inplace(std::size_t n, double* A) { return transpose_inplace_any<double>(n, A); }
+int ref_sew(int op, std::size_t n, float const* a, float const* b, float* c) { return ew_any<float>(op, n, a, b, c); }
+int ref_dew(int op, std::size_t n, double const* a, double const* b, double* c) {
+  return ew_any<double>(op, n, a, b, c);
+}
+
 
 int ref_sgemm(int lc, int la, int lb, std::size_t M, std::size_t N, std::size_t K, float const* A,
               float const* B, float* C) {

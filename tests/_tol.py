@@ -35,3 +35,28 @@ def assert_vec_close(got, ref, scale, K, dtype, c=C_GEMM, what=""):
         i = int(np.argmax(err / tol))
         raise AssertionError(f"{what}: {bad.sum()} entries beyond c*K*eps; worst at {i}: got {got[i]!r} "
                              f"ref {ref[i]!r} tol {tol[i]:.3g}")
+
+
+# The reference's f32 division under its -ffast-math x86 build is a
+# reciprocal estimate refined by one Newton step, up to 3 ulp from the IEEE
+# quotient (measured on 10^5 random quotients); this build divides exactly.
+REF_F32_DIV_ULP = 4
+
+
+def ulp_distance(x, y):
+    """Distance in units in the last place between same-sign finite floats."""
+    x = np.asarray(x)
+    y = np.asarray(y)
+    it = np.int32 if x.dtype == np.float32 else np.int64
+    return np.abs(x.view(it).astype(np.int64) - y.view(it).astype(np.int64))
+
+
+def assert_ew_matches_reference(got, ref, op):
+    """Element-wise results against values the reference produced: bit equality,
+    except float division (see REF_F32_DIV_ULP)."""
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    if op == 3 and got.dtype == np.float32:
+        assert np.all(ulp_distance(got, ref) <= REF_F32_DIV_ULP)
+    else:
+        np.testing.assert_array_equal(got, ref)

@@ -1,6 +1,7 @@
-// Drop-in test of include/{mtm,mtv,dot}.hpp: the reference's own test cases
-// (test/test.mtm.cpp, test.mtv.cpp, test.vtm.cpp, test.dot_prod.cpp,
-// test.pack.cpp) rewritten without Catch2/BLIS, calling the amt:: templates
+// Drop-in test of include/{mtm,mtv,dot,outer,trans,el_wise_op}.hpp: the
+// reference's own test cases (test/test.mtm.cpp, test.mtv.cpp, test.vtm.cpp,
+// test.dot_prod.cpp, test.pack.cpp, test.outer_prod.cpp, test.trans.cpp)
+// rewritten without Catch2/BLIS/Eigen, calling the amt:: templates
 // exactly as the reference's tests do - `amt::mtm(rres, A, B, std::nullopt)();`
 // - and checking the results against the CPU oracle (oracle/oracle.c), the
 // reference's arithmetic restated.  Built and run by tests/test_dropin_cpp.py.
@@ -14,8 +15,11 @@
 #include <vector>
 
 #include <dot.hpp>
+#include <el_wise_op.hpp>
 #include <mtm.hpp>
 #include <mtv.hpp>
+#include <outer.hpp>
+#include <trans.hpp>
 
 extern "C" {
 int orc_sgemm(size_t, size_t, size_t, const float*, ptrdiff_t, ptrdiff_t, const float*, ptrdiff_t, ptrdiff_t, float*,
@@ -26,6 +30,8 @@ void orc_smtv(int, size_t, size_t, const float*, const float*, float*);
 void orc_dmtv(int, size_t, size_t, const double*, const double*, double*);
 void orc_svtm(int, size_t, size_t, const float*, const float*, float*);
 void orc_dvtm(int, size_t, size_t, const double*, const double*, double*);
+void orc_souter(int, size_t, size_t, const float*, const float*, float*);
+void orc_douter(int, size_t, size_t, const double*, const double*, double*);
 }
 
 namespace ub = boost::numeric::ublas;
@@ -171,6 +177,70 @@ void pack_case() {
   for (auto& p : trans) REQUIRE(in[p[0]] == out[p[1]]);
 }
 
+// test/test.outer_prod.cpp: square and rectangular sizes 2..33, both layouts
+template <typename T, typename LC>
+void outer_case() {
+  constexpr int lay = std::is_same_v<LC, ub::layout::last_order> ? 1 : 0;
+  for (std::size_t m = 2; m < 34; m += 3) {
+    for (std::size_t n = 2; n < 34; n += 5) {
+      auto a = amt::make_tensor<T>(1ul, m);
+      auto b = amt::make_tensor<T>(1ul, n);
+      rand_gen<T>(a);
+      rand_gen<T>(b);
+      auto lres = amt::make_tensor<T, LC>(m, n, T(1));
+      auto rres = amt::make_tensor<T, LC>(m, n, T(1));
+      if constexpr (std::is_same_v<T, float>)
+        orc_souter(lay, m, n, a.data(), b.data(), lres.data());
+      else
+        orc_douter(lay, m, n, a.data(), b.data(), lres.data());
+      amt::outer_prod(rres, a, b, std::nullopt)();
+      for (std::size_t i = 0; i < rres.size(); ++i) REQUIRE(rres[i] == lres[i]);
+    }
+  }
+}
+
+// test/test.trans.cpp: out of place (every layout pair) and in place, sizes 2..31
+template <typename T, typename LA, typename LC>
+void trans_case() {
+  for (std::size_t sz = 2; sz < 32; ++sz) {
+    for (std::size_t n2 : {sz, sz + 3}) {
+      auto A = amt::make_tensor<T, LA>(sz, n2);
+      rand_gen<T>(A);
+      auto C = amt::make_tensor<T, LC>(n2, sz);
+      amt::transpose(C, A, std::nullopt)();
+      for (std::size_t i = 0; i < sz; ++i)
+        for (std::size_t j = 0; j < n2; ++j) REQUIRE(C(j, i) == A(i, j));
+    }
+    auto S = amt::make_tensor<T, LA>(sz, sz);
+    rand_gen<T>(S);
+    auto orig = S;
+    amt::transpose(S, std::nullopt)();
+    for (std::size_t i = 0; i < sz; ++i)
+      for (std::size_t j = 0; j < sz; ++j) REQUIRE(S(i, j) == orig(j, i));
+  }
+}
+
+template <typename T>
+void el_wise_case() {
+  for (std::size_t n : {1ul, 7ul, 1000ul, 4099ul}) {
+    auto a = amt::make_tensor<T>(1ul, n);
+    auto b = amt::make_tensor<T>(1ul, n);
+    auto c = amt::make_tensor<T>(1ul, n);
+    rand_gen<T>(a);
+    std::generate(b.begin(), b.end(), [] { return static_cast<T>(std::rand() % 100 + 1); });
+    amt::el_op::add(c, a, b, std::nullopt);
+    for (std::size_t i = 0; i < n; ++i) REQUIRE(c[i] == a[i] + b[i]);
+    amt::el_op::sub(c, a, b, std::nullopt);
+    for (std::size_t i = 0; i < n; ++i) REQUIRE(c[i] == a[i] - b[i]);
+    amt::el_op::mul(c, a, b, std::nullopt);
+    for (std::size_t i = 0; i < n; ++i) REQUIRE(c[i] == a[i] * b[i]);
+    amt::el_op::div(c, a, b, std::nullopt);
+    for (std::size_t i = 0; i < n; ++i) REQUIRE(c[i] == a[i] / b[i]);
+    amt::el_op::apply_ops(c, a, b, std::nullopt, std::multiplies<T>{});
+    for (std::size_t i = 0; i < n; ++i) REQUIRE(c[i] == a[i] * b[i]);
+  }
+}
+
 void error_cases() {
   // shape errors throw std::runtime_error when the callable is created
   auto A = amt::make_tensor<float>(4, 5);
@@ -204,6 +274,24 @@ void error_cases() {
     threw = true;
   }
   REQUIRE(threw);
+  threw = false;
+  auto rect = amt::make_tensor<float>(3, 5);
+  try {
+    auto f = amt::transpose(rect, std::nullopt);  // in place needs a square matrix
+    (void)f;
+  } catch (std::runtime_error const&) {
+    threw = true;
+  }
+  REQUIRE(threw);
+  threw = false;
+  auto o = amt::make_tensor<float>(4, 4);
+  try {
+    auto f = amt::outer_prod(o, v, notvec, std::nullopt);
+    (void)f;
+  } catch (std::runtime_error const&) {
+    threw = true;
+  }
+  REQUIRE(threw);
 }
 
 int main() {
@@ -222,6 +310,16 @@ int main() {
   mv_case<double, ub::layout::last_order, true>();
   dot_case<float>();
   dot_case<double>();
+  outer_case<float, ub::layout::first_order>();
+  outer_case<float, ub::layout::last_order>();
+  outer_case<double, ub::layout::first_order>();
+  outer_case<double, ub::layout::last_order>();
+  trans_case<float, ub::layout::first_order, ub::layout::first_order>();
+  trans_case<float, ub::layout::first_order, ub::layout::last_order>();
+  trans_case<float, ub::layout::last_order, ub::layout::first_order>();
+  trans_case<double, ub::layout::last_order, ub::layout::last_order>();
+  el_wise_case<float>();
+  el_wise_case<double>();
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;
 }

@@ -5,7 +5,7 @@ Run here, where the reference sources exist:
     make -C oracle ref && python tests/golden/make_golden.py
 
 The outputs come from oracle/_ref/libamt_ref.so, i.e. the reference's
-include/{mtm,mtv,dot}.hpp compiled unmodified.  The inputs follow the
+include/{mtm,mtv,dot,outer,trans,el_wise_op}.hpp compiled unmodified.  The inputs follow the
 reference tests' rule of integer values in [0, 99] (test/test_utils.hpp:4-8),
 drawn here from a seeded numpy generator and stored as uint8, so every
 product and every partial sum below 2**24 is exact in float32: for those
@@ -24,7 +24,13 @@ Cases:
         correctly (include/mtv.hpp:224-227);
   dot   the closed form of test/test.dot_prod.cpp (iota . iota) and random
         integer vectors crossing the three size regimes of include/dot.hpp;
-  pack  the 3x3 known answers of test/test.pack.cpp:8-83.
+  pack  the 3x3 known answers of test/test.pack.cpp:8-83;
+  outer C += a b^T, both layouts, integer and uniform values (one fused
+        multiply-add per element, so every value is pinned bit for bit),
+        sizes as test/test.outer_prod.cpp;
+  transpose  out of place for all four layout pairs, and in place for square
+        sizes (test/test.trans.cpp);
+  ew    c = a op b for the four std functors of include/el_wise_op.hpp.
 """
 from __future__ import annotations
 
@@ -57,7 +63,7 @@ def main() -> None:
         names.append(name)
         for k, v in arrs.items():
             v = np.asarray(v)
-            if v.size > 64 and k not in ("C", "y", "r", "out"):
+            if v.size > 64 and k not in ("C", "y", "r", "out", "c"):
                 key = shared.get(id(v))
                 if key is None:
                     key = f"in/{len(shared)}"
@@ -144,6 +150,35 @@ def main() -> None:
         ib = min(2, 3 - i)
         O.ref_pack(inp, w, ib, ib, 3, out, offset_in=i * w[1], offset_out=i * 3, trans=True)
     put("pack_trans_3x3", inp=inp, out=out)
+
+    # ---------------- outer / transpose / element-wise ----------------
+    for dt in (np.float32, np.float64):
+        tn = np.dtype(dt).name
+        for (M, N) in [(2, 2), (7, 5), (31, 32), (33, 17)]:
+            a8 = rng.integers(0, 100, M, dtype=np.uint8)
+            b8 = rng.integers(0, 100, N, dtype=np.uint8)
+            C8 = rng.integers(0, 100, (M, N), dtype=np.uint8).astype(dt)
+            au = rng.uniform(-1, 1, M).astype(dt)
+            bu = rng.uniform(-1, 1, N).astype(dt)
+            Cu = rng.uniform(-1, 1, (M, N)).astype(dt)
+            for lc in (0, 1):
+                put(f"outer_{tn}_{M}x{N}_c{lc}_int", a=a8, b=b8, C0=C8,
+                    C=O.ref_outer(a8.astype(dt), b8.astype(dt), C8, lc), lc=lc)
+                # one fused multiply-add per element: bit-exact for any values
+                put(f"outer_{tn}_{M}x{N}_c{lc}_uniform", a=au, b=bu, C0=Cu, C=O.ref_outer(au, bu, Cu, lc), lc=lc)
+        for (M, N) in [(2, 2), (5, 7), (32, 31), (40, 3)]:
+            A = rng.uniform(-1, 1, (M, N)).astype(dt)
+            for la in (0, 1):
+                for lc in (0, 1):
+                    put(f"transpose_{tn}_{M}x{N}_a{la}c{lc}", A=A, C=O.ref_transpose(A, la, lc), la=la, lc=lc)
+        for n in (2, 3, 31, 32, 33):
+            buf = rng.uniform(-1, 1, n * n).astype(dt)
+            put(f"transpose_inplace_{tn}_{n}", inp=buf, out=O.ref_transpose_inplace(buf), n=n)
+        for n in (1, 7, 1000):
+            a = rng.uniform(-1, 1, n).astype(dt)
+            b = (rng.uniform(0.5, 2, n) * rng.choice([-1, 1], n)).astype(dt)
+            for op in range(4):
+                put(f"ew_{tn}_{n}_op{op}", a=a, b=b, c=O.ref_ew(op, a, b), op=op)
 
     g["_names"] = np.array(names)
     np.savez_compressed(OUT, **g)

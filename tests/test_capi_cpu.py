@@ -50,6 +50,17 @@ def test_status_strings():
     ("gbblas_sdot", (-5, 16, 16, 16, None)),
     ("gbblas_sdot", (5, None, 16, 16, None)),
     ("gbblas_ddot_tuning", (5, 16, 16, 0, 1, 1, 16, None)),
+    ("gbblas_souter", (2, 4, 4, 16, 16, 16, None)),
+    ("gbblas_douter", (1, -1, 4, 16, 16, 16, None)),
+    ("gbblas_souter", (1, 4, 4, None, 16, 16, None)),
+    ("gbblas_stranspose", (4, 4, 16, -1, 1, 16, 4, 1, None)),
+    ("gbblas_dtranspose", (4, 4, 16, 4, 1, 16, 0, 1, None)),
+    ("gbblas_stranspose", (4, 4, None, 4, 1, 16, 4, 1, None)),
+    ("gbblas_stranspose_inplace", (-2, 16, None)),
+    ("gbblas_dtranspose_inplace", (3, None, None)),
+    ("gbblas_sew", (4, 8, 16, 16, 16, None)),
+    ("gbblas_dew", (0, -8, 16, 16, 16, None)),
+    ("gbblas_sew_host", (1, 8, None, 16, 16)),
 ])
 def test_invalid_arguments_rejected_without_device(fn, args):
     assert gbblas.status_of(fn, *args) == 1  # GBBLAS_STATUS_INVALID_VALUE

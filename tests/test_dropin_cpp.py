@@ -55,3 +55,14 @@ def test_dropin_runs_reference_cases_on_gpu(cuda):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert " 0 failures" in r.stdout
+
+
+def test_el_op_rejects_predicates_without_a_device_form(tmp_path):
+    src = tmp_path / "bad_pred.cpp"
+    src.write_text(
+        "#include <el_wise_op.hpp>\n"
+        "int main(){ auto a = amt::make_tensor<float>(1,4); auto c = amt::make_tensor<float>(1,4);\n"
+        "amt::el_op::apply_ops(c, a, a, std::nullopt, [](float x, float y){ return x > y ? x : y; }); }\n")
+    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", *INCLUDES, str(src)], capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "std::plus" in r.stderr

@@ -14,7 +14,7 @@ import pytest
 from oracle import oracle as O
 
 import _golden as G
-from _tol import assert_gemm_close, assert_vec_close
+from _tol import assert_ew_matches_reference, assert_gemm_close, assert_vec_close
 
 
 # ------------------------------------------------------------ known answers
@@ -208,3 +208,71 @@ def test_dot_vs_reference(dt):
         _, absdot = O.dot_exact(a, b)
         assert abs(O.dot(a, b) - O.ref_dot(a, b)) <= 2 * n * np.finfo(dt).eps * absdot
         assert abs(O.dot_tuning(a, b, 64, 32, 1024) - O.ref_dot_tuning(a, b, 64, 32, 1024)) <= 2 * n * np.finfo(dt).eps * absdot
+
+
+# ------------------------------------------- outer / transpose / element-wise
+
+def _dt(name):
+    return np.float64 if "float64" in name else np.float32
+
+
+@pytest.mark.parametrize("name", G.names("outer_"))
+def test_outer_golden_exact(name):
+    c = G.case(name)
+    dt = _dt(name)
+    got = O.outer(c["a"].astype(dt), c["b"].astype(dt), c["C0"].astype(dt), int(c["lc"]))
+    np.testing.assert_array_equal(got, c["C"])
+
+
+@pytest.mark.parametrize("name", [n for n in G.names("transpose_") if "inplace" not in n])
+def test_transpose_golden_exact(name):
+    c = G.case(name)
+    np.testing.assert_array_equal(O.transpose(c["A"], int(c["la"]), int(c["lc"])), c["C"])
+
+
+@pytest.mark.parametrize("name", G.names("transpose_inplace_"))
+def test_transpose_inplace_golden_exact(name):
+    c = G.case(name)
+    np.testing.assert_array_equal(O.transpose_inplace(c["inp"]), c["out"])
+
+
+@pytest.mark.parametrize("name", G.names("ew_"))
+def test_ew_golden(name):
+    c = G.case(name)
+    assert_ew_matches_reference(O.ew(int(c["op"]), c["a"], c["b"]), c["c"], int(c["op"]))
+
+
+def test_ew_division_is_ieee():
+    rng = np.random.default_rng(3)
+    a = rng.uniform(-1, 1, 10000).astype(np.float32)
+    b = rng.uniform(0.5, 3, 10000).astype(np.float32)
+    np.testing.assert_array_equal(O.ew(3, a, b), a / b)
+    np.testing.assert_array_equal(O.ew(3, a.astype(np.float64), b.astype(np.float64)), a.astype(np.float64) / b)
+
+
+def test_outer_matches_definition():
+    rng = np.random.default_rng(7)
+    a = rng.integers(-50, 50, 40).astype(np.float64)
+    b = rng.integers(-50, 50, 23).astype(np.float64)
+    C = rng.integers(-50, 50, (40, 23)).astype(np.float64)
+    for lc in (0, 1):
+        np.testing.assert_array_equal(O.outer(a, b, C, lc), C + np.outer(a, b))
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_stream_ops_bitexact_vs_reference(dt):
+    rng = np.random.default_rng(11)
+    for (M, N) in [(3, 2), (65, 129), (300, 7)]:
+        a, b = rng.uniform(-1, 1, M).astype(dt), rng.uniform(-1, 1, N).astype(dt)
+        C = rng.uniform(-1, 1, (M, N)).astype(dt)
+        A = rng.uniform(-1, 1, (M, N)).astype(dt)
+        for lc in (0, 1):
+            np.testing.assert_array_equal(O.outer(a, b, C, lc), O.ref_outer(a, b, C, lc))
+            for la in (0, 1):
+                np.testing.assert_array_equal(O.transpose(A, la, lc), O.ref_transpose(A, la, lc))
+    s = rng.uniform(-1, 1, 77 * 77).astype(dt)
+    np.testing.assert_array_equal(O.transpose_inplace(s), O.ref_transpose_inplace(s))
+    x, y = rng.uniform(-1, 1, 4099).astype(dt), rng.uniform(0.25, 4, 4099).astype(dt)
+    for op in range(4):
+        assert_ew_matches_reference(O.ew(op, x, y), O.ref_ew(op, x, y), op)
