@@ -807,9 +807,117 @@ def run_serving(args):
     srv.close()
 
 
+def run_stream_ops(args):
+    """The streaming operations beside the hot path, one JSON line each:
+    outer product C += a b^T (C 16384 x 16384 row-major f32; bytes 2*M*N*4 +
+    (M+N)*4), out-of-place transpose (16384 x 16384 f32, row-major in and
+    out; bytes 2*M*N*4) and element-wise add (2^28 f32; bytes 3*n*4), plus
+    their f64 forms.  U[-1,1) from seed 4; every operand is larger than L2.
+    GB/s of algorithmic bytes against the measured HBM copy bandwidth; the
+    CPU oracle (the reference's code restated) on a 4096^2 / 2^24 sample on
+    all host cores."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    peak, peak_kind = measured_peaks()
+    g = torch.Generator(device="cuda").manual_seed(4)
+    n2 = 16384
+    nvec = 1 << 28
+    for dt, tdt, pf in ((np.float32, torch.float32, "s"), (np.float64, torch.float64, "d")):
+        s = np.dtype(dt).itemsize
+
+        def U(*shape):
+            return torch.rand(*shape, generator=g, device="cuda", dtype=tdt) * 2 - 1
+        cases = []
+        A = U(n2, n2)
+        a, b = U(n2), U(n2)
+        C = torch.empty(n2, n2, device="cuda", dtype=tdt)
+        cases.append(("outer", 2 * n2 * n2 * s + 2 * n2 * s,
+                      lambda: gbblas.call(f"gbblas_{pf}outer", 1, n2, n2, a.data_ptr(), b.data_ptr(), A.data_ptr(),
+                                          None),
+                      f"C {n2}x{n2} row-major += a b^T"))
+        cases.append(("transpose", 2 * n2 * n2 * s,
+                      lambda: gbblas.call(f"gbblas_{pf}transpose", n2, n2, A.data_ptr(), n2, 1, C.data_ptr(), n2, 1,
+                                          None),
+                      f"C = A^T, {n2}x{n2} row-major"))
+        x, y = U(nvec // (s // 4)), U(nvec // (s // 4))
+        z = torch.empty_like(x)
+        nv = x.numel()
+        cases.append(("ew_add", 3 * nv * s,
+                      lambda: gbblas.call(f"gbblas_{pf}ew", 0, nv, x.data_ptr(), y.data_ptr(), z.data_ptr(), None),
+                      f"c = a + b, n = {nv}"))
+        for name, nbytes, fn, what in cases:
+            for _ in range(args.warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            iters = 20
+            with ClockSampler(0) as clk:
+                t0 = time.time()
+                e0.record()
+                for _ in range(iters):
+                    fn()
+                e1.record()
+                torch.cuda.synchronize()
+                clk.mark(t0, time.time())
+            gbblas.call("gbblas_check_stream", None)
+            ms = e0.elapsed_time(e1) / iters
+            gbs = nbytes / (ms / 1e3) / 1e9
+            line = {"metric": "streaming op GB/s", "op": name, "dtype": "f32" if s == 4 else "f64",
+                    "value": round(gbs, 1), "unit": "GB/s", "ms_per_call": round(ms, 4), "workload": what,
+                    "bytes": "algorithmic", "roofline": {"bound": "hbm", "achieved": round(gbs, 1),
+                                                        "peak": peak, "unit": "GB/s",
+                                                        "frac": round(gbs / peak, 4),
+                                                        "peak_source": peak_kind},
+                    "clocks": clk.summary()}
+            if not args.no_cpu:
+                rng = np.random.default_rng(4)
+                O.set_threads(os.cpu_count() or 1)
+                m = 4096
+                if name == "outer":
+                    hA = rng.uniform(-1, 1, (m, m)).astype(dt)
+                    ha, hb = rng.uniform(-1, 1, m).astype(dt), rng.uniform(-1, 1, m).astype(dt)
+                    buf = hA.ravel().copy()
+                    run = lambda: getattr(O.lib(), f"orc_{pf}outer")(1, m, m, ha.ctypes.data, hb.ctypes.data,
+                                                                          buf.ctypes.data)
+                    cb = 2 * m * m * s + 2 * m * s
+                    sample = f"{m}x{m}"
+                elif name == "transpose":
+                    hA = rng.uniform(-1, 1, m * m).astype(dt)
+                    hC = np.empty_like(hA)
+                    run = lambda: O.transpose_raw(m, m, hA, m, 1, hC, m, 1)
+                    cb = 2 * m * m * s
+                    sample = f"{m}x{m}"
+                else:
+                    k = 1 << 24
+                    hx, hy = rng.uniform(-1, 1, k).astype(dt), rng.uniform(-1, 1, k).astype(dt)
+                    hz = np.empty_like(hx)
+                    run = lambda: getattr(O.lib(), f"orc_{pf}ew")(0, k, hx.ctypes.data, hy.ctypes.data,
+                                                                       hz.ctypes.data)
+                    cb = 3 * k * s
+                    sample = f"n = {k}"
+                run()
+                t0 = time.perf_counter()
+                reps = 0
+                while time.perf_counter() - t0 < 2.0 or reps < 3:
+                    run()
+                    reps += 1
+                dtc = (time.perf_counter() - t0) / reps
+                line["cpu_baseline"] = {"value": round(cb / dtc / 1e9, 2), "unit": "GB/s",
+                                        "cores": os.cpu_count(), "kind": "port",
+                                        "sample": f"oracle restatement, {sample}, {reps} reps"}
+            print(json.dumps(line), flush=True)
+        del A, C, a, b, x, y, z
+        torch.cuda.empty_cache()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="bandwidth", choices=["bandwidth", "precision", "batching", "serving"])
+    ap.add_argument("--workload", default="bandwidth",
+                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops"])
     ap.add_argument("--rates", type=float, nargs="+", default=[1000, 2000, 5000, 10000, 20000, 50000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--min-requests", type=int, default=400)
@@ -847,6 +955,8 @@ def main():
         run_batching(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "stream_ops":
+        run_stream_ops(args)
     else:
         run_gpu(args)
 

@@ -52,33 +52,61 @@ __global__ void __launch_bounds__(kThreads) rank1_kernel(int64_t R, int64_t L, c
 
 // ---------------------------------------------------------------- transpose
 // C(j, i) = A(i, j) for i < M, j < N; A(i, j) at A[i*rsa + j*csa], C(j, i) at
-// C[j*rsc + i*csc].  32 x 32 tiles through shared memory: the tile is read
+// C[j*rsc + i*csc].  TILE x TILE tiles through shared memory: the tile is read
 // with consecutive threads along A's unit-stride index and written with
 // consecutive threads along C's, so both sides coalesce for every layout pair.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) transpose_kernel(int64_t M, int64_t N, const T* __restrict__ A,
-                                                             int64_t rsa, int64_t csa, T* __restrict__ C,
-                                                             int64_t rsc, int64_t csc, int64_t tiles_n,
-                                                             int64_t ntiles) {
-  __shared__ T tile[32][33];
+// Each thread first loads its (TILE/8) x (TILE/32) elements into registers,
+// so that many loads are in flight before the first shared-memory store.
+template <typename T, int TILE>
+__global__ void __launch_bounds__(kThreads, 3) transpose_kernel(int64_t M, int64_t N, const T* __restrict__ A,
+                                                                int64_t rsa, int64_t csa, T* __restrict__ C,
+                                                                int64_t rsc, int64_t csc, int64_t tiles_n,
+                                                                int64_t ntiles) {
+  constexpr int KR = TILE / 8, KC = TILE / 32;  // passes of the 32 x 8 thread block
+  __shared__ T tile[TILE][TILE + 1];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const bool a_rows = csa == 1;  // A's j (column) index is contiguous
   const bool c_rows = csc == 1;  // C's i index is contiguous
+  // pass (k, h) of the load touches tile element (ai + da, aj + db) ...
+  const int ai = a_rows ? ty : tx, aj = a_rows ? tx : ty;
+  const int64_t ak = a_rows ? 8 * rsa : 8 * csa, ah = a_rows ? 32 * csa : 32 * rsa;  // ... element steps
+  const int ci = c_rows ? tx : ty, cj = c_rows ? ty : tx;
+  const int64_t ck = c_rows ? 8 * rsc : 8 * csc, ch = c_rows ? 32 * csc : 32 * rsc;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int64_t i0 = (t / tiles_n) * 32, j0 = (t % tiles_n) * 32;
+    const int64_t i0 = (t / tiles_n) * TILE, j0 = (t % tiles_n) * TILE;
+    const bool full = i0 + TILE <= M && j0 + TILE <= N;
+    T r[KR][KC];
+    const T* pa = A + (i0 + ai) * rsa + (j0 + aj) * csa;
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int ii = a_rows ? ty + 8 * k : tx, jj = a_rows ? tx : ty + 8 * k;
-      const int64_t i = i0 + ii, j = j0 + jj;
-      if (i < M && j < N) tile[ii][jj] = A[i * rsa + j * csa];
+      for (int k = 0; k < KR; ++k)
+#pragma unroll
+        for (int h = 0; h < KC; ++h) r[k][h] = pa[k * ak + h * ah];
+    } else {
+#pragma unroll
+      for (int k = 0; k < KR; ++k)
+#pragma unroll
+        for (int h = 0; h < KC; ++h) {
+          const int ii = a_rows ? ai + 8 * k : ai + 32 * h, jj = a_rows ? aj + 32 * h : aj + 8 * k;
+          r[k][h] = (i0 + ii < M && j0 + jj < N) ? pa[k * ak + h * ah] : T(0);
+        }
     }
+#pragma unroll
+    for (int k = 0; k < KR; ++k)
+#pragma unroll
+      for (int h = 0; h < KC; ++h) {
+        const int ii = a_rows ? ai + 8 * k : ai + 32 * h, jj = a_rows ? aj + 32 * h : aj + 8 * k;
+        tile[ii][jj] = r[k][h];
+      }
     __syncthreads();
+    T* pc = C + (j0 + cj) * rsc + (i0 + ci) * csc;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int ii = c_rows ? tx : ty + 8 * k, jj = c_rows ? ty + 8 * k : tx;
-      const int64_t i = i0 + ii, j = j0 + jj;
-      if (i < M && j < N) C[j * rsc + i * csc] = tile[ii][jj];
-    }
+    for (int k = 0; k < KR; ++k)
+#pragma unroll
+      for (int h = 0; h < KC; ++h) {
+        const int ii = c_rows ? ci + 32 * h : ci + 8 * k, jj = c_rows ? cj + 8 * k : cj + 32 * h;
+        if (full || (i0 + ii < M && j0 + jj < N)) pc[k * ck + h * ch] = tile[ii][jj];
+      }
     __syncthreads();
   }
 }
@@ -207,11 +235,12 @@ template <typename T>
 gbblas_status launch_transpose(DeviceCtx* c, int64_t M, int64_t N, const T* A, int64_t rsa, int64_t csa, T* C,
                                int64_t rsc, int64_t csc, cudaStream_t s) {
   if (M == 0 || N == 0) return GBBLAS_STATUS_SUCCESS;
-  const int64_t tm = (M + 31) / 32, tn = (N + 31) / 32, nt = tm * tn;
+  constexpr int TILE = 64;  // 16 (f32) / 32 (f64) KB of shared memory per CTA
+  const int64_t tm = (M + TILE - 1) / TILE, tn = (N + TILE - 1) / TILE, nt = tm * tn;
   int64_t grid = nt;
-  const int64_t cap = (int64_t)c->num_sms * 16;
+  const int64_t cap = (int64_t)c->num_sms * 8;
   if (grid > cap) grid = cap;
-  transpose_kernel<T><<<(unsigned)grid, kThreads, 0, s>>>(M, N, A, rsa, csa, C, rsc, csc, tn, nt);
+  transpose_kernel<T, TILE><<<(unsigned)grid, kThreads, 0, s>>>(M, N, A, rsa, csa, C, rsc, csc, tn, nt);
   return check_launch("transpose_kernel");
 }
 
