@@ -914,10 +914,124 @@ def run_stream_ops(args):
         torch.cuda.empty_cache()
 
 
+def run_sweep(args):
+    """The reference's benchmark drivers (src/mtm.cpp:355-372, src/mtv.cpp:326-345,
+    src/dot.cpp:198-205) on the GPU: the same size sweeps, ones-filled
+    operands (make_tensor(..., 1.)), first_order float, MaxIter timed calls per
+    size averaged, GFLOP/s = ops / ns with the reference's op counts
+    (mtm M*N*(2K-1), mtv and dot as in their drivers), written in the
+    reference's metric formats (gbblas/metric.py: csv, summary text).
+
+    Series: "gbblas.GB300" (device-resident operands, CUDA events per call),
+    "gbblas.GB300.host" (the drop-in's host-buffer call, wall clock - what
+    amt::mtm(...)() costs a host caller), "Boost.ublas.tensor" (the
+    reference's algorithm on the host cores through the oracle port, which
+    restates it; sizes up to --sweep-cpu-max, 0 beyond)."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from gbblas.metric import Metric, reference_range
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    op = args.sweep_op
+    if op == "mtm":
+        x = reference_range(32.0, 3 * 1024.0, 32.0, "plus")
+        iters = 4
+    elif op == "mtv":
+        x = reference_range(2.0, float(1 << 16), 2.0, "multiplies")
+        iters = 10
+    else:
+        x = reference_range(2.0, float(1 << 20), 1024.0, "plus")
+        iters = 100
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    # GPU peak for the summary: FP32 FMA for mtm (152 SMs x 128 lanes x 2 flop x max clock),
+    # HBM-bound ops: flops at the measured copy bandwidth (2 flop per 4-byte element)
+    mhz = peaks.get("sm_max_mhz", 2070.0)
+    peak = 152 * 128 * 2 * mhz / 1e3 if op == "mtm" else peaks.get("hbm_gbs", 6680.8) / 2.0
+    m = Metric(len(x), np.float32, peak=peak)
+    gpu, host, cpu = m["gbblas.GB300"], m["gbblas.GB300.host"], m["Boost.ublas.tensor"]
+    O.set_threads(os.cpu_count() or 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for el in x:
+        n = int(el)
+        if op == "mtm":
+            ops = float(n) * n * (2.0 * n - 1.0)
+            A = torch.ones(n * n, device="cuda")
+            B = torch.ones(n * n, device="cuda")
+            C = torch.zeros(n * n, device="cuda")
+            dev_call = lambda: gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), 1, n, B.data_ptr(), 1, n,
+                                           C.data_ptr(), 1, n, 0, None)
+            hA, hB, hC = np.ones(n * n, np.float32), np.ones(n * n, np.float32), np.zeros(n * n, np.float32)
+            host_call = lambda: gbblas.call("gbblas_sgemm_host", n, n, n, hA.ctypes.data, 1, n, hB.ctypes.data, 1,
+                                            n, hC.ctypes.data, 1, n, 0)
+            cpu_call = lambda: O.gemm_raw(n, n, n, hA, 1, n, hB, 1, n, hC, 1, n)
+            cpu_ok = n <= args.sweep_cpu_max
+        elif op == "mtv":
+            ops = float(n) * (2.0 * n - 1.0)
+            A = torch.ones(n * n, device="cuda")
+            v = torch.ones(n, device="cuda")
+            y = torch.zeros(n, device="cuda")
+            dev_call = lambda: gbblas.call("gbblas_smtv", 0, n, n, A.data_ptr(), v.data_ptr(), y.data_ptr(), None)
+            hA, hv, hy = np.ones(n * n, np.float32), np.ones(n, np.float32), np.zeros(n, np.float32)
+            host_call = lambda: gbblas.call("gbblas_smtv_host", 0, n, n, hA.ctypes.data, hv.ctypes.data,
+                                            hy.ctypes.data)
+            cpu_call = lambda: O.mtv_raw(0, n, n, hA, hv, hy)
+            cpu_ok = n <= args.sweep_cpu_max * 16
+        else:
+            ops = 2.0 * n
+            a = torch.ones(n, device="cuda")
+            r = torch.zeros(1, device="cuda")
+            dev_call = lambda: gbblas.call("gbblas_sdot", n, a.data_ptr(), a.data_ptr(), r.data_ptr(), None)
+            ha, hr = np.ones(n, np.float32), np.zeros(1, np.float32)
+            host_call = lambda: gbblas.call("gbblas_sdot_host", n, ha.ctypes.data, ha.ctypes.data, hr.ctypes.data)
+            cpu_call = lambda: O.dot(ha, ha)
+            cpu_ok = True
+        dev_call()
+        torch.cuda.synchronize()
+        ns = 0.0
+        for _ in range(iters):
+            e0.record()
+            dev_call()
+            e1.record()
+            e1.synchronize()
+            ns += e0.elapsed_time(e1) * 1e6
+        gpu.update(ops / (ns / iters))
+        host_call()
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            host_call()
+        host.update(ops / ((time.perf_counter() - t0) * 1e9 / iters))
+        if cpu_ok and not args.no_cpu:
+            cpu_call()
+            t0 = time.perf_counter()
+            for _ in range(iters):
+                cpu_call()
+            cpu.update(ops / ((time.perf_counter() - t0) * 1e9 / iters))
+        else:
+            cpu.update(0.0)
+    gbblas.call("gbblas_check_stream", None)
+    csv_path = args.sweep_csv or os.path.join(ROOT, "gpurun_out", f"sweep_{op}.csv")
+    os.makedirs(os.path.dirname(csv_path), exist_ok=True)
+    m.csv(csv_path)
+    print(m.str("tensor"), file=sys.stderr)
+    line = {"metric": f"{op} sweep GFLOP/s", "unit": "GFLOP/s", "sizes": [int(v) for v in x], "max_iter": iters,
+            "series": {k: [round(v, 3) for v in d.plot] for k, d in m.data.items()},
+            "summary_peak": round(peak, 1), "csv": os.path.relpath(csv_path, ROOT),
+            "cpu": {"kind": "port", "cores": os.cpu_count(), "max_size": args.sweep_cpu_max},
+            "config": {"workload": f"reference driver sweep for {op}, first_order float, ones-filled"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="bandwidth",
-                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops"])
+                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops", "sweep"])
+    ap.add_argument("--sweep-op", default="mtm", choices=["mtm", "mtv", "dot"])
+    ap.add_argument("--sweep-cpu-max", type=int, default=1024,
+                    help="sweep workload: largest size the CPU series runs (0 beyond)")
+    ap.add_argument("--sweep-csv", default=None, help="sweep workload: CSV path (reference metric format)")
     ap.add_argument("--rates", type=float, nargs="+", default=[1000, 2000, 5000, 10000, 20000, 50000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--min-requests", type=int, default=400)
@@ -957,6 +1071,8 @@ def main():
         run_serving(args)
     elif args.workload == "stream_ops":
         run_stream_ops(args)
+    elif args.workload == "sweep":
+        run_sweep(args)
     else:
         run_gpu(args)
 
