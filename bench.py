@@ -254,6 +254,55 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def gemm_headline(dev, sp):
+    """The first part of the headline metric beside the bandwidth line
+    (outside the timed region): C = A*B at M = N = K = 8192 from float32
+    U[-1,1) (seed 2), split-BF16 with six products (FP32-accurate) and three
+    products against plain FP32 FMA; 2*M*N*K algorithmic flops, CUDA events
+    over 3 calls after 1 warm-up; max / mean relative error against
+    long-double dots on 1024 sampled entries.  The full two-input-set report
+    is `--workload precision`."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    n = 8192
+    g = torch.Generator(device=dev).manual_seed(2)
+    A = torch.rand(n, n, generator=g, device=dev) * 2 - 1
+    B = torch.rand(n, n, generator=g, device=dev) * 2 - 1
+    C = torch.zeros(n, n, device=dev)
+    rng = np.random.default_rng(2)
+    rows, cols = rng.integers(0, n, 1024), rng.integers(0, n, 1024)
+    An, Bn = A.cpu().numpy(), B.cpu().numpy()
+    exact, _ = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
+    out = {"config": "M=N=K=8192 float32 U[-1,1) seed 2, 2*M*N*K flops", "unit": "TFLOP/s"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for path, acc in (("bf16x6", 4), ("bf16x3", 1), ("fp32", 0)):
+        def call():
+            gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1, acc, sp)
+        call()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(3):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        gbblas.call("gbblas_check_stream", sp)
+        ms = e0.elapsed_time(e1) / 3
+        C.zero_()
+        call()
+        got = C.cpu().numpy()[rows, cols].astype(np.float64)
+        rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
+        out[path] = {"value": round(2.0 * n ** 3 / (ms / 1e3) / 1e12, 2), "ms": round(ms, 3),
+                     "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean())}
+    out["bf16x6_over_fp32"] = round(out["bf16x6"]["value"] / out["fp32"]["value"], 2)
+    out["bf16x3_over_fp32"] = round(out["bf16x3"]["value"] / out["fp32"]["value"], 2)
+    del A, B, C
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -406,6 +455,10 @@ def run_gpu(args):
                "sample": f"{len(times)} full steps (all four calls at full size) after 1 warm-up, "
                          f"mean {statistics.mean(times) * 1e3:.1f} ms/step, OpenMP on all host cores"}
 
+    gemm = None
+    if rank == 0 and not args.no_gemm:
+        gemm = gemm_headline(dev, sp)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -421,6 +474,7 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "clocks": clocks,
             "results": results,
+            "fp32_accurate_gemm": gemm,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -1049,6 +1103,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-gemm", action="store_true",
+                    help="default workload: skip the FP32-accurate GEMM figures added beside the line")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--small", action="store_true",
                     help="profiling case: mtv 8192^2 and dot 2^26 (still larger than L2), "

@@ -249,10 +249,25 @@ __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
 #pragma unroll
         for (int j = 0; j < 4; ++j) b[g * 4 + j] = t[j];
       }
+      if constexpr (sizeof(T) == 4) {
+        // packed FP32x2 FMAs: two columns per instruction, each lane an IEEE
+        // fmaf (bit-identical to the scalar form), half the issue slots
 #pragma unroll
-      for (int i = 0; i < TM; ++i)
+        for (int i = 0; i < TM; ++i) {
+          const float2 ai = make_float2(a[i], a[i]);
 #pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < TN; j += 2) {
+            const float2 r = __ffma2_rn(ai, make_float2(b[j], b[j + 1]), make_float2(acc[i][j], acc[i][j + 1]));
+            acc[i][j] = r.x;
+            acc[i][j + 1] = r.y;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
     }
     if (more) {
       store_a(buf ^ 1);
