@@ -90,3 +90,24 @@ def test_element_wise_past_2_pow_31(cuda):
     assert torch.equal(z[:1 << 20], x[:1 << 20] * 3.0)
     del x, y, z
     _free(torch)
+
+
+@pytest.mark.parametrize("accuracy", [0, 1, 2, 4])  # FP32, BF16X3, FP8, BF16X6
+def test_gemm_operand_past_2_pow_31_elements(cuda, accuracy):
+    """A is 40000 x 60000 (2.4e9 elements; its BF16 / FP8 arena is past 2^31
+    elements too): C = A * ones, A one only on its last 1000 columns and on
+    its last row."""
+    import gbblas
+    torch = cuda
+    M, K, N = 40000, 60000, 128
+    A = torch.zeros(M, K, device="cuda")
+    A[:, K - 1000:] = 1.0
+    A[M - 1, :] = 1.0
+    B = torch.ones(K, N, device="cuda")
+    C = torch.zeros(M, N, device="cuda")
+    gbblas.call("gbblas_sgemm", M, N, K, A.data_ptr(), K, 1, B.data_ptr(), N, 1, C.data_ptr(), N, 1, accuracy, None)
+    gbblas.call("gbblas_check_stream", None)
+    assert torch.all(C[:-1] == 1000.0)
+    assert torch.all(C[-1] == float(K))
+    del A, B, C
+    _free(torch)
