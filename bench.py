@@ -1086,7 +1086,7 @@ def main():
     ap.add_argument("--sweep-cpu-max", type=int, default=1024,
                     help="sweep workload: largest size the CPU series runs (0 beyond)")
     ap.add_argument("--sweep-csv", default=None, help="sweep workload: CSV path (reference metric format)")
-    ap.add_argument("--rates", type=float, nargs="+", default=[1000, 2000, 5000, 10000, 20000, 50000])
+    ap.add_argument("--rates", type=float, nargs="+", default=[500, 1000, 2000, 5000, 10000, 20000, 50000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--min-requests", type=int, default=400)
     ap.add_argument("--max-requests", type=int, default=4000)

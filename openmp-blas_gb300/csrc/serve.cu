@@ -83,7 +83,7 @@ int64_t working_set(const gbblas_request& r) {
 
 // Estimated GPU time (us) of a request from its flops / bytes and the rate of
 // the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP8
-// ~600, FP32 FMA ~50, FP64 ~0.8 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1
+// ~600, FP32 FMA ~55, FP64 ~1.2 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1
 // TFLOP/s).
 double estimate_us(const gbblas_request& r) {
   const double launch = 5.0;
@@ -92,9 +92,9 @@ double estimate_us(const gbblas_request& r) {
       const double fl = 2.0 * (double)r.M * (double)r.N * (double)r.K;
       double rate;  // flop per us
       if (r.dtype == GBBLAS_F64)
-        rate = 0.8e6;
+        rate = 1.2e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP32)
-        rate = 50e6;
+        rate = 55e6;
       else if (r.accuracy == GBBLAS_ACCURACY_BF16X3)
         rate = 430e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP8)
@@ -312,11 +312,13 @@ void scheduler_main(gbblas_server_s* s) {
         s->round_reqs_total += (int64_t)rd->reqs.size();
         if (s->inflight_bytes > s->stats.peak_inflight_bytes) s->stats.peak_inflight_bytes = s->inflight_bytes;
         // A heavy round's CTAs run for milliseconds and are not preempted by
-        // higher-priority streams: while light work is waiting or running,
-        // cap its grid at three quarters of the SMs so light rounds keep a
-        // quarter of the GPU; on an otherwise idle GPU it gets every SM.
-        if (heavy && (!s->pending.empty() || s->inflight_rounds > 0))
-          rd->max_ctas = std::max(1, s->ctx->num_sms * 3 / 4);
+        // higher-priority streams, and light requests that arrive after it
+        // started would find every SM taken: a heavy round's grid is capped
+        // at three quarters of the SMs, so light rounds always keep a quarter
+        // of the GPU.  (Capping only while light work was already queued let
+        // later arrivals wait behind whole heavy kernels: p99 2.3x the lone
+        // p99 at 1 k req/s against 1.1x with the permanent cap.)
+        if (heavy) rd->max_ctas = std::max(1, s->ctx->num_sms * 3 / 4);
         cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
         lk.unlock();
         gbblas_status e = launch_round(s, rd, st);
