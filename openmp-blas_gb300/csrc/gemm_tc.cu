@@ -23,9 +23,9 @@
 //      Split-BF16 (tcgen05.mma kind::f16, BF16 in, FP32 accumulate): C += sum
 //      of the piece products p_i(A) p_j(B) with i + j < P, into two TMEM
 //      accumulators - p0*p0 alone, and every smaller product together (so
-//      small terms are summed at their own scale); chunks of 512 K (the
-//      tensor core's own accumulation over long K is measurably less accurate
-//      than FP32).
+//      small terms are summed at their own scale); chunks of 512 K (P = 2) or
+//      128 K (P = 3): the tensor core's own accumulation over long K is
+//      measurably less accurate than FP32.
 //        P = 2 ("bf16x3"):  p0p0 + (p0p1 + p1p0)                     3 MMAs
 //        P = 3 ("bf16x6"):  p0p0 + (p0p1 + p1p0 + p0p2 + p1p1 + p2p0) 6 MMAs
 //      Three pieces hold all 24 significand bits of an FP32 value and the
@@ -76,7 +76,13 @@ using namespace tc;
 constexpr int kBM = 128;
 constexpr int kBN = 128;
 constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
-constexpr int kChunkTiles = 8;   // K slices folded into registers per chunk (512 of K)
+// K slices folded into FP32 registers per chunk: three-product split every
+// 512 of K, six-product split every 128 (the tensor core's accumulation over
+// a 512-K chunk made the six-product result's max relative error worse than
+// plain FP32 on operands spanning 2^+-10; at 128 it is 5x better, within 1 %
+// of the speed), FP8 every 128 (one scale block).
+constexpr int kChunkTiles3 = 8;
+constexpr int kChunkTiles6 = 2;
 constexpr int kTileRing = 4;     // tiles in flight between scheduler and consumers
 // FP8: chunks of scales in flight between producer and epilogue.  The ring
 // couples the producer to the epilogue, so it is deep enough (16 x 1 KB) that
@@ -94,7 +100,7 @@ struct ModeTraits {
   static constexpr bool fp8 = MODE == kModeFp8;
   static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
   static constexpr int kBKe = fp8 ? 128 : kBK;  // K elements per slice (128 bytes either way)
-  static constexpr int kChunk = fp8 ? 1 : kChunkTiles;  // slices per TMEM chunk (FP8: one scale block)
+  static constexpr int kChunk = fp8 ? 1 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
   // Epilogue warps: 4 (each 32 tile rows x 128 columns) or, for FP8, whose
   // chunks are four times shorter, 8 (32 rows x 64 columns each).
   static constexpr int kEpiWarps = fp8 ? 8 : 4;

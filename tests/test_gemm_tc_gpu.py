@@ -146,3 +146,27 @@ def test_auto_accuracy_small_uses_fp32_path(cuda):
     B = rng.uniform(-1, 1, (17, 9)).astype(np.float32)
     Z = np.zeros((33, 9), np.float32)
     np.testing.assert_array_equal(run(cuda, A, B, Z, 1, 1, 1, accuracy=3), run(cuda, A, B, Z, 1, 1, 1, accuracy=0))
+
+
+@pytest.mark.parametrize("dataset", ["uniform", "wide"])
+def test_six_products_at_most_fp32_max_relative_error(cuda, dataset):
+    """M = N = K = 1024 (seed 12): the six-product split's largest
+    elementwise relative error against FP64 is no larger than plain FP32's,
+    on U[-1,1) and on s * m * 2^e (e in [-10, 10]) operands."""
+    rng = np.random.default_rng(12)
+    n = 1024
+    if dataset == "uniform":
+        A = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+        B = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    else:
+        def wide(shape):
+            return (rng.choice([-1.0, 1.0], shape) * rng.uniform(1, 2, shape) *
+                    np.exp2(rng.integers(-10, 11, shape))).astype(np.float32)
+        A, B = wide((n, n)), wide((n, n))
+    Z = np.zeros((n, n), np.float32)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    denom = np.maximum(np.abs(exact), 1e-300)
+    r6 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=BF16X6) - exact) / denom)
+    r32 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=0) - exact) / denom)
+    print(f"{dataset}: max relative error bf16x6 {r6:.3e}  fp32 {r32:.3e}")
+    assert r6 <= r32
