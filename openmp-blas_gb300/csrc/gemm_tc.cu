@@ -37,9 +37,9 @@
 // Warp roles (192 threads; FP8: 320):
 //   warp 0      tile scheduler + TMA producer: takes the next tile from the
 //               global counter, publishes it in a shared-memory tile ring,
-//               then streams its K slices (2P tiles of 128 bytes of K each)
-//               into a stage ring with 2-D tiled bulk copies (128-byte
-//               swizzle);
+//               then streams its K slices (128 bytes of K of all P pieces of
+//               A and of B: one 3-D tiled bulk copy per operand, 128-byte
+//               swizzle) into a stage ring;
 //   warp 1      allocates TMEM and issues the MMAs (one elected lane);
 //               tcgen05.commit frees a stage once its MMAs have read it and
 //               signals a TMEM chunk buffer as full;
@@ -62,6 +62,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -84,6 +86,7 @@ constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
 constexpr int kChunkTiles3 = 8;
 constexpr int kChunkTiles6 = 2;
 constexpr int kTileRing = 4;     // tiles in flight between scheduler and consumers
+constexpr int kMaxStages = 8;    // operand stages in flight (as many as shared memory holds, up to this)
 // FP8: chunks of scales in flight between producer and epilogue.  The ring
 // couples the producer to the epilogue, so it is deep enough (16 x 1 KB) that
 // the operand stages, not the scales, bound how far the copies run ahead.
@@ -112,20 +115,20 @@ struct ModeTraits {
   static constexpr uint32_t kBufCols = 512 / kBufs;
 };
 
-template <int MODE>
+template <int MODE, bool PAIR>
 struct TcCfg {
   static constexpr int P = ModeTraits<MODE>::P;
-  static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A
-  static constexpr uint32_t kBBytes = kBN * 128;
+  static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A (this CTA's rows)
+  static constexpr uint32_t kBBytes = (PAIR ? kBN / 2 : kBN) * 128;  // B^T rows this CTA stages
   static constexpr uint32_t kStageBytes = P * (kABytes + kBBytes);
   static constexpr uint32_t kTmemCols = 512;  // the chunk buffers (ModeTraits::kBufs x kBufCols)
   // FP8: ring of per-chunk scales (128 row scales of A, 128 column scales of B)
   static constexpr uint32_t kScaleBytes = ModeTraits<MODE>::fp8 ? kScaleSlots * 2 * 128 * 4 : 0;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
   static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kScaleBytes) / kStageBytes);
-  static constexpr int kStages = kStagesFit > 6 ? 6 : kStagesFit;
+  static constexpr int kStages = kStagesFit > kMaxStages ? kMaxStages : kStagesFit;
   static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kScaleBytes + kBarBytes;
-  static_assert((2 * 6 + 2 * 4 + 2 * kTileRing + 2 * kScaleSlots + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
+  static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 2 * kScaleSlots + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
                 "barrier area too small");
   static_assert(kStages >= 2, "need at least a double-buffered stage ring");
   static_assert(kSmem <= kSmemLimit, "exceeds the 227 KB per-CTA shared memory limit");
@@ -301,8 +304,10 @@ __device__ __forceinline__ int find_problem(const TcProblem* __restrict__ probs,
   return lo;
 }
 
-// Output tile of global index t: grouped raster inside its problem
-// (consecutive tiles walk 8 row-tiles of one column band for L2 reuse).
+// Output tile of global index t (BMT rows x 128 columns): grouped raster
+// inside its problem (consecutive tiles walk 8 row-tiles of one column band
+// for L2 reuse).
+template <int BMT>
 __device__ __forceinline__ void tile_coords(const TcProblem& p, int t, int& m0, int& n0) {
   constexpr int kGroup = 8;
   const int local = t - p.tile_start;
@@ -311,20 +316,30 @@ __device__ __forceinline__ void tile_coords(const TcProblem& p, int t, int& m0, 
   const int first_m = g * kGroup;
   const int gm = min(p.tiles_m - first_m, kGroup);
   const int in_g = local % group_span;
-  m0 = (first_m + in_g % gm) * kBM;
+  m0 = (first_m + in_g % gm) * BMT;
   n0 = (in_g / gm) * kBN;
 }
 
-template <int MODE>
+// PAIR = false: one CTA per SM computes 128 x 128 tiles (tcgen05 .cta_group::1).
+// PAIR = true: clusters of two CTAs compute 256 x 128 tiles with
+// .cta_group::2 MMAs issued by the even CTA: each CTA stages its own 128 rows
+// of A and 64 of the 128 rows of B^T (so a CTA moves 3/4 of the operand bytes
+// per MMA flop of the single form, and fits more stages), both CTAs' copies
+// complete on the even CTA's stage barrier, its commits release both CTAs'
+// stages and signal both CTAs' epilogues, and both epilogues report drained
+// TMEM buffers to it.  Pairs walk tiles in a static order (cluster i takes
+// tiles i, i + clusters, ...), so both CTAs see the same sequence.
+template <int MODE, bool PAIR>
 __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                       const TcProblem* __restrict__ probs, int nprob, int total_tiles, int a_piece_rows,
                       int b_piece_rows, int* __restrict__ tile_counter, int* __restrict__ err,
                       const float* __restrict__ sa, const float* __restrict__ sb) {
   using MT = ModeTraits<MODE>;
-  using CF = TcCfg<MODE>;
+  using CF = TcCfg<MODE, PAIR>;
   constexpr int P = MT::P;
   constexpr int ST = CF::kStages;
+  constexpr int BMT = PAIR ? 2 * kBM : kBM;  // output tile rows (both CTAs of a pair)
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -350,6 +365,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;  // 0 = the CTA that issues the MMAs
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < ST; ++s) {
@@ -358,7 +374,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     }
     for (int b = 0; b < MT::kBufs; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], MT::kEpiWarps);  // one arrival per epilogue warp
+      mbar_init(&tempty[b], MT::kEpiWarps * (PAIR ? 2 : 1));  // one arrival per epilogue warp (of both CTAs)
     }
     for (int r = 0; r < kTileRing; ++r) {
       mbar_init(&ring_full[r], 1);
@@ -375,11 +391,17 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     prefetch_tensormap(&tm_b);
   }
   if (warp == 1) {
-    tmem_alloc(tmem_slot, CF::kTmemCols);
-    tmem_relinquish();
+    if constexpr (PAIR) {
+      tmem_alloc2(tmem_slot, CF::kTmemCols);
+      tmem_relinquish2();
+    } else {
+      tmem_alloc(tmem_slot, CF::kTmemCols);
+      tmem_relinquish();
+    }
   }
   tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) cluster_sync_all();  // the peer's barriers exist before anyone signals them
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -395,7 +417,11 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       bool stop = false;
       for (int it = 0; !stop; ++it) {
         const int slot = it % kTileRing, use = it / kTileRing;
-        int t = atomicAdd(tile_counter, 1);
+        int t;
+        if constexpr (PAIR)
+          t = (int)(blockIdx.x >> 1) + it * (int)(gridDim.x >> 1);
+        else
+          t = atomicAdd(tile_counter, 1);
         if (t >= total_tiles) t = -1;
         if (use > 0 && !mbar_wait_bounded(&ring_empty[slot], (use - 1) & 1, abort_flag, kWaitLimitNs)) {
           fail();
@@ -406,7 +432,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         if (t < 0) break;
         const TcProblem& pr = probs[find_problem(probs, nprob, t)];
         int m0, n0;
-        tile_coords(pr, t, m0, n0);
+        tile_coords<BMT>(pr, t, m0, n0);
+        const int own_m0 = m0 + (int)rank * kBM;  // this CTA's rows
         for (int kt = 0; kt < pr.num_kt; ++kt) {
           const int s = issued % ST, round = issued / ST;
           if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
@@ -414,18 +441,27 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             stop = true;
             break;
           }
-          mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
-          // piece p of A occupies rows [p*a_piece_rows, (p+1)*a_piece_rows) of the arena map
-#pragma unroll
-          for (int p = 0; p < P; ++p)
-            tma_load_2d(a_tile(s, p), &tm_a, &full[s], kt * MT::kBKe, p * a_piece_rows + pr.a_row + m0);
-#pragma unroll
-          for (int p = 0; p < P; ++p)
-            tma_load_2d(b_tile(s, p), &tm_b, &full[s], kt * MT::kBKe, p * b_piece_rows + pr.b_row + n0);
+          // one 3-D copy per operand brings all P piece planes of the tile
+          // (planes a_piece_rows / b_piece_rows rows apart in the arena)
+          if constexpr (PAIR) {
+            if (rank == 0) {
+              mbar_arrive_expect_tx(&full[s], 2 * CF::kStageBytes);  // both CTAs' copies
+              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
+              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
+            } else {
+              const uint32_t fb = mapa_shared(smem_u32(&full[s]), 0);
+              tma_load_3d_pair(a_tile(s, 0), &tm_a, fb, kt * MT::kBKe, pr.a_row + own_m0, 0);
+              tma_load_3d_pair(b_tile(s, 0), &tm_b, fb, kt * MT::kBKe, pr.b_row + n0 + kBN / 2, 0);
+            }
+          } else {
+            mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
+            tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
+            tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
+          }
           ++issued;
           if constexpr (MT::fp8) {
-            // this chunk's 128 row scales of A and 128 column scales of B
-            // (scale planes are K-block-major: both runs contiguous)
+            // this chunk's 128 row scales of A (this CTA's rows) and 128 column
+            // scales of B (scale planes are K-block-major: both runs contiguous)
             const int ss = sissued % kScaleSlots, sr = sissued / kScaleSlots;
             if (sr > 0 && !mbar_wait_bounded(&sempty[ss], (sr - 1) & 1, abort_flag, kWaitLimitNs)) {
               fail();
@@ -433,7 +469,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
               break;
             }
             mbar_arrive_expect_tx(&sfull[ss], 2 * 128 * 4);
-            bulk_load(scale_slot(ss), sa + (int64_t)kt * a_piece_rows + pr.a_row + m0, 128 * 4, &sfull[ss]);
+            bulk_load(scale_slot(ss), sa + (int64_t)kt * a_piece_rows + pr.a_row + own_m0, 128 * 4, &sfull[ss]);
             bulk_load(scale_slot(ss) + 128, sb + (int64_t)kt * b_piece_rows + pr.b_row + n0, 128 * 4, &sfull[ss]);
             ++sissued;
           }
@@ -441,8 +477,21 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      constexpr uint32_t idesc = MT::fp8 ? idesc_e4m3_f32(kBM, kBN) : idesc_bf16_f32(kBM, kBN);
+    if (lane == 0 && PAIR && rank != 0) {
+      // the odd CTA of a pair issues no MMAs: it only keeps its tile ring moving
+      for (int it = 0;; ++it) {
+        const int slot = it % kTileRing, use = it / kTileRing;
+        if (!mbar_wait_bounded(&ring_full[slot], use & 1, abort_flag, kWaitLimitNs)) {
+          fail();
+          break;
+        }
+        const int t = ring[slot];
+        mbar_arrive(&ring_empty[slot]);
+        if (t < 0) break;
+      }
+    } else if (lane == 0) {
+      constexpr uint32_t idesc =
+          MT::fp8 ? idesc_e4m3_f32(BMT, kBN) : idesc_bf16_f32(BMT, kBN);  // M = 256 for a pair
       int consumed = 0;  // K slices consumed (all tiles)
       int chunk_g = 0;   // chunks started (all tiles)
       bool stop = false;
@@ -462,7 +511,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
           const bool chunk_last = ((kt + 1) % MT::kChunk) == 0 || kt + 1 == num_kt;
           if (chunk_first) ++chunk_g;
           const int chunk = chunk_g - 1, b = chunk % MT::kBufs;
-          if (chunk_first && chunk >= MT::kBufs) {  // buffer b must have been drained by the epilogue
+          if (chunk_first && chunk >= MT::kBufs) {  // buffer b must have been drained by the epilogue(s)
             if (!mbar_wait_bounded(&tempty[b], ((chunk / MT::kBufs) - 1) & 1, abort_flag, kWaitLimitNs)) {
               fail();
               stop = true;
@@ -483,35 +532,54 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             a[p] = smem_u32(a_tile(s, p));
             bb[p] = smem_u32(b_tile(s, p));
           }
+          auto mma = [&](uint32_t d, uint32_t ad, uint32_t bd, uint32_t accumulate) {
+            if constexpr (PAIR) {
+              if constexpr (MT::fp8)
+                mma2_f8f6f4(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
+              else
+                mma2_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
+            } else {
+              if constexpr (MT::fp8)
+                mma_f8f6f4(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
+              else
+                mma_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
+            }
+          };
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             // 32 bytes along K per MMA inside the swizzled 128-byte row:
             // 16 bf16 (kind::f16) or 32 e4m3 (kind::f8f6f4)
             const uint32_t off = kk * 32;
             const uint32_t acc = (chunk_first && kk == 0) ? 0u : 1u;
-            if constexpr (MT::fp8) {
-              mma_f8f6f4(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc, acc);
-            } else {
-              mma_f16(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc, acc);
+            mma(acc_main, a[0] + off, bb[0] + off, acc);
+            if constexpr (!MT::fp8) {
               // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
-              mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[1] + off), idesc, acc);
-              mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
+              mma(acc_corr, a[0] + off, bb[1] + off, acc);
+              mma(acc_corr, a[1] + off, bb[0] + off, 1u);
               if constexpr (P == 3) {
-                mma_f16(acc_corr, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[2] + off), idesc, 1u);
-                mma_f16(acc_corr, sw128_kmajor_desc(a[1] + off), sw128_kmajor_desc(bb[1] + off), idesc, 1u);
-                mma_f16(acc_corr, sw128_kmajor_desc(a[2] + off), sw128_kmajor_desc(bb[0] + off), idesc, 1u);
+                mma(acc_corr, a[0] + off, bb[2] + off, 1u);
+                mma(acc_corr, a[1] + off, bb[1] + off, 1u);
+                mma(acc_corr, a[2] + off, bb[0] + off, 1u);
               }
             }
           }
-          mma_commit(&empty[s]);
-          if (chunk_last) mma_commit(&tfull[b]);
+          if constexpr (PAIR) {
+            mma_commit2(&empty[s], 3);  // both CTAs' stage s
+            if (chunk_last) mma_commit2(&tfull[b], 3);
+          } else {
+            mma_commit(&empty[s]);
+            if (chunk_last) mma_commit(&tfull[b]);
+          }
           ++consumed;
         }
       }
       // accf completes once every MMA issued above has finished, on the
-      // normal path and after an abort alike, so TMEM is never freed under a
-      // running MMA.
-      mma_commit(accf);
+      // normal path and after an abort alike, so TMEM (and, for a pair, the
+      // peer's shared memory) is never released under a running MMA.
+      if constexpr (PAIR)
+        mma_commit2(accf, 1);
+      else
+        mma_commit(accf);
       if (*abort_flag) {
         int never = 0;
         (void)mbar_wait_bounded(accf, 0, &never, kWaitLimitNs);
@@ -539,7 +607,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       if (t < 0) break;
       const TcProblem& pr = probs[find_problem(probs, nprob, t)];
       int m0, n0;
-      tile_coords(pr, t, m0, n0);
+      tile_coords<BMT>(pr, t, m0, n0);
+      m0 += (int)rank * kBM;  // this CTA's rows
       const int nchunks = (pr.num_kt + MT::kChunk - 1) / MT::kChunk;
       float acc[kCols];
 #pragma unroll
@@ -607,7 +676,12 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&tempty[b]);
+        if (lane == 0) {
+          if constexpr (PAIR)
+            mbar_arrive_cluster(mapa_shared(smem_u32(&tempty[b]), 0));  // the MMA-issuing CTA's barrier
+          else
+            mbar_arrive(&tempty[b]);
+        }
       }
       if (!ok) break;
       const int aborted = __shfl_sync(0xffffffffu, *abort_flag, 0);
@@ -639,22 +713,41 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   }
 
   // ---- teardown: drain in-flight copies if the pipeline stopped early,
-  // make sure every tcgen05 op finished, free TMEM.
-  if (warp == 0 && lane == 0 && *abort_flag) {
+  // make sure every tcgen05 op finished, free TMEM.  (In a pair, every copy of
+  // both CTAs completes on the even CTA's stage barriers, so it drains for
+  // both, and the odd CTA leaves only after the cluster barrier below.)
+  if (warp == 0 && lane == 0 && rank == 0 && *abort_flag) {
     int never = 0;
     const int from = issued > ST ? issued - ST : 0;
     for (int k = from; k < issued; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
+  }
+  if (warp == 0 && lane == 0 && *abort_flag) {
+    int never = 0;
     const int sfrom = sissued > kScaleSlots ? sissued - kScaleSlots : 0;
     for (int k = sfrom; k < sissued; ++k)
       (void)mbar_wait_bounded(&sfull[k % kScaleSlots], (k / kScaleSlots) & 1, &never, kWaitLimitNs / 2);
   }
+  if constexpr (PAIR) {
+    // after an abort the odd CTA cannot see when its last copies (counted on
+    // the even CTA's barriers) land in its shared memory: give them 100 us
+    if (warp == 0 && lane == 0 && *abort_flag) {
+      const uint64_t t0 = global_timer_ns();
+      while (global_timer_ns() - t0 < 100000ull) {
+      }
+    }
+  }
   tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) cluster_sync_all();
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    tmem_dealloc(tmem, CF::kTmemCols);
+    if constexpr (PAIR)
+      tmem_dealloc2(tmem, CF::kTmemCols);
+    else
+      tmem_dealloc(tmem, CF::kTmemCols);
   }
+  if constexpr (PAIR) cluster_sync_all();
 }
 
 // ------------------------------------------------------------ host side
@@ -672,26 +765,27 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D tensor map over a rows x cols (cols contiguous) buffer of BF16 or
-// 8-bit elements, box of box_rows x 128 bytes with 128-byte swizzle.
-gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows,
-                       bool bytes) {
+// 3-D tensor map over `planes` planes of rows x cols (cols contiguous) BF16
+// or 8-bit elements, planes one after another; box of box_rows x 128 bytes x
+// all planes, 128-byte swizzle.
+gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint64_t planes,
+                       uint32_t box_rows, bool bytes) {
   auto fn = encode_fn();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled is not available from the driver");
     return GBBLAS_STATUS_CUDA_ERROR;
   }
   const uint64_t esize = bytes ? 1 : 2;
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols * esize};
-  cuuint32_t box[2] = {(cuuint32_t)(128 / esize), box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+  cuuint64_t dims[3] = {cols, rows, planes};
+  cuuint64_t strides[2] = {cols * esize, rows * cols * esize};
+  cuuint32_t box[3] = {(cuuint32_t)(128 / esize), box_rows, (cuuint32_t)planes};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
                   const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d) for %llu x %llu", (int)r, (unsigned long long)rows,
-              (unsigned long long)cols);
+    set_error("cuTensorMapEncodeTiled failed (%d) for %llu x %llu x %llu", (int)r, (unsigned long long)planes,
+              (unsigned long long)rows, (unsigned long long)cols);
     return GBBLAS_STATUS_CUDA_ERROR;
   }
   return GBBLAS_STATUS_SUCCESS;
@@ -715,6 +809,7 @@ struct TcGroupPlan {
   char* base = nullptr;  // device: zeroed header | problems | jobs | arena | FP8 scales
   bool owned = false;    // base allocated by the plan (graph plans)
   CUtensorMap map_a, map_b;
+  bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool fp8() const { return mode == kModeFp8; }
   int planes() const { return fp8() ? 1 : mode; }
   int slice_k() const { return fp8() ? 128 : kBK; }  // K elements per 128-byte slice
@@ -743,6 +838,21 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     if (g.M > 0 && g.N > 0 && g.K > 0) order.push_back(i);
   }
   std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return d[x].K > d[y].K; });
+  // Single CTAs by default: at 8192^3 CTA pairs measured the same for the
+  // three-product split (458 vs 459 TFLOP/s), +1 % for six products and much
+  // slower for FP8 (551 vs 871), where each 128-K chunk waits on both CTAs'
+  // epilogues.  GBBLAS_TC_PAIR=1 selects pairs where padding every problem
+  // to 256 rows adds at most 10 % of MMA work.
+  if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1') {
+    double w1 = 0, w2 = 0;
+    for (int64_t i : order) {
+      const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, sk);
+      w1 += (double)round_up(d[i].M, kBM) * nk;
+      w2 += (double)round_up(d[i].M, 2 * kBM) * nk;
+    }
+    pl.pair = w2 <= 1.1 * w1;
+  }
+  const int64_t bmt = pl.pair ? 2 * kBM : kBM;  // output tile rows
   pl.nprob = (int)order.size();
   pl.probs.resize(pl.nprob);
   pl.ajobs.resize(pl.nprob);
@@ -750,14 +860,14 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   for (int i = 0; i < pl.nprob; ++i) pl.pitch = std::max<int64_t>(pl.pitch, round_up(d[order[i]].K, sk));
   for (int i = 0; i < pl.nprob; ++i) {
     const gbblas_gemm_desc& g = d[order[i]];
-    const int64_t Mp = round_up(g.M, kBM), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
+    const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
     TcProblem& p = pl.probs[i];
     p.M = (int)g.M;
     p.N = (int)g.N;
     p.num_kt = (int)(Kp / sk);
     p.a_row = (int)pl.a_rows;
     p.b_row = (int)pl.b_rows;
-    p.tiles_m = (int)(Mp / kBM);
+    p.tiles_m = (int)(Mp / bmt);
     p.tiles_n = (int)(Np / kBN);
     p.tile_start = (int)pl.tiles;
     p.C = g.C;
@@ -808,18 +918,94 @@ gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
                               cudaMemcpyHostToDevice, stream));
   GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs + sizeof(SplitJob) * pl.nprob, pl.bjobs.data(),
                               sizeof(SplitJob) * pl.nprob, cudaMemcpyHostToDevice, stream));
-  GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)(pl.planes() * pl.a_rows), (uint64_t)pl.pitch, kBM, pl.fp8()));
-  GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)(pl.planes() * pl.b_rows), (uint64_t)pl.pitch, kBN, pl.fp8()));
+  GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)pl.a_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(), kBM,
+                  pl.fp8()));
+  GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)pl.b_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(),
+                  pl.pair ? kBN / 2 : kBN, pl.fp8()));
   return GBBLAS_STATUS_SUCCESS;
+}
+
+// Kernel attributes (dynamic shared memory) and how many CTAs (single) or
+// CTA pairs (PAIR) are resident at once on this device; set once per device,
+// before any launch or stream capture.
+template <int MODE, bool PAIR>
+int kernel_setup(DeviceCtx* c) {
+  using CF = TcCfg<MODE, PAIR>;
+  static std::mutex mu;
+  static int resident[64] = {0};
+  std::lock_guard<std::mutex> lk(mu);
+  int& n = resident[c->device & 63];
+  if (n == 0) {
+    cudaFuncSetAttribute(gemm_split_kernel<MODE, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::kSmem);
+    n = c->num_sms;
+    if (PAIR) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * c->num_sms);
+      cfg.blockDim = dim3(ModeTraits<MODE>::kThreads);
+      cfg.dynamicSmemBytes = CF::kSmem;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int k = 0;
+      n = (cudaOccupancyMaxActiveClusters(&k, gemm_split_kernel<MODE, PAIR>, &cfg) == cudaSuccess && k > 0)
+              ? k
+              : c->num_sms / 2;
+      cudaGetLastError();  // a refused query leaves no sticky error behind
+    }
+  }
+  return n;
+}
+
+template <int MODE, bool PAIR>
+gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
+  using CF = TcCfg<MODE, PAIR>;
+  int* err = reinterpret_cast<int*>(pl.base + kErrWordOffset);
+  int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
+  const auto* dprobs = reinterpret_cast<const TcProblem*>(pl.base + pl.off_probs);
+  const int resident = kernel_setup<MODE, PAIR>(c);
+  int units = (int)std::min<int64_t>(pl.tiles, resident);  // CTAs, or CTA pairs
+  if (max_ctas > 0) {
+    const int cap = PAIR ? std::max(1, max_ctas / 2) : max_ctas;
+    if (units > cap) units = cap;
+  }
+  if (!PAIR) {
+    gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
+        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, (int)pl.a_rows, (int)pl.b_rows, counter, err,
+        scales_a(pl), scales_b(pl));
+    return check_launch("gemm_split_kernel");
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * units);
+  cfg.blockDim = dim3(ModeTraits<MODE>::kThreads);
+  cfg.dynamicSmemBytes = CF::kSmem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const cudaError_t e =
+      cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
+                         (int)pl.a_rows, (int)pl.b_rows, counter, err, (const float*)scales_a(pl),
+                         (const float*)scales_b(pl));
+  if (e != cudaSuccess) {
+    count_launch();
+    set_error("launch of gemm_split_kernel (CTA pairs) failed: %s", cudaGetErrorString(e));
+    return GBBLAS_STATUS_CUDA_ERROR;
+  }
+  return check_launch("gemm_split_kernel");
 }
 
 template <int MODE>
 gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
-  using CF = TcCfg<MODE>;
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
-  int* err = reinterpret_cast<int*>(pl.base + kErrWordOffset);
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
-  const auto* dprobs = reinterpret_cast<const TcProblem*>(pl.base + pl.off_probs);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
   prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.nprob, arena_a(pl),
@@ -830,18 +1016,8 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
                                                           pl.b_rows);
   GB_TRY(check_launch("prep_group_kernel(B)"));
-  static bool attr_set[64] = {false};
-  if (!attr_set[c->device & 63]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_split_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)CF::kSmem));
-    attr_set[c->device & 63] = true;
-  }
-  int grid = (int)std::min<int64_t>(pl.tiles, c->num_sms);
-  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  gemm_split_kernel<MODE><<<grid, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(pl.map_a, pl.map_b, dprobs, pl.nprob,
-                                                                 (int)pl.tiles, (int)pl.a_rows, (int)pl.b_rows,
-                                                                 counter, err, scales_a(pl), scales_b(pl));
-  return check_launch("gemm_split_kernel");
+  return pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
+                 : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
 }
 
 }  // namespace
@@ -858,16 +1034,17 @@ int tc_mode(gbblas_accuracy acc) {
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
   const bool fp8 = mode == kModeFp8;
   const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? 128 : kBK;
-  const int64_t rows = round_up(M, kBM) + round_up(N, kBN), Kp = round_up(K, sk);
+  const int64_t rows = round_up(M, 2 * kBM) + round_up(N, kBN), Kp = round_up(K, sk);
   return (size_t)(rows * Kp * planes * (fp8 ? 1 : 2) + (fp8 ? rows * (Kp / 128) * 4 : 0));
 }
 
 void tc_prepare(DeviceCtx* c) {
-  (void)c;
-  cudaFuncSetAttribute(gemm_split_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<2>::kSmem);
-  cudaFuncSetAttribute(gemm_split_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<3>::kSmem);
-  cudaFuncSetAttribute(gemm_split_kernel<kModeFp8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)TcCfg<kModeFp8>::kSmem);
+  kernel_setup<2, false>(c);
+  kernel_setup<3, false>(c);
+  kernel_setup<kModeFp8, false>(c);
+  kernel_setup<2, true>(c);
+  kernel_setup<3, true>(c);
+  kernel_setup<kModeFp8, true>(c);
 }
 
 gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas) {
