@@ -11,8 +11,9 @@
 //        p0 = bf16_rn(a), p1 = bf16_rn(a - p0), p2 = bf16_rn(a - p0 - p1),
 //        piece planes one after another.
 //      prep_group_kernel, FP8: every 128-element K-block of a row becomes
-//        128 E4M3 values and one power-of-two FP32 scale (scale planes stored
-//        K-block-major beside the arena).
+//        128 E4M3 values and one power-of-two scale, kept as its UE8M0
+//        exponent byte in 512-byte atoms (128 rows of one K-block) beside
+//        the arena, laid out the way tcgen05.cp moves them into TMEM.
 //   2. gemm_split_kernel (persistent, one CTA per SM): a device-side tile
 //      scheduler hands out 128 x 128 output tiles of all problems (largest K
 //      first) through an atomic counter.  K is walked in chunks: each chunk
@@ -31,22 +32,24 @@
 //      Three pieces hold all 24 significand bits of an FP32 value and the
 //      dropped products are below 2^-23 of |a||b|: bf16x6 is at least as
 //      accurate as FP32 FMA arithmetic.  bf16x3 keeps about 16 bits.
-//      FP8 (tcgen05.mma kind::f8f6f4, E4M3 in, FP32 accumulate): one chunk
-//      per 128-K scale block; the epilogue adds partial * sa(row) * sb(col).
+//      FP8 (tcgen05.mma kind::mxf8f6f4 block_scale, E4M3 in, FP32
+//      accumulate): the tensor core applies the row and column block scales
+//      itself (UE8M0 scales copied from the stage into TMEM by tcgen05.cp
+//      ahead of each slice's MMAs); chunks of 512 K as for the split.
 //
-// Warp roles (192 threads; FP8: 320):
+// Warp roles (192 threads):
 //   warp 0      tile scheduler + TMA producer: takes the next tile from the
 //               global counter, publishes it in a shared-memory tile ring,
 //               then streams its K slices (128 bytes of K of all P pieces of
 //               A and of B: one 3-D tiled bulk copy per operand, 128-byte
-//               swizzle) into a stage ring;
+//               swizzle; FP8 adds the two 512-byte scale atoms) into a
+//               stage ring;
 //   warp 1      allocates TMEM and issues the MMAs (one elected lane);
 //               tcgen05.commit frees a stage once its MMAs have read it and
 //               signals a TMEM chunk buffer as full;
 //   warps 2-5   epilogue: tcgen05.ld each finished chunk (warp w reads TMEM
-//   (FP8: 2-9)  lanes 32*(w%4)..+31 = tile rows; with 8 warps, warps 6-9 take
-//               the upper 64 columns) into FP32 registers, release the
-//               buffer, add the registers into C.
+//               lanes 32*(w%4)..+31 = tile rows) into FP32 registers,
+//               release the buffer, add the registers into C.
 // Every mbarrier wait is bounded (2 s by %globaltimer); a wait that gives up
 // records GBBLAS_STATUS_TIMEOUT in the stream's error word, the CTA drains
 // its in-flight copies (bounded again), lets its MMAs finish, frees TMEM and
@@ -82,15 +85,12 @@ constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
 // 512 of K, six-product split every 128 (the tensor core's accumulation over
 // a 512-K chunk made the six-product result's max relative error worse than
 // plain FP32 on operands spanning 2^+-10; at 128 it is 5x better, within 1 %
-// of the speed), FP8 every 128 (one scale block).
+// of the speed), FP8 every 512 (four scale blocks).
 constexpr int kChunkTiles3 = 8;
 constexpr int kChunkTiles6 = 2;
+constexpr int kChunkTilesFp8 = 4;
 constexpr int kTileRing = 4;     // tiles in flight between scheduler and consumers
 constexpr int kMaxStages = 8;    // operand stages in flight (as many as shared memory holds, up to this)
-// FP8: chunks of scales in flight between producer and epilogue.  The ring
-// couples the producer to the epilogue, so it is deep enough (16 x 1 KB) that
-// the operand stages, not the scales, bound how far the copies run ahead.
-constexpr int kScaleSlots = 16;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
 
@@ -103,16 +103,18 @@ struct ModeTraits {
   static constexpr bool fp8 = MODE == kModeFp8;
   static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
   static constexpr int kBKe = fp8 ? 128 : kBK;  // K elements per slice (128 bytes either way)
-  static constexpr int kChunk = fp8 ? 1 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
-  // Epilogue warps: 4 (each 32 tile rows x 128 columns) or, for FP8, whose
-  // chunks are four times shorter, 8 (32 rows x 64 columns each).
-  static constexpr int kEpiWarps = fp8 ? 8 : 4;
-  static constexpr int kCols = kBN * 4 / kEpiWarps;  // tile columns per epilogue thread
+  static constexpr int kChunk = fp8 ? kChunkTilesFp8 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
+  // Epilogue warps: 4, each 32 tile rows x 128 columns.
+  static constexpr int kEpiWarps = 4;
+  static constexpr int kCols = kBN;  // tile columns per epilogue thread
   static constexpr int kThreads = 64 + 32 * kEpiWarps;
-  // TMEM chunk buffers (512 columns in all): 2 x (main + correction) for the
-  // split, 4 x main for FP8 (the MMAs may run three chunks ahead).
-  static constexpr int kBufs = fp8 ? 4 : 2;
-  static constexpr uint32_t kBufCols = 512 / kBufs;
+  // TMEM: two chunk buffers (the MMAs may run one chunk ahead of the
+  // epilogue), main + correction accumulators for the split (2 x 256
+  // columns), one accumulator for FP8 (2 x 128 columns, then one 8-column
+  // scale slot per stage from column 256).
+  static constexpr int kBufs = 2;
+  static constexpr uint32_t kBufCols = fp8 ? kBN : 2 * kBN;
+  static constexpr uint32_t kSfCol0 = 2 * kBN;
 };
 
 template <int MODE, bool PAIR>
@@ -120,15 +122,19 @@ struct TcCfg {
   static constexpr int P = ModeTraits<MODE>::P;
   static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A (this CTA's rows)
   static constexpr uint32_t kBBytes = (PAIR ? kBN / 2 : kBN) * 128;  // B^T rows this CTA stages
-  static constexpr uint32_t kStageBytes = P * (kABytes + kBBytes);
-  static constexpr uint32_t kTmemCols = 512;  // the chunk buffers (ModeTraits::kBufs x kBufCols)
-  // FP8: ring of per-chunk scales (128 row scales of A, 128 column scales of B)
-  static constexpr uint32_t kScaleBytes = ModeTraits<MODE>::fp8 ? kScaleSlots * 2 * 128 * 4 : 0;
+  // FP8: the slice's scale atoms of A and of B (512 bytes each) follow the tiles
+  static constexpr uint32_t kSfBytes = ModeTraits<MODE>::fp8 ? 2 * 512 : 0;
+  static constexpr uint32_t kStageBytes = P * (kABytes + kBBytes) + kSfBytes;
+  static constexpr uint32_t kTmemCols = 512;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
-  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kScaleBytes) / kStageBytes);
+  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
   static constexpr int kStages = kStagesFit > kMaxStages ? kMaxStages : kStagesFit;
-  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kScaleBytes + kBarBytes;
-  static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 2 * kScaleSlots + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
+  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kBarBytes;
+  static_assert(!(PAIR && ModeTraits<MODE>::fp8), "FP8 runs on single CTAs");
+  static_assert(ModeTraits<MODE>::kBufs * ModeTraits<MODE>::kBufCols <= kTmemCols, "chunk buffers exceed TMEM");
+  static_assert(!ModeTraits<MODE>::fp8 || ModeTraits<MODE>::kSfCol0 + 8 * kStages <= kTmemCols,
+                "scale slots exceed TMEM");
+  static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
                 "barrier area too small");
   static_assert(kStages >= 2, "need at least a double-buffered stage ring");
   static_assert(kSmem <= kSmemLimit, "exceeds the 227 KB per-CTA shared memory limit");
@@ -171,18 +177,22 @@ struct PrepTile {
 // `pitch` elements), zero outside rows x K:
 //  * split-BF16 (MODE 2, 3): MODE pieces p0 = bf16_rn(a), p1 = bf16_rn(a - p0),
 //    ... (piece p at out + p * piece_stride);
-//  * FP8: E4M3 bytes and one power-of-two scale per (row, 128-K block) at
-//    scales[kb * scale_stride + arena row].  Block scale s = 2^e with e the
-//    smallest integer such that amax * 2^-e <= 448 (the largest finite E4M3),
-//    so v * 2^-e is exact and only the E4M3 rounding (nearest-even,
-//    saturating) loses bits.  All-zero (and padding) blocks get s = 1.
+//  * FP8: E4M3 bytes and one power-of-two scale per (row, 128-K block).
+//    Block scale s = 2^e with e the smallest integer such that
+//    amax * 2^-e <= 448 (the largest finite E4M3), so v * 2^-e is exact and
+//    only the E4M3 rounding (nearest-even, saturating) loses bits.  All-zero
+//    (and padding) blocks get s = 1.  The scale is stored as its UE8M0 byte
+//    e + 127, repeated in the four bytes of a 32-bit word (one per 32-K
+//    sub-block of the MMA), words in 512-byte atoms of 128 arena rows:
+//    row R = 128 a + 32 j + i of K-block kb at word
+//    kb * scale_stride + 128 a + 4 i + j  (the layout tmem_cp_scales expects).
 // One CTA per tile.  Interior tiles of 16-byte-aligned sources are read with
 // 128-bit loads along whichever dimension is contiguous; edge tiles and other
 // strides element by element (still coalesced along the contiguous side).
 template <int MODE>
 __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                          void* __restrict__ out, int64_t piece_stride, int64_t pitch,
-                                                         float* __restrict__ scales, int64_t scale_stride) {
+                                                         uint32_t* __restrict__ scales, int64_t scale_stride) {
   using PT = PrepTile<MODE>;
   constexpr int TK = PT::TK, TR = PT::TR, LD = PT::LD;
   __shared__ __align__(16) float tile[TR * LD];
@@ -263,7 +273,9 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
           __nv_cvt_float2_to_fp8x2(make_float2(v.z * inv, v.w * inv), __NV_SATFINITE, __NV_E4M3);
       const int64_t row = j.dst_row + r0 + r;
       *reinterpret_cast<uint32_t*>(q8 + row * pitch + k0 + lane * 4) = (uint32_t)lo | ((uint32_t)hi << 16);
-      if (lane == 0) scales[(k0 >> 7) * scale_stride + row] = __int_as_float((127 + e) << 23);
+      if (lane == 0)
+        scales[(k0 >> 7) * scale_stride + (row & ~int64_t(127)) + 4 * (row & 31) + ((row >> 5) & 3)] =
+            (uint32_t)(127 + e) * 0x01010101u;
     }
   } else {
     // half-warp per row: rows 8w + 2i + (lane / 16), lane % 16: 4 consecutive K of 64
@@ -334,7 +346,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                       const TcProblem* __restrict__ probs, int nprob, int total_tiles, int a_piece_rows,
                       int b_piece_rows, int* __restrict__ tile_counter, int* __restrict__ err,
-                      const float* __restrict__ sa, const float* __restrict__ sb) {
+                      const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb) {
   using MT = ModeTraits<MODE>;
   using CF = TcCfg<MODE, PAIR>;
   constexpr int P = MT::P;
@@ -348,18 +360,18 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   auto b_tile = [&](int s, int p) {
     return smem + (size_t)s * CF::kStageBytes + (size_t)P * CF::kABytes + (size_t)p * CF::kBBytes;
   };
-  float* scale_ring = reinterpret_cast<float*>(smem + (size_t)ST * CF::kStageBytes);  // [kScaleSlots][256] (FP8)
-  auto scale_slot = [&](int i) { return scale_ring + i * 256; };  // sa[0..127] then sb[0..127]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes + CF::kScaleBytes);
+  // FP8: the slice's scale atom of A (op 0) / of B^T (op 1), after the tiles
+  auto sf_atom = [&](int s, int op) {
+    return smem + (size_t)s * CF::kStageBytes + (size_t)P * (CF::kABytes + CF::kBBytes) + (size_t)op * 512;
+  };
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
   uint64_t* full = bars;                   // [ST]  TMA -> MMA
   uint64_t* empty = full + ST;             // [ST]  MMA -> TMA
   uint64_t* tfull = empty + ST;            // [kBufs] MMA -> epilogue: chunk in TMEM buffer b
   uint64_t* tempty = tfull + 4;            // [kBufs] epilogue -> MMA: TMEM buffer b drained
   uint64_t* ring_full = tempty + 4;        // [kTileRing] scheduler -> consumers
   uint64_t* ring_empty = ring_full + kTileRing;  // [kTileRing] consumers -> scheduler
-  uint64_t* sfull = ring_empty + kTileRing;     // [kScaleSlots] producer -> epilogue (FP8 scales landed)
-  uint64_t* sempty = sfull + kScaleSlots;       // [kScaleSlots] epilogue -> producer (scales read)
-  uint64_t* accf = sempty + kScaleSlots;        // [1] every MMA of this CTA finished
+  uint64_t* accf = ring_empty + kTileRing;       // [1] every MMA of this CTA finished
   int* ring = reinterpret_cast<int*>(accf + 1);  // [kTileRing] tile ids, -1 = no more work
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kTileRing);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -379,10 +391,6 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     for (int r = 0; r < kTileRing; ++r) {
       mbar_init(&ring_full[r], 1);
       mbar_init(&ring_empty[r], 1 + MT::kEpiWarps);  // MMA lane + the epilogue warps
-    }
-    for (int i = 0; i < kScaleSlots; ++i) {
-      mbar_init(&sfull[i], 1);
-      mbar_init(&sempty[i], MT::kEpiWarps);  // one arrival per epilogue warp
     }
     mbar_init(accf, 1);
     *abort_flag = 0;
@@ -410,8 +418,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
   };
 
-  int issued = 0;   // producer: K slices whose copies were issued (all tiles)
-  int sissued = 0;  // producer (FP8): chunks whose scale copies were issued
+  int issued = 0;  // producer: K slices whose copies were issued (all tiles)
   if (warp == 0) {
     if (lane == 0) {
       bool stop = false;
@@ -457,22 +464,14 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
             tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
             tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
+            if constexpr (MT::fp8) {
+              // K-block kt's scale atoms of these 128 rows of A and of B^T
+              // (arena rows are 128-aligned: one contiguous 512-byte run each)
+              bulk_load(sf_atom(s, 0), sa + (int64_t)kt * a_piece_rows + pr.a_row + own_m0, 512, &full[s]);
+              bulk_load(sf_atom(s, 1), sb + (int64_t)kt * b_piece_rows + pr.b_row + n0, 512, &full[s]);
+            }
           }
           ++issued;
-          if constexpr (MT::fp8) {
-            // this chunk's 128 row scales of A (this CTA's rows) and 128 column
-            // scales of B (scale planes are K-block-major: both runs contiguous)
-            const int ss = sissued % kScaleSlots, sr = sissued / kScaleSlots;
-            if (sr > 0 && !mbar_wait_bounded(&sempty[ss], (sr - 1) & 1, abort_flag, kWaitLimitNs)) {
-              fail();
-              stop = true;
-              break;
-            }
-            mbar_arrive_expect_tx(&sfull[ss], 2 * 128 * 4);
-            bulk_load(scale_slot(ss), sa + (int64_t)kt * a_piece_rows + pr.a_row + own_m0, 128 * 4, &sfull[ss]);
-            bulk_load(scale_slot(ss) + 128, sb + (int64_t)kt * b_piece_rows + pr.b_row + n0, 128 * 4, &sfull[ss]);
-            ++sissued;
-          }
         }
       }
     }
@@ -490,8 +489,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         if (t < 0) break;
       }
     } else if (lane == 0) {
-      constexpr uint32_t idesc =
-          MT::fp8 ? idesc_e4m3_f32(BMT, kBN) : idesc_bf16_f32(BMT, kBN);  // M = 256 for a pair
+      constexpr uint32_t idesc = idesc_bf16_f32(BMT, kBN);  // split-BF16; M = 256 for a pair
       int consumed = 0;  // K slices consumed (all tiles)
       int chunk_g = 0;   // chunks started (all tiles)
       bool stop = false;
@@ -532,27 +530,33 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             a[p] = smem_u32(a_tile(s, p));
             bb[p] = smem_u32(b_tile(s, p));
           }
+          uint32_t sfa_t = 0, sfb_t = 0;
+          if constexpr (MT::fp8) {
+            // stage s's TMEM scale slot: its previous user, the slice ST
+            // earlier, has finished (the stage came back), so it is free
+            sfa_t = tmem + MT::kSfCol0 + 8u * (uint32_t)s;
+            sfb_t = sfa_t + 4u;
+            tmem_cp_scales(sfa_t, smem_u32(sf_atom(s, 0)));
+            tmem_cp_scales(sfb_t, smem_u32(sf_atom(s, 1)));
+          }
           auto mma = [&](uint32_t d, uint32_t ad, uint32_t bd, uint32_t accumulate) {
-            if constexpr (PAIR) {
-              if constexpr (MT::fp8)
-                mma2_f8f6f4(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
-              else
-                mma2_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
-            } else {
-              if constexpr (MT::fp8)
-                mma_f8f6f4(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
-              else
-                mma_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
-            }
+            if constexpr (PAIR)
+              mma2_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
+            else
+              mma_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
           };
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             // 32 bytes along K per MMA inside the swizzled 128-byte row:
-            // 16 bf16 (kind::f16) or 32 e4m3 (kind::f8f6f4)
+            // 16 bf16 (kind::f16) or 32 e4m3 (kind::mxf8f6f4)
             const uint32_t off = kk * 32;
             const uint32_t acc = (chunk_first && kk == 0) ? 0u : 1u;
-            mma(acc_main, a[0] + off, bb[0] + off, acc);
-            if constexpr (!MT::fp8) {
+            if constexpr (MT::fp8) {
+              // 32-K sub-block kk of the 128-K scale block: byte kk of each scale word
+              mma_mxf8(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off),
+                       idesc_mxe4m3(kBM, kBN, kk, kk), sfa_t, sfb_t, acc);
+            } else {
+              mma(acc_main, a[0] + off, bb[0] + off, acc);
               // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
               mma(acc_corr, a[0] + off, bb[1] + off, acc);
               mma(acc_corr, a[1] + off, bb[0] + off, 1u);
@@ -626,48 +630,16 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         }
         tc_fence_after();
         const uint32_t tb = trow + (uint32_t)b * MT::kBufCols;
-        if constexpr (MT::fp8) {
-          // chunk c is 128-K block c: C += partial * scale_a(row, c) * scale_b(col, c),
-          // the scales staged in shared memory by the producer (slot chunk_g % kScaleSlots).
-          const int ss = chunk_g % kScaleSlots;
-          const bool landed = __all_sync(
-              0xffffffffu, mbar_wait_bounded(&sfull[ss], (chunk_g / kScaleSlots) & 1, abort_flag, kWaitLimitNs));
-          if (!landed) {
-            if (lane == 0) fail();
-            ok = false;
-            break;
-          }
-          const float* sc = scale_slot(ss);
-          const float sr = sc[q * 32 + lane];
-          const float2 sr2 = make_float2(sr, sr);
 #pragma unroll
-          for (int h = 0; h < kCols; h += 64) {
-            float v[64];
-#pragma unroll
-            for (int c0 = 0; c0 < 64; c0 += 16) tmem_ld16p(tb + h + c0, v + c0);
+        for (int c0 = 0; c0 < kCols; c0 += 16) {
+          float v0[16];
+          tmem_ld16(tb + c0, v0);
+          if constexpr (MT::fp8) {
             tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 64; j += 4) {
-              // column scales: the same address across the warp (broadcast)
-              const float4 s4 = *reinterpret_cast<const float4*>(sc + 128 + col0 + h + j);
-              const float2 c01 = __fmul2_rn(make_float2(s4.x, s4.y), sr2);
-              const float2 c23 = __fmul2_rn(make_float2(s4.z, s4.w), sr2);
-              const float2 a01 = __ffma2_rn(make_float2(v[j], v[j + 1]), c01, make_float2(acc[h + j], acc[h + j + 1]));
-              const float2 a23 =
-                  __ffma2_rn(make_float2(v[j + 2], v[j + 3]), c23, make_float2(acc[h + j + 2], acc[h + j + 3]));
-              acc[h + j] = a01.x;
-              acc[h + j + 1] = a01.y;
-              acc[h + j + 2] = a23.x;
-              acc[h + j + 3] = a23.y;
-            }
-          }
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sempty[ss]);
-        } else {
-#pragma unroll
-          for (int c0 = 0; c0 < kCols; c0 += 16) {
-            float v0[16], v1[16];
-            tmem_ld16(tb + c0, v0);
+            for (int j = 0; j < 16; ++j) acc[c0 + j] += v0[j];
+          } else {
+            float v1[16];
             tmem_ld16(tb + kBN + c0, v1);
             tmem_ld_wait();
 #pragma unroll
@@ -720,12 +692,6 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     int never = 0;
     const int from = issued > ST ? issued - ST : 0;
     for (int k = from; k < issued; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
-  }
-  if (warp == 0 && lane == 0 && *abort_flag) {
-    int never = 0;
-    const int sfrom = sissued > kScaleSlots ? sissued - kScaleSlots : 0;
-    for (int k = sfrom; k < sissued; ++k)
-      (void)mbar_wait_bounded(&sfull[k % kScaleSlots], (k / kScaleSlots) & 1, &never, kWaitLimitNs / 2);
   }
   if constexpr (PAIR) {
     // after an abort the odd CTA cannot see when its last copies (counted on
@@ -839,11 +805,11 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   }
   std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return d[x].K > d[y].K; });
   // Single CTAs by default: at 8192^3 CTA pairs measured the same for the
-  // three-product split (458 vs 459 TFLOP/s), +1 % for six products and much
-  // slower for FP8 (551 vs 871), where each 128-K chunk waits on both CTAs'
-  // epilogues.  GBBLAS_TC_PAIR=1 selects pairs where padding every problem
-  // to 256 rows adds at most 10 % of MMA work.
-  if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1') {
+  // three-product split (458 vs 459 TFLOP/s) and +1 % for six products.
+  // GBBLAS_TC_PAIR=1 selects pairs for the split where padding every
+  // problem to 256 rows adds at most 10 % of MMA work (FP8 always runs on
+  // single CTAs).
+  if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1' && mode != kModeFp8) {
     double w1 = 0, w2 = 0;
     for (int64_t i : order) {
       const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, sk);
@@ -893,9 +859,9 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   pl.off_arena = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.nprob);
   const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
   pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
-  const size_t kb = pl.fp8() ? (size_t)(pl.pitch / 128) : 0;
-  pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(float));
-  pl.bytes = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(float));
+  const size_t kb = pl.fp8() ? (size_t)(pl.pitch / 128) : 0;  // one 4-byte scale word per row and K-block
+  pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
+  pl.bytes = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -904,8 +870,8 @@ char* arena_b(const TcGroupPlan& pl) {
   const size_t esize = pl.fp8() ? 1 : sizeof(__nv_bfloat16);
   return arena_a(pl) + (size_t)pl.planes() * (size_t)(pl.a_rows * pl.pitch) * esize;
 }
-float* scales_a(const TcGroupPlan& pl) { return reinterpret_cast<float*>(pl.base + pl.off_sa); }
-float* scales_b(const TcGroupPlan& pl) { return reinterpret_cast<float*>(pl.base + pl.off_sb); }
+uint32_t* scales_a(const TcGroupPlan& pl) { return reinterpret_cast<uint32_t*>(pl.base + pl.off_sa); }
+uint32_t* scales_b(const TcGroupPlan& pl) { return reinterpret_cast<uint32_t*>(pl.base + pl.off_sb); }
 
 // Point the plan at device memory `base` (>= pl.bytes, header zeroed), copy
 // the tables there on `stream`, and encode the arena tensor maps.
@@ -972,12 +938,12 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
     const int cap = PAIR ? std::max(1, max_ctas / 2) : max_ctas;
     if (units > cap) units = cap;
   }
-  if (!PAIR) {
+  if constexpr (!PAIR) {
     gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
         pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, (int)pl.a_rows, (int)pl.b_rows, counter, err,
         scales_a(pl), scales_b(pl));
     return check_launch("gemm_split_kernel");
-  }
+  } else {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * units);
   cfg.blockDim = dim3(ModeTraits<MODE>::kThreads);
@@ -992,14 +958,15 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   cfg.numAttrs = 1;
   const cudaError_t e =
       cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                         (int)pl.a_rows, (int)pl.b_rows, counter, err, (const float*)scales_a(pl),
-                         (const float*)scales_b(pl));
+                         (int)pl.a_rows, (int)pl.b_rows, counter, err, (const uint32_t*)scales_a(pl),
+                         (const uint32_t*)scales_b(pl));
   if (e != cudaSuccess) {
     count_launch();
     set_error("launch of gemm_split_kernel (CTA pairs) failed: %s", cudaGetErrorString(e));
     return GBBLAS_STATUS_CUDA_ERROR;
   }
   return check_launch("gemm_split_kernel");
+  }
 }
 
 template <int MODE>
@@ -1016,8 +983,10 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
                                                           pl.b_rows);
   GB_TRY(check_launch("prep_group_kernel(B)"));
-  return pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
-                 : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
+  if constexpr (MODE != kModeFp8) {
+    if (pl.pair) return launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas);
+  }
+  return launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
 }
 
 }  // namespace
@@ -1044,7 +1013,6 @@ void tc_prepare(DeviceCtx* c) {
   kernel_setup<kModeFp8, false>(c);
   kernel_setup<2, true>(c);
   kernel_setup<3, true>(c);
-  kernel_setup<kModeFp8, true>(c);
 }
 
 gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas) {

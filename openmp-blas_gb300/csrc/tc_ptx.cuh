@@ -127,16 +127,45 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64
       : "memory");
 }
 
-// D[tmem] (+)= A * B^T, kind::f8f6f4 (8/6/4-bit float in, F32 acc; K = 32
-// for 8-bit operands, i.e. 32 bytes of each 128-byte swizzled row).
-__device__ __forceinline__ void mma_f8f6f4(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
-                                           uint32_t accumulate) {
+// D[tmem] (+)= (A * 2^(sa - 127)) * (B * 2^(sb - 127))^T, kind::mxf8f6f4 with
+// one UE8M0 scale per 32 elements of K (scale_vec::1X; K = 32 per MMA for
+// 8-bit operands, i.e. 32 bytes of each 128-byte swizzled row).  The scales
+// live in TMEM at sfa_tmem / sfb_tmem: for M = N = 128 the scale of A row m
+// is byte (instruction descriptor's A scale id) of column m / 32 in lane m,
+// the scale of B column n is the same byte of column n / 32 in lane
+// n % 32 of each lane quarter (the layout tcgen05.cp 32x128b.warpx4 makes,
+// see tmem_cp_scales).
+__device__ __forceinline__ void mma_mxf8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t sfa_tmem, uint32_t sfb_tmem, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      "setp.ne.b32 p, %6, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::mxf8f6f4.block_scale.scale_vec::1X [%0], %1, %2, %3, [%4], [%5], p;\n\t}\n" ::"r"(
+          d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(sfa_tmem), "r"(sfb_tmem), "r"(accumulate)
       : "memory");
+}
+
+// Shared-memory descriptor of a plain (unswizzled) block of 16-byte rows,
+// 8-row core matrices 128 bytes apart: the source of tmem_cp_scales.
+__device__ __forceinline__ uint64_t plain_rows16_desc(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((smem_addr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>(128u >> 4) << 16;
+  d |= static_cast<uint64_t>(128u >> 4) << 32;
+  d |= static_cast<uint64_t>(1u) << 46;
+  return d;
+}
+
+// Copy one 512-byte scale atom from shared memory into 4 TMEM columns at
+// `taddr` (tcgen05.cp 32x128b.warpx4): atom row i (16 bytes, i < 32) lands in
+// lane i of every lane quarter, its 4-byte word j in column j.  With the
+// scale of operand row r = i + 32 j in word j of atom row i (every byte of the
+// word, one per 32-K sub-block), mma_mxf8 finds each row's scale.  Ordered
+// before later tcgen05.mma of the issuing thread; tcgen05.commit tracks it.
+__device__ __forceinline__ void tmem_cp_scales(uint32_t taddr, uint32_t atom_smem) {
+  asm volatile("tcgen05.cp.cta_group::1.32x128b.warpx4 [%0], %1;" ::"r"(taddr), "l"(plain_rows16_desc(atom_smem))
+               : "memory");
 }
 
 // Arrive on `bar` once every MMA previously issued by this thread completes.
@@ -156,9 +185,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
       : "memory");
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_ld16p(uint32_t taddr, float* v) {
-  tmem_ld16(taddr, *reinterpret_cast<float(*)[16]>(v));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -185,10 +211,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
-// Instruction descriptor for kind::f8f6f4 with E4M3 A/B (format 0 in bits
-// 7-9 and 10-12), F32 D, both K-major; same N / M fields.
-__host__ __device__ constexpr uint32_t idesc_e4m3_f32(uint32_t M, uint32_t N) {
-  return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
+// Instruction descriptor for kind::mxf8f6f4 with E4M3 A/B (format 0 in bits
+// 7-9 and 10-12), F32 D, both K-major, UE8M0 scales (bit 23): bits 4-5 pick
+// the byte of B's scale word, 29-30 that of A's; same N / M fields.
+__host__ __device__ constexpr uint32_t idesc_mxe4m3(uint32_t M, uint32_t N, uint32_t sfa_id, uint32_t sfb_id) {
+  return (sfb_id << 4) | ((N >> 3) << 17) | (1u << 23) | ((M >> 4) << 24) | (sfa_id << 29);
 }
 
 }  // namespace gbblas::tc
@@ -255,15 +282,6 @@ __device__ __forceinline__ void mma2_f16(uint32_t d_tmem, uint64_t a_desc, uint6
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void mma2_f8f6f4(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
-                                            uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
