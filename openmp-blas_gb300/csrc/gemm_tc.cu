@@ -88,7 +88,7 @@ constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
 // of the speed), FP8 every 512 (four scale blocks).
 constexpr int kChunkTiles3 = 8;
 constexpr int kChunkTiles6 = 2;
-constexpr int kChunkTilesFp8 = 4;
+constexpr int kChunkTilesFp8 = 2;  // FP8 stages are 256 K deep
 constexpr int kTileRing = 4;     // tiles in flight between scheduler and consumers
 constexpr int kMaxStages = 8;    // operand stages in flight (as many as shared memory holds, up to this)
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
@@ -102,7 +102,11 @@ template <int MODE>
 struct ModeTraits {
   static constexpr bool fp8 = MODE == kModeFp8;
   static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
-  static constexpr int kBKe = fp8 ? 128 : kBK;  // K elements per slice (128 bytes either way)
+  // 128-byte K sub-tiles per stage: one for the split (64 BF16 of every
+  // piece), two for FP8 (256 E4M3: twice the MMAs per barrier round trip,
+  // the per-stage hand-offs being what bounds the four-MMA FP8 stage).
+  static constexpr int kSub = fp8 ? 2 : 1;
+  static constexpr int kBKe = fp8 ? 128 * kSub : kBK;  // K elements per stage
   static constexpr int kChunk = fp8 ? kChunkTilesFp8 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
   // Epilogue warps: 4, each 32 tile rows x 128 columns.
   static constexpr int kEpiWarps = 4;
@@ -122,9 +126,10 @@ struct TcCfg {
   static constexpr int P = ModeTraits<MODE>::P;
   static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A (this CTA's rows)
   static constexpr uint32_t kBBytes = (PAIR ? kBN / 2 : kBN) * 128;  // B^T rows this CTA stages
-  // FP8: the slice's scale atoms of A and of B (512 bytes each) follow the tiles
-  static constexpr uint32_t kSfBytes = ModeTraits<MODE>::fp8 ? 2 * 512 : 0;
-  static constexpr uint32_t kStageBytes = P * (kABytes + kBBytes) + kSfBytes;
+  static constexpr int kSub = ModeTraits<MODE>::kSub;
+  // FP8: the stage's scale atoms (512 bytes per 128-K block) of A, then of B
+  static constexpr uint32_t kSfBytes = ModeTraits<MODE>::fp8 ? 2 * 512 * kSub : 0;
+  static constexpr uint32_t kStageBytes = P * kSub * (kABytes + kBBytes) + kSfBytes;
   static constexpr uint32_t kTmemCols = 512;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
   static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
@@ -132,7 +137,7 @@ struct TcCfg {
   static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kBarBytes;
   static_assert(!(PAIR && ModeTraits<MODE>::fp8), "FP8 runs on single CTAs");
   static_assert(ModeTraits<MODE>::kBufs * ModeTraits<MODE>::kBufCols <= kTmemCols, "chunk buffers exceed TMEM");
-  static_assert(!ModeTraits<MODE>::fp8 || ModeTraits<MODE>::kSfCol0 + 8 * kStages <= kTmemCols,
+  static_assert(!ModeTraits<MODE>::fp8 || ModeTraits<MODE>::kSfCol0 + 8 * kSub * kStages <= kTmemCols,
                 "scale slots exceed TMEM");
   static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
                 "barrier area too small");
@@ -146,7 +151,7 @@ struct TcCfg {
 // One GEMM of a group, as the kernel sees it (device memory).
 struct TcProblem {
   int M, N;
-  int num_kt;      // K slices of 128 bytes: padded K / 64 (BF16) or / 128 (FP8)
+  int num_kt;      // K stages: padded K / 64 (BF16) or / 256 (FP8)
   int a_row;       // first row of this problem in the A arena (piece 0)
   int b_row;       // first row in the B^T arena (piece 0)
   int tiles_m, tiles_n;
@@ -183,9 +188,11 @@ struct PrepTile {
 //    only the E4M3 rounding (nearest-even, saturating) loses bits.  All-zero
 //    (and padding) blocks get s = 1.  The scale is stored as its UE8M0 byte
 //    e + 127, repeated in the four bytes of a 32-bit word (one per 32-K
-//    sub-block of the MMA), words in 512-byte atoms of 128 arena rows:
+//    sub-block of the MMA), words in 512-byte atoms of 128 arena rows and
+//    one K-block, the atoms of a row block consecutive along K:
 //    row R = 128 a + 32 j + i of K-block kb at word
-//    kb * scale_stride + 128 a + 4 i + j  (the layout tmem_cp_scales expects).
+//    a * scale_stride + 128 kb + 4 i + j  (scale_stride = 128 x the K-blocks;
+//    each atom in the layout tmem_cp_scales expects).
 // One CTA per tile.  Interior tiles of 16-byte-aligned sources are read with
 // 128-bit loads along whichever dimension is contiguous; edge tiles and other
 // strides element by element (still coalesced along the contiguous side).
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
       const int64_t row = j.dst_row + r0 + r;
       *reinterpret_cast<uint32_t*>(q8 + row * pitch + k0 + lane * 4) = (uint32_t)lo | ((uint32_t)hi << 16);
       if (lane == 0)
-        scales[(k0 >> 7) * scale_stride + (row & ~int64_t(127)) + 4 * (row & 31) + ((row >> 5) & 3)] =
+        scales[(row >> 7) * scale_stride + k0 + 4 * (row & 31) + ((row >> 5) & 3)] =
             (uint32_t)(127 + e) * 0x01010101u;
     }
   } else {
@@ -344,8 +351,8 @@ __device__ __forceinline__ void tile_coords(const TcProblem& p, int t, int& m0, 
 template <int MODE, bool PAIR>
 __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
-                      const TcProblem* __restrict__ probs, int nprob, int total_tiles, int a_piece_rows,
-                      int b_piece_rows, int* __restrict__ tile_counter, int* __restrict__ err,
+                      const TcProblem* __restrict__ probs, int nprob, int total_tiles, int64_t sf_stride,
+                      int* __restrict__ tile_counter, int* __restrict__ err,
                       const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb) {
   using MT = ModeTraits<MODE>;
   using CF = TcCfg<MODE, PAIR>;
@@ -355,14 +362,17 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // stage s: A pieces 0..P-1, then B pieces 0..P-1
+  // stage s: A pieces 0..P-1 (split) or K sub-tiles 0..kSub-1 (FP8), then
+  // the same of B, then (FP8) the scale atoms
+  constexpr int NT = P * MT::kSub;  // 128-byte-wide tiles per operand and stage
   auto a_tile = [&](int s, int p) { return smem + (size_t)s * CF::kStageBytes + (size_t)p * CF::kABytes; };
   auto b_tile = [&](int s, int p) {
-    return smem + (size_t)s * CF::kStageBytes + (size_t)P * CF::kABytes + (size_t)p * CF::kBBytes;
+    return smem + (size_t)s * CF::kStageBytes + (size_t)NT * CF::kABytes + (size_t)p * CF::kBBytes;
   };
-  // FP8: the slice's scale atom of A (op 0) / of B^T (op 1), after the tiles
+  // FP8: the stage's scale atoms of A (op 0) / of B^T (op 1), kSub x 512 bytes each
   auto sf_atom = [&](int s, int op) {
-    return smem + (size_t)s * CF::kStageBytes + (size_t)P * (CF::kABytes + CF::kBBytes) + (size_t)op * 512;
+    return smem + (size_t)s * CF::kStageBytes + (size_t)NT * (CF::kABytes + CF::kBBytes) +
+           (size_t)op * 512 * MT::kSub;
   };
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
   uint64_t* full = bars;                   // [ST]  TMA -> MMA
@@ -449,7 +459,6 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             break;
           }
           // one 3-D copy per operand brings all P piece planes of the tile
-          // (planes a_piece_rows / b_piece_rows rows apart in the arena)
           if constexpr (PAIR) {
             if (rank == 0) {
               mbar_arrive_expect_tx(&full[s], 2 * CF::kStageBytes);  // both CTAs' copies
@@ -462,13 +471,22 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             }
           } else {
             mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
-            tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
-            tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
             if constexpr (MT::fp8) {
-              // K-block kt's scale atoms of these 128 rows of A and of B^T
-              // (arena rows are 128-aligned: one contiguous 512-byte run each)
-              bulk_load(sf_atom(s, 0), sa + (int64_t)kt * a_piece_rows + pr.a_row + own_m0, 512, &full[s]);
-              bulk_load(sf_atom(s, 1), sb + (int64_t)kt * b_piece_rows + pr.b_row + n0, 512, &full[s]);
+#pragma unroll
+              for (int u = 0; u < MT::kSub; ++u) {
+                tma_load_3d(a_tile(s, u), &tm_a, &full[s], kt * MT::kBKe + u * 128, pr.a_row + own_m0, 0);
+                tma_load_3d(b_tile(s, u), &tm_b, &full[s], kt * MT::kBKe + u * 128, pr.b_row + n0, 0);
+              }
+              // the stage's K-blocks' scale atoms of these 128 rows of A and
+              // of B^T: consecutive in the scale arrays (one run each)
+              const int64_t kb0 = (int64_t)kt * MT::kSub * 128;
+              bulk_load(sf_atom(s, 0), sa + (int64_t)((pr.a_row + own_m0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
+                        &full[s]);
+              bulk_load(sf_atom(s, 1), sb + (int64_t)((pr.b_row + n0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
+                        &full[s]);
+            } else {
+              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
+              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
             }
           }
           ++issued;
@@ -524,20 +542,22 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
           }
           tc_fence_after();
           const uint32_t acc_main = tmem + (uint32_t)b * MT::kBufCols, acc_corr = acc_main + kBN;
-          uint32_t a[P], bb[P];
+          uint32_t a[NT], bb[NT];
 #pragma unroll
-          for (int p = 0; p < P; ++p) {
+          for (int p = 0; p < NT; ++p) {
             a[p] = smem_u32(a_tile(s, p));
             bb[p] = smem_u32(b_tile(s, p));
           }
-          uint32_t sfa_t = 0, sfb_t = 0;
+          // FP8: stage s's TMEM scale slot (8 columns per 128-K block: 4 for
+          // A's scales, 4 for B's).  Its previous user, the stage's previous
+          // round, has finished (the stage came back), so it is free.
+          const uint32_t sf_slot = tmem + MT::kSfCol0 + 8u * MT::kSub * (uint32_t)s;
           if constexpr (MT::fp8) {
-            // stage s's TMEM scale slot: its previous user, the slice ST
-            // earlier, has finished (the stage came back), so it is free
-            sfa_t = tmem + MT::kSfCol0 + 8u * (uint32_t)s;
-            sfb_t = sfa_t + 4u;
-            tmem_cp_scales(sfa_t, smem_u32(sf_atom(s, 0)));
-            tmem_cp_scales(sfb_t, smem_u32(sf_atom(s, 1)));
+#pragma unroll
+            for (int u = 0; u < MT::kSub; ++u) {
+              tmem_cp_scales(sf_slot + 8u * u, smem_u32(sf_atom(s, 0)) + 512u * u);
+              tmem_cp_scales(sf_slot + 8u * u + 4u, smem_u32(sf_atom(s, 1)) + 512u * u);
+            }
           }
           auto mma = [&](uint32_t d, uint32_t ad, uint32_t bd, uint32_t accumulate) {
             if constexpr (PAIR)
@@ -552,9 +572,12 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             const uint32_t off = kk * 32;
             const uint32_t acc = (chunk_first && kk == 0) ? 0u : 1u;
             if constexpr (MT::fp8) {
-              // 32-K sub-block kk of the 128-K scale block: byte kk of each scale word
-              mma_mxf8(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off),
-                       idesc_mxe4m3(kBM, kBN, kk, kk), sfa_t, sfb_t, acc);
+              // 32-K sub-block kk of each 128-K scale block: byte kk of each scale word
+#pragma unroll
+              for (int u = 0; u < MT::kSub; ++u)
+                mma_mxf8(acc_main, sw128_kmajor_desc(a[u] + off), sw128_kmajor_desc(bb[u] + off),
+                         idesc_mxe4m3(kBM, kBN, kk, kk), sf_slot + 8u * u, sf_slot + 8u * u + 4u,
+                         u == 0 ? acc : 1u);
             } else {
               mma(acc_main, a[0] + off, bb[0] + off, acc);
               // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
@@ -778,7 +801,7 @@ struct TcGroupPlan {
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool fp8() const { return mode == kModeFp8; }
   int planes() const { return fp8() ? 1 : mode; }
-  int slice_k() const { return fp8() ? 128 : kBK; }  // K elements per 128-byte slice
+  int slice_k() const { return fp8() ? ModeTraits<kModeFp8>::kBKe : kBK; }  // K elements per stage
   int job_k() const { return fp8() ? 128 : 64; }     // K extent of one preparation tile (PrepTile::TK)
 };
 
@@ -940,8 +963,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   }
   if constexpr (!PAIR) {
     gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
-        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, (int)pl.a_rows, (int)pl.b_rows, counter, err,
-        scales_a(pl), scales_b(pl));
+        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.pitch, counter, err, scales_a(pl), scales_b(pl));
     return check_launch("gemm_split_kernel");
   } else {
   cudaLaunchConfig_t cfg = {};
@@ -958,8 +980,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   cfg.numAttrs = 1;
   const cudaError_t e =
       cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                         (int)pl.a_rows, (int)pl.b_rows, counter, err, (const uint32_t*)scales_a(pl),
-                         (const uint32_t*)scales_b(pl));
+                         pl.pitch, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl));
   if (e != cudaSuccess) {
     count_launch();
     set_error("launch of gemm_split_kernel (CTA pairs) failed: %s", cudaGetErrorString(e));
@@ -975,13 +996,14 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+  // FP8 scale words: 128 per K-block of each 128-row block, i.e. `pitch` per row block
   prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.nprob, arena_a(pl),
                                                           (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
-                                                          pl.a_rows);
+                                                          pl.pitch);
   GB_TRY(check_launch("prep_group_kernel(A)"));
   prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.nprob, pl.nprob, arena_b(pl),
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
-                                                          pl.b_rows);
+                                                          pl.pitch);
   GB_TRY(check_launch("prep_group_kernel(B)"));
   if constexpr (MODE != kModeFp8) {
     if (pl.pair) return launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas);
@@ -1002,7 +1024,7 @@ int tc_mode(gbblas_accuracy acc) {
 
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
   const bool fp8 = mode == kModeFp8;
-  const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? 128 : kBK;
+  const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? ModeTraits<kModeFp8>::kBKe : kBK;
   const int64_t rows = round_up(M, 2 * kBM) + round_up(N, kBN), Kp = round_up(K, sk);
   return (size_t)(rows * Kp * planes * (fp8 ? 1 : 2) + (fp8 ? rows * (Kp / 128) * 4 : 0));
 }
