@@ -781,6 +781,9 @@ gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64
 }
 
 inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Bytes added to every arena row beyond the padded K.
+constexpr int64_t kPitchPadBytes = 0;
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 }  // namespace
@@ -790,7 +793,9 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 struct TcGroupPlan {
   int mode = 2;  // 2 / 3 BF16 pieces, kModeFp8
   int nprob = 0;
-  int64_t a_rows = 0, b_rows = 0, pitch = 0, tiles = 0;  // pitch in elements (FP8: bytes)
+  int64_t a_rows = 0, b_rows = 0, tiles = 0;
+  int64_t kpad = 0;   // longest padded K of the group (elements)
+  int64_t pitch = 0;  // arena row pitch in elements (FP8: bytes): kpad + kPitchPadBytes
   int a_tiles = 0, b_tiles = 0;
   std::vector<TcProblem> probs;
   std::vector<SplitJob> ajobs, bjobs;
@@ -846,7 +851,8 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   pl.probs.resize(pl.nprob);
   pl.ajobs.resize(pl.nprob);
   pl.bjobs.resize(pl.nprob);
-  for (int i = 0; i < pl.nprob; ++i) pl.pitch = std::max<int64_t>(pl.pitch, round_up(d[order[i]].K, sk));
+  for (int i = 0; i < pl.nprob; ++i) pl.kpad = std::max<int64_t>(pl.kpad, round_up(d[order[i]].K, sk));
+  pl.pitch = pl.kpad + kPitchPadBytes / (pl.fp8() ? 1 : (int64_t)sizeof(__nv_bfloat16));
   for (int i = 0; i < pl.nprob; ++i) {
     const gbblas_gemm_desc& g = d[order[i]];
     const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
@@ -882,7 +888,7 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   pl.off_arena = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.nprob);
   const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
   pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
-  const size_t kb = pl.fp8() ? (size_t)(pl.pitch / 128) : 0;  // one 4-byte scale word per row and K-block
+  const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : 0;  // one 4-byte scale word per row and K-block
   pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
   pl.bytes = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
   return GBBLAS_STATUS_SUCCESS;
@@ -963,7 +969,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   }
   if constexpr (!PAIR) {
     gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
-        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.pitch, counter, err, scales_a(pl), scales_b(pl));
+        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.kpad, counter, err, scales_a(pl), scales_b(pl));
     return check_launch("gemm_split_kernel");
   } else {
   cudaLaunchConfig_t cfg = {};
@@ -980,7 +986,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   cfg.numAttrs = 1;
   const cudaError_t e =
       cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                         pl.pitch, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl));
+                         pl.kpad, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl));
   if (e != cudaSuccess) {
     count_launch();
     set_error("launch of gemm_split_kernel (CTA pairs) failed: %s", cudaGetErrorString(e));
@@ -996,14 +1002,14 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
-  // FP8 scale words: 128 per K-block of each 128-row block, i.e. `pitch` per row block
+  // FP8 scale words: 128 per K-block of each 128-row block, i.e. `kpad` per row block
   prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.nprob, arena_a(pl),
                                                           (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
-                                                          pl.pitch);
+                                                          pl.kpad);
   GB_TRY(check_launch("prep_group_kernel(A)"));
   prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.nprob, pl.nprob, arena_b(pl),
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
-                                                          pl.pitch);
+                                                          pl.kpad);
   GB_TRY(check_launch("prep_group_kernel(B)"));
   if constexpr (MODE != kModeFp8) {
     if (pl.pair) return launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas);
@@ -1026,7 +1032,7 @@ size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
   const bool fp8 = mode == kModeFp8;
   const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? ModeTraits<kModeFp8>::kBKe : kBK;
   const int64_t rows = round_up(M, 2 * kBM) + round_up(N, kBN), Kp = round_up(K, sk);
-  return (size_t)(rows * Kp * planes * (fp8 ? 1 : 2) + (fp8 ? rows * (Kp / 128) * 4 : 0));
+  return (size_t)(rows * (Kp * (fp8 ? 1 : 2) + kPitchPadBytes) * planes + (fp8 ? rows * (Kp / 128) * 4 : 0));
 }
 
 void tc_prepare(DeviceCtx* c) {
