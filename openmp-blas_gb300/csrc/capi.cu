@@ -210,6 +210,9 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
     int mode = tc_mode(acc);
     if (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1) mode = tc_mode(GBBLAS_ACCURACY_BF16X6);
     if (mode != 0) return launch_gemm_tc(c, mode, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    // FP32 on the FMA pipe: the tile shape the autotuner measured faster
+    return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s, 0,
+                              tuned_fma_tile(c, M, N, K, s));
   }
   return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
 }

@@ -120,10 +120,12 @@ gbblas_status launch_dot(DeviceCtx* c, int64_t n, const T* a, const T* b, T* res
 
 // max_ctas > 0 caps the grid (the kernel loops over tiles), leaving SMs to
 // other streams.
+// tile (FP32 only): 1 = 128 x 128 CTA tiles, 0 = 64 x 64, -1 = by the tile
+// count (128 x 128 once they fill the GPU twice over).
 template <typename T>
 gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc,
-                              int64_t csc, cudaStream_t stream, int max_ctas = 0);
+                              int64_t csc, cudaStream_t stream, int max_ctas = 0, int tile = -1);
 
 // C += A*B on the tcgen05 tensor cores (gemm_tc.cu).  mode = tc_mode(acc):
 // 2 / 3 = FP32 operands split into that many BF16 pieces, 8 = FP8-E4M3 with
@@ -132,9 +134,25 @@ int tc_mode(gbblas_accuracy acc);
 // Device bytes of the operand arena one problem needs in `mode`.
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K);
 
+// K stage depth of the tensor-core kernel in `mode` (K is padded to it).
+int tc_stage_k(int mode);
+
+// Shape of one tensor-core launch: split = K parts per problem (split-K:
+// each part a tile problem of its own writing a partial, the parts then
+// added into C in order; 1 = none), pair = CTA form for the split-BF16
+// modes (-1 = the GBBLAS_TC_PAIR setting, 0 = single CTAs, 1 = CTA pairs).
+struct TcLaunchOpts {
+  int split = 1;
+  int pair = -1;
+};
+
+// One problem with the autotuner's launch shape for it.
 gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                              int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
                              int64_t csc, cudaStream_t stream);
+// One problem with a given launch shape.
+gbblas_status launch_gemm_tc_opts(DeviceCtx* c, int mode, const gbblas_gemm_desc& d, const TcLaunchOpts& opt,
+                                  cudaStream_t stream);
 
 // The same for a group of independent problems in one persistent launch
 // (tables and operand arena in the stream's scratch).
@@ -159,6 +177,10 @@ gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t
 
 // Autotuner (tune.cu): AUTO accuracy -> 1 = split-BF16 six products, 0 = FMA.
 int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
+// Autotuner: split-K parts and CTA form of one tensor-core GEMM.
+TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, cudaStream_t stream);
+// Autotuner: FP32 FMA tile (launch_gemm_fma's `tile`).
+int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t stream);
 
 // Streaming operations beside the hot path (stream_ops.cu).
 // C[r*ld + l] += u[r] * v[l] (rows of C contiguous).

@@ -326,7 +326,7 @@ gbblas_status launch_cfg(int la, int lb, int64_t M, int64_t N, int64_t K, const 
 template <typename T>
 gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
                               int64_t csa, const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc,
-                              cudaStream_t stream, int max_ctas) {
+                              cudaStream_t stream, int max_ctas, int tile) {
   constexpr int W = Vec16<T>::w;
   // Which loader each operand can use.
   int la = kScalar, lb = kScalar;
@@ -341,7 +341,8 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if constexpr (sizeof(T) == 4) {
     const int64_t big_tiles = ((M + 127) / 128) * ((N + 127) / 128);
-    if (big_tiles >= 2 * (int64_t)c->num_sms)
+    if (tile < 0) tile = big_tiles >= 2 * (int64_t)c->num_sms ? 1 : 0;
+    if (tile == 1)
       return launch_cfg<float, 128, 128, 16, 8, 8>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
                                                    max_ctas);
     return launch_cfg<float, 64, 64, 16, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
@@ -354,9 +355,9 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
 
 template gbblas_status launch_gemm_fma<float>(DeviceCtx*, int64_t, int64_t, int64_t, const float*, int64_t,
                                               int64_t, const float*, int64_t, int64_t, float*, int64_t, int64_t,
-                                              cudaStream_t, int);
+                                              cudaStream_t, int, int);
 template gbblas_status launch_gemm_fma<double>(DeviceCtx*, int64_t, int64_t, int64_t, const double*, int64_t,
                                                int64_t, const double*, int64_t, int64_t, double*, int64_t,
-                                               int64_t, cudaStream_t, int);
+                                               int64_t, cudaStream_t, int, int);
 
 }  // namespace gbblas

@@ -151,13 +151,25 @@ struct TcCfg {
 // One GEMM of a group, as the kernel sees it (device memory).
 struct TcProblem {
   int M, N;
-  int num_kt;      // K stages: padded K / 64 (BF16) or / 256 (FP8)
+  int num_kt;      // K stages of this (sub)problem: 64 of K (BF16) or 256 (FP8) each
+  int kt0;         // its first K stage (a split-K part covers stages kt0 .. kt0 + num_kt - 1)
   int a_row;       // first row of this problem in the A arena (piece 0)
   int b_row;       // first row in the B^T arena (piece 0)
   int tiles_m, tiles_n;
   int tile_start;  // first global tile index of this problem
+  int overwrite;   // 1: the epilogue stores (a split-K partial), 0: C += result
   float* C;
   int64_t rsc, csc;
+};
+
+// One split-K problem's final step: C += sum over s of part[s] (in order of
+// s, so the result does not depend on which part finished first); parts are
+// M x pitch row-major, `parts` x M x pitch floats in all.
+struct SplitReduce {
+  float* C;
+  int64_t rsc, csc;
+  const float* part;
+  int M, N, pitch, parts;
 };
 
 // One operand matrix to split or quantise (device memory).
@@ -458,35 +470,36 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             stop = true;
             break;
           }
+          const int kx = (pr.kt0 + kt) * MT::kBKe;  // first K element of the stage
           // one 3-D copy per operand brings all P piece planes of the tile
           if constexpr (PAIR) {
             if (rank == 0) {
               mbar_arrive_expect_tx(&full[s], 2 * CF::kStageBytes);  // both CTAs' copies
-              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
-              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
+              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kx, pr.a_row + own_m0, 0);
+              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kx, pr.b_row + n0, 0);
             } else {
               const uint32_t fb = mapa_shared(smem_u32(&full[s]), 0);
-              tma_load_3d_pair(a_tile(s, 0), &tm_a, fb, kt * MT::kBKe, pr.a_row + own_m0, 0);
-              tma_load_3d_pair(b_tile(s, 0), &tm_b, fb, kt * MT::kBKe, pr.b_row + n0 + kBN / 2, 0);
+              tma_load_3d_pair(a_tile(s, 0), &tm_a, fb, kx, pr.a_row + own_m0, 0);
+              tma_load_3d_pair(b_tile(s, 0), &tm_b, fb, kx, pr.b_row + n0 + kBN / 2, 0);
             }
           } else {
             mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
             if constexpr (MT::fp8) {
 #pragma unroll
               for (int u = 0; u < MT::kSub; ++u) {
-                tma_load_3d(a_tile(s, u), &tm_a, &full[s], kt * MT::kBKe + u * 128, pr.a_row + own_m0, 0);
-                tma_load_3d(b_tile(s, u), &tm_b, &full[s], kt * MT::kBKe + u * 128, pr.b_row + n0, 0);
+                tma_load_3d(a_tile(s, u), &tm_a, &full[s], kx + u * 128, pr.a_row + own_m0, 0);
+                tma_load_3d(b_tile(s, u), &tm_b, &full[s], kx + u * 128, pr.b_row + n0, 0);
               }
               // the stage's K-blocks' scale atoms of these 128 rows of A and
               // of B^T: consecutive in the scale arrays (one run each)
-              const int64_t kb0 = (int64_t)kt * MT::kSub * 128;
+              const int64_t kb0 = kx;  // 128 words per K-block of 128 = one word per K element
               bulk_load(sf_atom(s, 0), sa + (int64_t)((pr.a_row + own_m0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
                         &full[s]);
               bulk_load(sf_atom(s, 1), sb + (int64_t)((pr.b_row + n0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
                         &full[s]);
             } else {
-              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * MT::kBKe, pr.a_row + own_m0, 0);
-              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kt * MT::kBKe, pr.b_row + n0, 0);
+              tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kx, pr.a_row + own_m0, 0);
+              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kx, pr.b_row + n0, 0);
             }
           }
           ++issued;
@@ -687,7 +700,17 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         const bool vec =
             (pr.csc == 1) && ((pr.rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(pr.C) & 15) == 0);
         const int cn = n0 + col0;
-        if (vec && cn + kCols <= pr.N) {
+        if (pr.overwrite) {  // split-K partial: dense, 16-byte-aligned rows
+          if (cn + kCols <= pr.N) {
+#pragma unroll
+            for (int j = 0; j < kCols; j += 4)
+              *reinterpret_cast<float4*>(crow + cn + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < kCols; ++j)
+              if (cn + j < pr.N) crow[cn + j] = acc[j];
+          }
+        } else if (vec && cn + kCols <= pr.N) {
 #pragma unroll
           for (int j = 0; j < kCols; j += 4) {
             float4* p = reinterpret_cast<float4*>(crow + cn + j);
@@ -737,6 +760,20 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       tmem_dealloc(tmem, CF::kTmemCols);
   }
   if constexpr (PAIR) cluster_sync_all();
+}
+
+// Split-K: C += part[0] + part[1] + ... (in that order) for every element of
+// every split problem; blockIdx.y = problem, grid-stride over its elements.
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(const SplitReduce* __restrict__ jobs) {
+  const SplitReduce j = jobs[blockIdx.y];
+  const int64_t total = (int64_t)j.M * j.N, plane = (int64_t)j.M * j.pitch;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / j.N, c = e % j.N;
+    const float* p = j.part + r * j.pitch + c;
+    float sum = p[0];
+    for (int s = 1; s < j.parts; ++s) sum += p[s * plane];
+    j.C[r * j.rsc + c * j.csc] += sum;
+  }
 }
 
 // ------------------------------------------------------------ host side
@@ -792,15 +829,19 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // the operand arena live on the device, and the two arena tensor maps.
 struct TcGroupPlan {
   int mode = 2;  // 2 / 3 BF16 pieces, kModeFp8
-  int nprob = 0;
+  int nprob = 0;  // tile problems (a split-K problem counts once per part)
+  int njobs = 0;  // operand preparations (one per problem of the group)
   int64_t a_rows = 0, b_rows = 0, tiles = 0;
   int64_t kpad = 0;   // longest padded K of the group (elements)
   int64_t pitch = 0;  // arena row pitch in elements (FP8: bytes): kpad + kPitchPadBytes
   int a_tiles = 0, b_tiles = 0;
   std::vector<TcProblem> probs;
   std::vector<SplitJob> ajobs, bjobs;
-  size_t off_probs = 0, off_jobs = 0, off_arena = 0, off_sa = 0, off_sb = 0, bytes = 0;
-  char* base = nullptr;  // device: zeroed header | problems | jobs | arena | FP8 scales
+  std::vector<SplitReduce> reds;     // split-K problems' final sums
+  std::vector<int64_t> part_off;     // per tile problem: byte offset of its partial in the workspace, or -1
+  std::vector<int64_t> red_off;      // per reduction: byte offset of its first partial
+  size_t off_probs = 0, off_jobs = 0, off_red = 0, off_arena = 0, off_sa = 0, off_sb = 0, off_ws = 0, bytes = 0;
+  char* base = nullptr;  // device: zeroed header | problems | jobs | reductions | arena | FP8 scales | partials
   bool owned = false;    // base allocated by the plan (graph plans)
   CUtensorMap map_a, map_b;
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
@@ -813,8 +854,13 @@ struct TcGroupPlan {
 namespace {
 
 // Host-side planning (no device work): problem order (largest K first),
-// arena rows, tile numbering, split jobs, device layout.
-gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl) {
+// arena rows, tile numbering, split jobs, device layout.  opt.split > 1
+// cuts every problem's K into that many parts (at most one per K stage),
+// each a tile problem of its own that stores a partial; a reduction then adds
+// the parts into C in order.  opt.pair forces the CTA form (-1: the
+// GBBLAS_TC_PAIR setting).
+gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl,
+                         const TcLaunchOpts& opt = TcLaunchOpts()) {
   if (mode != 2 && mode != 3 && mode != kModeFp8) {
     set_error("tensor-core gemm: unknown mode %d", mode);
     return GBBLAS_STATUS_INVALID_VALUE;
@@ -834,10 +880,13 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return d[x].K > d[y].K; });
   // Single CTAs by default: at 8192^3 CTA pairs measured the same for the
   // three-product split (458 vs 459 TFLOP/s) and +1 % for six products.
-  // GBBLAS_TC_PAIR=1 selects pairs for the split where padding every
-  // problem to 256 rows adds at most 10 % of MMA work (FP8 always runs on
-  // single CTAs).
-  if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1' && mode != kModeFp8) {
+  // Pairs (GBBLAS_TC_PAIR=1, or the autotuner's choice for a shape) run the
+  // split where padding every problem to 256 rows adds at most 10 % of MMA
+  // work (FP8 always runs on single CTAs).
+  bool want_pair = opt.pair == 1;
+  if (opt.pair < 0)
+    if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1') want_pair = true;
+  if (want_pair && mode != kModeFp8) {
     double w1 = 0, w2 = 0;
     for (int64_t i : order) {
       const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, sk);
@@ -847,27 +896,42 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     pl.pair = w2 <= 1.1 * w1;
   }
   const int64_t bmt = pl.pair ? 2 * kBM : kBM;  // output tile rows
-  pl.nprob = (int)order.size();
-  pl.probs.resize(pl.nprob);
-  pl.ajobs.resize(pl.nprob);
-  pl.bjobs.resize(pl.nprob);
-  for (int i = 0; i < pl.nprob; ++i) pl.kpad = std::max<int64_t>(pl.kpad, round_up(d[order[i]].K, sk));
+  pl.njobs = (int)order.size();
+  pl.ajobs.resize(pl.njobs);
+  pl.bjobs.resize(pl.njobs);
+  for (int i = 0; i < pl.njobs; ++i) pl.kpad = std::max<int64_t>(pl.kpad, round_up(d[order[i]].K, sk));
   pl.pitch = pl.kpad + kPitchPadBytes / (pl.fp8() ? 1 : (int64_t)sizeof(__nv_bfloat16));
-  for (int i = 0; i < pl.nprob; ++i) {
+  int64_t ws = 0;  // partial workspace bytes
+  for (int i = 0; i < pl.njobs; ++i) {
     const gbblas_gemm_desc& g = d[order[i]];
     const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
-    TcProblem& p = pl.probs[i];
-    p.M = (int)g.M;
-    p.N = (int)g.N;
-    p.num_kt = (int)(Kp / sk);
-    p.a_row = (int)pl.a_rows;
-    p.b_row = (int)pl.b_rows;
-    p.tiles_m = (int)(Mp / bmt);
-    p.tiles_n = (int)(Np / kBN);
-    p.tile_start = (int)pl.tiles;
-    p.C = g.C;
-    p.rsc = g.rsc;
-    p.csc = g.csc;
+    const int num_kt = (int)(Kp / sk);
+    const int parts = std::max(1, std::min(opt.split, num_kt));
+    const int64_t ppitch = round_up(g.N, 4);  // partial rows stay 16-byte aligned
+    if (parts > 1) {
+      pl.reds.push_back({g.C, g.rsc, g.csc, nullptr, (int)g.M, (int)g.N, (int)ppitch, parts});
+      pl.red_off.push_back(ws);
+    }
+    for (int part = 0; part < parts; ++part) {
+      TcProblem p;
+      p.M = (int)g.M;
+      p.N = (int)g.N;
+      p.kt0 = (int)((int64_t)num_kt * part / parts);
+      p.num_kt = (int)((int64_t)num_kt * (part + 1) / parts) - p.kt0;
+      p.a_row = (int)pl.a_rows;
+      p.b_row = (int)pl.b_rows;
+      p.tiles_m = (int)(Mp / bmt);
+      p.tiles_n = (int)(Np / kBN);
+      p.tile_start = (int)pl.tiles;
+      p.overwrite = parts > 1 ? 1 : 0;
+      p.C = parts > 1 ? nullptr : g.C;  // partials: pointed into the workspace when bound
+      p.rsc = parts > 1 ? ppitch : g.rsc;
+      p.csc = parts > 1 ? 1 : g.csc;
+      pl.probs.push_back(p);
+      pl.part_off.push_back(parts > 1 ? ws : -1);
+      if (parts > 1) ws += (int64_t)g.M * ppitch * (int64_t)sizeof(float);
+      pl.tiles += (int64_t)p.tiles_m * p.tiles_n;
+    }
     pl.ajobs[i] = {g.A, g.M, g.K, g.rsa, g.csa, pl.a_rows, (int)(Mp / jr), (int)(Kp / jk), pl.a_tiles};
     pl.a_tiles += pl.ajobs[i].tiles_r * pl.ajobs[i].tiles_k;
     // B^T: element (n, k) = B[k*rsb + n*csb]
@@ -875,8 +939,8 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     pl.b_tiles += pl.bjobs[i].tiles_r * pl.bjobs[i].tiles_k;
     pl.a_rows += Mp;
     pl.b_rows += Np;
-    pl.tiles += (int64_t)p.tiles_m * p.tiles_n;
   }
+  pl.nprob = (int)pl.probs.size();
   if ((double)(pl.a_rows + pl.b_rows) * pl.planes() >= 2.0e9 || pl.tiles >= (1ll << 31) ||
       (double)pl.a_tiles >= 2.0e9 || (double)pl.b_tiles >= 2.0e9) {
     set_error("tensor-core gemm: group too large for one launch");
@@ -885,12 +949,14 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   const size_t esize = pl.fp8() ? 1 : sizeof(__nv_bfloat16);
   pl.off_probs = kScratchZeroBytes;
   pl.off_jobs = pl.off_probs + align256(sizeof(TcProblem) * pl.nprob);
-  pl.off_arena = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.nprob);
+  pl.off_red = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.njobs);
+  pl.off_arena = pl.off_red + align256(sizeof(SplitReduce) * pl.reds.size());
   const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
   pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
   const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : 0;  // one 4-byte scale word per row and K-block
   pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
-  pl.bytes = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
+  pl.off_ws = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
+  pl.bytes = pl.off_ws + align256((size_t)ws);
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -907,12 +973,20 @@ uint32_t* scales_b(const TcGroupPlan& pl) { return reinterpret_cast<uint32_t*>(p
 gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
   pl.base = base;
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
+  for (int i = 0; i < pl.nprob; ++i)
+    if (pl.part_off[i] >= 0) pl.probs[i].C = reinterpret_cast<float*>(base + pl.off_ws + pl.part_off[i]);
+  for (size_t r = 0; r < pl.reds.size(); ++r)
+    pl.reds[r].part = reinterpret_cast<const float*>(base + pl.off_ws + pl.red_off[r]);
+  // (the host tables must outlive these copies: they live in the plan)
   GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_probs, pl.probs.data(), sizeof(TcProblem) * pl.nprob,
                               cudaMemcpyHostToDevice, stream));
-  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs, pl.ajobs.data(), sizeof(SplitJob) * pl.nprob,
+  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs, pl.ajobs.data(), sizeof(SplitJob) * pl.njobs,
                               cudaMemcpyHostToDevice, stream));
-  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs + sizeof(SplitJob) * pl.nprob, pl.bjobs.data(),
-                              sizeof(SplitJob) * pl.nprob, cudaMemcpyHostToDevice, stream));
+  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs + sizeof(SplitJob) * pl.njobs, pl.bjobs.data(),
+                              sizeof(SplitJob) * pl.njobs, cudaMemcpyHostToDevice, stream));
+  if (!pl.reds.empty())
+    GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_red, pl.reds.data(), sizeof(SplitReduce) * pl.reds.size(),
+                                cudaMemcpyHostToDevice, stream));
   GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)pl.a_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(), kBM,
                   pl.fp8()));
   GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)pl.b_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(),
@@ -1003,21 +1077,33 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
   // FP8 scale words: 128 per K-block of each 128-row block, i.e. `kpad` per row block
-  prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.nprob, arena_a(pl),
+  prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, arena_a(pl),
                                                           (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
                                                           pl.kpad);
   GB_TRY(check_launch("prep_group_kernel(A)"));
-  prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.nprob, pl.nprob, arena_b(pl),
+  prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, arena_b(pl),
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
                                                           pl.kpad);
   GB_TRY(check_launch("prep_group_kernel(B)"));
+  gbblas_status st;
   if constexpr (MODE != kModeFp8) {
-    if (pl.pair) return launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas);
+    st = pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
+                 : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
+  } else {
+    st = launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
   }
-  return launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
+  if (st != GBBLAS_STATUS_SUCCESS || pl.reds.empty()) return st;
+  int64_t most = 0;
+  for (const SplitReduce& r : pl.reds) most = std::max<int64_t>(most, (int64_t)r.M * r.N);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((most + 255) / 256, 4 * (int64_t)c->num_sms));
+  splitk_reduce_kernel<<<dim3(blocks, (unsigned)pl.reds.size()), 256, 0, stream>>>(
+      reinterpret_cast<const SplitReduce*>(pl.base + pl.off_red));
+  return check_launch("splitk_reduce_kernel");
 }
 
 }  // namespace
+
+int tc_stage_k(int mode) { return mode == kModeFp8 ? ModeTraits<kModeFp8>::kBKe : kBK; }
 
 int tc_mode(gbblas_accuracy acc) {
   switch (acc) {
@@ -1105,12 +1191,23 @@ gbblas_status launch_gemm_tc_group(DeviceCtx* c, int mode, const gbblas_gemm_des
   return tc_group_launch(c, &pl, stream, max_ctas);
 }
 
+gbblas_status launch_gemm_tc_opts(DeviceCtx* c, int mode, const gbblas_gemm_desc& d, const TcLaunchOpts& opt,
+                                  cudaStream_t stream) {
+  TcGroupPlan pl;
+  GB_TRY(plan_group(mode, &d, 1, pl, opt));
+  if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
+  void* s = nullptr;
+  GB_TRY(get_scratch(c, stream, pl.bytes, &s));
+  GB_TRY(bind_group(pl, static_cast<char*>(s), stream));
+  return tc_group_launch(c, &pl, stream, 0);
+}
+
 gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                              int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
                              int64_t csc, cudaStream_t stream) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   gbblas_gemm_desc d{M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc};
-  return launch_gemm_tc_group(c, mode, &d, 1, stream);
+  return launch_gemm_tc_opts(c, mode, d, tuned_tc_opts(c, mode, M, N, K, stream), stream);
 }
 
 }  // namespace gbblas

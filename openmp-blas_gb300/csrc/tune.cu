@@ -18,7 +18,16 @@
 //                    (1, 2, 4, 8), bucketed by median log2 rows / cols;
 //   gemm_auto        for GBBLAS_ACCURACY_AUTO, FP32 FMA kernel or split-BF16
 //                    (six products) - both FP32-accurate - bucketed by
-//                    log2 M, N, K.
+//                    log2 M, N, K;
+//   gemm_tc          per tensor-core mode and log2 M, N, K bucket: split-K
+//                    parts (1, 2, 4, 8, 16; offered when K >= 4 max(M, N) and
+//                    the output tiles fill at most half the SMs) and the CTA
+//                    form (single CTAs or CTA pairs, split-BF16 only);
+//                    GBBLAS_TC_SPLITK=n forces n parts;
+//   gemm_fma_tile    FP32 FMA CTA tile, 128 x 128 or 64 x 64, per bucket.
+// Nothing is timed while the caller's stream is being captured into a graph
+// (the defaults apply); single-call paths consult the tuner, grouped,
+// batched and served launches use the defaults.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -128,6 +137,79 @@ std::string device_tag(DeviceCtx* c) {
 
 int log2_bucket(int64_t v) { return v <= 1 ? 0 : (int)std::lround(std::log2((double)v)); }
 
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return true;  // unknown: do not time
+  }
+  return st != cudaStreamCaptureStatusNone;
+}
+
+// Scratch FP32 operands (zeros) for timing one GEMM shape on the tuner's own
+// stream; each candidate runs once to warm up, then 3 times between events.
+class GemmBench {
+ public:
+  GemmBench(DeviceCtx* c, int64_t m, int64_t n, int64_t k) : c_(c), m_(m), n_(n), k_(k) {
+    if (cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking) != cudaSuccess) return;
+    const size_t bytes = sizeof(float) * (size_t)(m * k + k * n + m * n);
+    if (cudaMallocAsync(&mem_, bytes, s_) != cudaSuccess) {
+      mem_ = nullptr;
+      return;
+    }
+    cudaMemsetAsync(mem_, 0, bytes, s_);
+    cudaEventCreate(&e0_);
+    cudaEventCreate(&e1_);
+  }
+  ~GemmBench() {
+    if (mem_) cudaFreeAsync(mem_, s_);
+    if (s_) {
+      cudaStreamSynchronize(s_);
+      release_scratch(c_, s_);
+      cudaStreamDestroy(s_);
+    }
+    if (e0_) cudaEventDestroy(e0_);
+    if (e1_) cudaEventDestroy(e1_);
+  }
+  bool ok() const { return mem_ != nullptr; }
+  gbblas_gemm_desc desc() const {
+    float* A = static_cast<float*>(mem_);
+    float* B = A + m_ * k_;
+    float* C = B + k_ * n_;
+    return gbblas_gemm_desc{m_, n_, k_, A, k_, 1, B, n_, 1, C, n_, 1};
+  }
+  cudaStream_t stream() const { return s_; }
+  // ms per call of run(stream), or a huge value if it failed
+  template <typename F>
+  float time(F&& run) {
+    if (run(s_) != GBBLAS_STATUS_SUCCESS) return 1e30f;
+    cudaEventRecord(e0_, s_);
+    for (int i = 0; i < 3; ++i)
+      if (run(s_) != GBBLAS_STATUS_SUCCESS) return 1e30f;
+    cudaEventRecord(e1_, s_);
+    if (cudaEventSynchronize(e1_) != cudaSuccess) return 1e30f;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0_, e1_);
+    return ms;
+  }
+
+ private:
+  DeviceCtx* c_;
+  int64_t m_, n_, k_;
+  cudaStream_t s_ = nullptr;
+  void* mem_ = nullptr;
+  cudaEvent_t e0_ = nullptr, e1_ = nullptr;
+};
+
+// Representative shape of a log2 bucket: 2^b per dimension, M and N at most
+// 8192, K at most 2^16, and the operands at most 2^28 elements.
+void bucket_shape(int bm, int bn, int bk, int64_t& m, int64_t& n, int64_t& k) {
+  m = std::min<int64_t>(int64_t(1) << bm, 8192);
+  n = std::min<int64_t>(int64_t(1) << bn, 8192);
+  k = std::min<int64_t>(int64_t(1) << bk, 65536);
+  while ((m + n) * k > (int64_t(1) << 28) && k > 64) k >>= 1;
+}
+
 }  // namespace
 
 int tuned_gemv_group_rows(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count) {
@@ -217,6 +299,93 @@ int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
   cudaStreamDestroy(s);
   if (best_ms[0] >= 1e30f && best_ms[1] >= 1e30f) return fallback;
   const int best = best_ms[1] < best_ms[0] ? 1 : 0;
+  t.store(key, best);
+  return best;
+}
+
+// Split-K parts worth trying for an M x N x K tensor-core GEMM: K at least
+// four times the larger output side, output tiles filling at most half the
+// SMs, every part at least 8 K stages, parts x tiles at most twice the SMs.
+static std::vector<int> split_candidates(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K) {
+  std::vector<int> out;
+  const int64_t tiles = ((M + 127) / 128) * ((N + 127) / 128);
+  const int64_t stages = (K + tc_stage_k(mode) - 1) / tc_stage_k(mode);
+  if (K < 4 * std::max(M, N) || 2 * tiles > c->num_sms) return out;
+  for (int s : {2, 4, 8, 16})
+    if (stages >= 8 * s && tiles * s <= 2 * (int64_t)c->num_sms) out.push_back(s);
+  return out;
+}
+
+TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, cudaStream_t stream) {
+  TcLaunchOpts def;
+  if (const char* e = std::getenv("GBBLAS_TC_SPLITK"); e && std::atoi(e) > 0) {
+    def.split = std::atoi(e);
+    return def;
+  }
+  const std::vector<int> splits = split_candidates(c, mode, M, N, K);
+  // GBBLAS_TC_PAIR, when set, fixes the CTA form; otherwise the tuner picks it
+  // (pairs only where padding M to 256 rows adds at most 10 % of the work)
+  const char* pe = std::getenv("GBBLAS_TC_PAIR");
+  const bool pair_env = pe && pe[0];
+  const int single = pair_env ? -1 : 0;
+  const bool pairs = !pair_env && mode != tc_mode(GBBLAS_ACCURACY_FP8) && M >= 256 &&
+                     (double)((M + 255) / 256 * 256) <= 1.1 * (double)((M + 127) / 128 * 128);
+  // without measurements: the largest listed split (the tiles alone leave
+  // most SMs idle) and the GBBLAS_TC_PAIR setting
+  TcLaunchOpts fallback = def;
+  if (!splits.empty()) fallback.split = splits.back();
+  if (splits.empty() && !pairs) return def;
+  Tuner& t = Tuner::get();
+  const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
+  const std::string key = "gemm_tc|" + device_tag(c) + "|mode" + std::to_string(mode) + "|m" + std::to_string(bm) +
+                          "|n" + std::to_string(bn) + "|k" + std::to_string(bk);
+  const int v = t.lookup(key);
+  if (v >= 0) return TcLaunchOpts{std::max(1, v / 4), pair_env ? -1 : v % 4 - 1};
+  if (!t.enabled() || capturing(stream)) return fallback;
+  int64_t m, n, k;
+  bucket_shape(bm, bn, bk, m, n, k);
+  std::vector<TcLaunchOpts> cands{TcLaunchOpts{1, single}};
+  for (int s : split_candidates(c, mode, m, n, k)) cands.push_back(TcLaunchOpts{s, single});
+  if (pairs && m >= 256) cands.push_back(TcLaunchOpts{1, 1});
+  if (cands.size() == 1) return fallback;
+  GemmBench b(c, m, n, k);
+  if (!b.ok()) return fallback;
+  const gbblas_gemm_desc d = b.desc();
+  TcLaunchOpts best = fallback;
+  float best_ms = 1e30f;
+  for (const TcLaunchOpts& o : cands) {
+    const float ms = b.time([&](cudaStream_t s) { return launch_gemm_tc_opts(c, mode, d, o, s); });
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = o;
+    }
+  }
+  if (best_ms >= 1e30f) return fallback;
+  t.store(key, best.split * 4 + best.pair + 1);
+  return best;
+}
+
+int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t stream) {
+  Tuner& t = Tuner::get();
+  const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
+  const std::string key = "gemm_fma_tile|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
+                          "|k" + std::to_string(bk) + "|f32";
+  const int v = t.lookup(key);
+  if (v >= 0) return v;
+  if (!t.enabled() || capturing(stream) || (double)M * N * K < 1.0e8) return -1;  // small: the tile-count rule
+  int64_t m, n, k;
+  bucket_shape(bm, bn, bk, m, n, k);
+  GemmBench b(c, m, n, k);
+  if (!b.ok()) return -1;
+  const gbblas_gemm_desc d = b.desc();
+  float ms[2];
+  for (int tile = 0; tile < 2; ++tile)
+    ms[tile] = b.time([&](cudaStream_t s) {
+      return launch_gemm_fma<float>(c, d.M, d.N, d.K, d.A, d.rsa, d.csa, d.B, d.rsb, d.csb, d.C, d.rsc, d.csc, s, 0,
+                                    tile);
+    });
+  if (ms[0] >= 1e30f && ms[1] >= 1e30f) return -1;
+  const int best = ms[1] < ms[0] ? 1 : 0;
   t.store(key, best);
   return best;
 }
