@@ -341,8 +341,16 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if constexpr (sizeof(T) == 4) {
     const int64_t big_tiles = ((M + 127) / 128) * ((N + 127) / 128);
-    if (tile < 0) tile = big_tiles >= 2 * (int64_t)c->num_sms ? 1 : 0;
-    if (tile == 1)
+    const bool tma = sgemm_tma_eligible(M, N, K, A, rsa, csa, B, rsb, csb);
+    // default: TMA-fed where B is row-major (at 8192^3: 63.8 / 58.7 TFLOP/s
+    // with A column- / row-major against 58.9 / 57.5 register-staged; with B
+    // column-major its FMA pairs need register moves and it trails)
+    if (tile < 0)
+      tile = (tma && csb == 1 && big_tiles >= (int64_t)c->num_sms) ? 2
+                                                                   : (big_tiles >= 2 * (int64_t)c->num_sms ? 1 : 0);
+    if (tile == 2 && tma)
+      return launch_sgemm_tma(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    if (tile >= 1)
       return launch_cfg<float, 128, 128, 16, 8, 8>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,
                                                    max_ctas);
     return launch_cfg<float, 64, 64, 16, 4, 4>(la, lb, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream,

@@ -72,6 +72,7 @@
 
 #include "common.cuh"
 #include "tc_ptx.cuh"
+#include "tma_map.cuh"
 
 namespace gbblas {
 namespace {
@@ -818,6 +819,32 @@ gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64
 }
 
 inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
+gbblas_status make_map_f32_2d(CUtensorMap* map, const float* base, uint64_t inner, uint64_t outer,
+                              uint64_t row_stride, uint32_t box_inner, uint32_t box_outer, bool swizzle128) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return GBBLAS_STATUS_CUDA_ERROR;
+  }
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {row_stride * sizeof(float)};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d) for a %llu x %llu float matrix", (int)r, (unsigned long long)outer,
+              (unsigned long long)inner);
+    return GBBLAS_STATUS_CUDA_ERROR;
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+namespace {
 
 // Bytes added to every arena row beyond the padded K.
 constexpr int64_t kPitchPadBytes = 0;
