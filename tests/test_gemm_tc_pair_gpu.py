@@ -1,7 +1,8 @@
 """The CTA-pair form of the tensor-core GEMM (GBBLAS_TC_PAIR=1: clusters of
 two CTAs, tcgen05 .cta_group::2 MMAs on 256 x 128 tiles) against FP64 with the
-split-BF16 bounds and bit-exact on integer FP8 data, including ragged shapes,
-both layouts and a grouped launch."""
+split-BF16 bounds, including ragged shapes, both layouts and a grouped launch.
+FP8 always runs on single CTAs: with the setting on it must still be
+bit-exact on integer data and follow the quantisation model."""
 import numpy as np
 import pytest
 
@@ -37,7 +38,7 @@ def test_pair_split_vs_fp64(cuda, pairs, mode, shape, lc, la, lb):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-def test_pair_fp8(cuda, pairs, shape):
+def test_fp8_unaffected_by_pair_setting(cuda, pairs, shape):
     M, N, K = shape
     rng = np.random.default_rng(M + N + K)
     A = rng.integers(-8, 9, (M, K)).astype(np.float32)
