@@ -265,5 +265,41 @@ __device__ __forceinline__ T block_sum(T v, T* sh) {
   return t;
 }
 
+// ---- thread-block clusters (distributed shared memory)
+// CTAs in this CTA's cluster (1 for a launch without clusters).
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+// Rank of this CTA in its cluster.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Barrier over every thread of every CTA of the cluster (release / acquire:
+// shared-memory writes before it are visible to the cluster's CTAs after).
+// Each thread must reach it: kernels that use it exit no thread early.
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Load the object at shared address `p` of this CTA as it sits in the shared
+// memory of CTA `rank` of the cluster.
+__device__ __forceinline__ double dsmem_ld(const double* p, unsigned rank) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
+  double v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(r) : "memory");
+  return v;
+}
+__device__ __forceinline__ float dsmem_ld(const float* p, unsigned rank) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
+  float v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(r) : "memory");
+  return v;
+}
+
 }  // namespace gbblas::dev
 #endif

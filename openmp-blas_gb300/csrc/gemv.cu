@@ -15,10 +15,16 @@
 //
 // Both stream A from HBM exactly once with 128-bit read-only loads and keep
 // x in L1/L2.  When the grid would be too small to fill the 152 SMs the
-// reduction dimension is split across CTAs; split partials go to per-stream
-// scratch and a second small kernel adds them in split order, so results are
-// deterministic (no atomics).  Roofline: HBM, (rows*cols + rows + cols) *
-// sizeof(T) bytes per call.
+// reduction dimension is split across CTAs.  Two splits, or up to 8 on a
+// small matrix, run as one thread-block cluster per row block: each CTA
+// leaves its partials in its shared memory and the cluster's rank 0 adds
+// them in split order through distributed shared memory.  Otherwise the
+// partials go to per-stream scratch and a second small kernel adds them in
+// split order.  Either way
+// the additions are in the same order and deterministic (no atomics).
+// Roofline: HBM, (rows*cols + rows + cols) * sizeof(T) bytes per call.
+#include <utility>
+
 #include "common.cuh"
 
 namespace gbblas {
@@ -52,8 +58,19 @@ __device__ __forceinline__ double2 ldg_vec(const double2* p) { return __ldg(p); 
 
 constexpr int kRowsThreads = 256;
 
+constexpr int kMaxClusterSplits = 8;  // portable cluster size
+
+// Whether the ksplit CTAs of a row block reduce as one cluster.  Measured on
+// split shapes: clusters of two stream as fast as separate CTAs; up to 8 pay
+// off while the matrix is small (12-60 MB: 17-24 % faster, the second launch
+// saved); on large matrices clusters of 3-4 lose up to 17 % of the bandwidth.
+inline bool cluster_splits(int64_t ksplit, int64_t rows, int64_t cols, size_t elem) {
+  return ksplit >= 2 && ksplit <= kMaxClusterSplits && (ksplit == 2 || (double)rows * cols * elem <= 64.0e6);
+}
+
 // grid = (ceil(rows / R), ksplit); CTA = 8 warps splitting its column range.
-template <typename T, int R, bool VEC>
+// CL: the ksplit CTAs of a row block form a cluster (1, ksplit, 1).
+template <typename T, int R, bool VEC, bool CL>
 __global__ void __launch_bounds__(kRowsThreads) gemv_rows_kernel(int64_t rows, int64_t cols,
                                                                  const T* __restrict__ A, int64_t lda,
                                                                  const T* __restrict__ x, T* __restrict__ y,
@@ -62,6 +79,7 @@ __global__ void __launch_bounds__(kRowsThreads) gemv_rows_kernel(int64_t rows, i
   using VT = typename V<T>::t;
   constexpr int W = V<T>::w;
   __shared__ T red[kRowsThreads / 32][R];
+  __shared__ T split_part[R];  // CL: this split's row sums, read by the cluster's rank 0
   const int64_t r0 = (int64_t)blockIdx.x * R;
   const int64_t c0 = (int64_t)blockIdx.y * cols_per_split;
   int64_t c1 = c0 + cols_per_split;
@@ -118,11 +136,23 @@ __global__ void __launch_bounds__(kRowsThreads) gemv_rows_kernel(int64_t rows, i
     T s = T(0);
 #pragma unroll
     for (int w = 0; w < kRowsThreads / 32; ++w) s += red[w][r];
-    if (gridDim.y == 1) {
+    if (CL) {
+      split_part[r] = s;
+    } else if (gridDim.y == 1) {
       y[r0 + r] = accumulate ? y[r0 + r] + s : s;
     } else {
       partials[(int64_t)blockIdx.y * rows + r0 + r] = s;
     }
+  }
+  if constexpr (CL) {
+    dev::cluster_sync();
+    if (blockIdx.y == 0 && threadIdx.x < nr) {  // rank 0 of the cluster: splits in order
+      const int r = threadIdx.x;
+      T s = T(0);
+      for (unsigned k = 0; k < gridDim.y; ++k) s += dev::dsmem_ld(&split_part[r], k);
+      y[r0 + r] = accumulate ? y[r0 + r] + s : s;
+    }
+    dev::cluster_sync();  // the other splits stay resident until rank 0 has read them
   }
 }
 
@@ -140,16 +170,18 @@ __global__ void finish_splits_kernel(int64_t rows, int ksplit, const T* __restri
 constexpr int kColsUnroll = 8;
 
 // grid = (ceil(rows / (threads*W)), ksplit).  Each thread owns W (VEC) or 1
-// consecutive rows and walks its CTA's column range.
-template <typename T, bool VEC>
+// consecutive rows and walks its CTA's column range.  CL: the ksplit CTAs of
+// a row block form a cluster (1, ksplit, 1); no thread leaves early then.
+template <typename T, bool VEC, bool CL>
 __global__ void __launch_bounds__(256) gemv_cols_kernel(int64_t rows, int64_t cols, const T* __restrict__ A,
                                                         int64_t lda, const T* __restrict__ x, T* __restrict__ y,
                                                         bool accumulate, T* __restrict__ partials,
                                                         int64_t cols_per_split) {
   using VT = typename V<T>::t;
   constexpr int W = VEC ? V<T>::w : 1;
+  __shared__ T split_part[CL ? 256 * W : 1];
   const int64_t rbase = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * W;
-  if (rbase >= rows) return;
+  if (!CL && rbase >= rows) return;
   const int64_t c0 = (int64_t)blockIdx.y * cols_per_split;
   int64_t c1 = c0 + cols_per_split;
   if (c1 > cols) c1 = cols;
@@ -157,7 +189,9 @@ __global__ void __launch_bounds__(256) gemv_cols_kernel(int64_t rows, int64_t co
 #pragma unroll
   for (int i = 0; i < W; ++i) acc[i] = T(0);
   const bool full = rbase + W <= rows;
-  if (VEC && full) {
+  if (rbase >= rows) {
+    // CL only: nothing to add, but the thread still meets the cluster barriers
+  } else if (VEC && full) {
     const T* base = A + rbase;
     int64_t c = c0;
     for (; c + kColsUnroll <= c1; c += kColsUnroll) {
@@ -190,19 +224,55 @@ __global__ void __launch_bounds__(256) gemv_cols_kernel(int64_t rows, int64_t co
         if (rbase + i < rows) acc[i] = fma(dev::ld_stream(A + rbase + i + c * lda), xc, acc[i]);
     }
   }
+  if constexpr (CL) {
 #pragma unroll
-  for (int i = 0; i < W; ++i) {
-    const int64_t r = rbase + i;
-    if (r < rows) {
-      if (gridDim.y == 1)
-        y[r] = accumulate ? y[r] + acc[i] : acc[i];
-      else
-        partials[(int64_t)blockIdx.y * rows + r] = acc[i];
+    for (int i = 0; i < W; ++i) split_part[threadIdx.x * W + i] = acc[i];
+    __syncwarp();  // lanes past the last row rejoin before the aligned cluster barrier
+    dev::cluster_sync();
+    if (blockIdx.y == 0) {  // rank 0 of the cluster: splits in order
+#pragma unroll
+      for (int i = 0; i < W; ++i) {
+        const int64_t r = rbase + i;
+        if (r < rows) {
+          T s = T(0);
+          for (unsigned k = 0; k < gridDim.y; ++k) s += dev::dsmem_ld(&split_part[threadIdx.x * W + i], k);
+          y[r] = accumulate ? y[r] + s : s;
+        }
+      }
+    }
+    dev::cluster_sync();  // the other splits stay resident until rank 0 has read them
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int64_t r = rbase + i;
+      if (r < rows) {
+        if (gridDim.y == 1)
+          y[r] = accumulate ? y[r] + acc[i] : acc[i];
+        else
+          partials[(int64_t)blockIdx.y * rows + r] = acc[i];
+      }
     }
   }
 }
 
 inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Launch with clusters of (1, grid.y, 1): the splits of one row block.
+template <typename... P, typename... A>
+cudaError_t launch_split_clusters(void (*kernel)(P...), dim3 grid, int threads, cudaStream_t stream, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 1;
+  at[0].val.clusterDim.y = grid.y;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 }  // namespace
 
@@ -226,27 +296,42 @@ gbblas_status launch_gemv_rows(DeviceCtx* c, int64_t rows, int64_t cols, const T
   int64_t cps = cdiv(cdiv(cols, ksplit), 256) * 256;  // multiple of the vector width
   ksplit = cdiv(cols, cps);
   if (ksplit < 1) ksplit = 1;
+  dim3 grid((unsigned)groups, (unsigned)ksplit);
   T* partials = nullptr;
+  if (cluster_splits(ksplit, rows, cols, sizeof(T))) {
+    cudaError_t e;
+    if (R == 4)
+      e = vec ? launch_split_clusters(gemv_rows_kernel<T, 4, true, true>, grid, kRowsThreads, stream, rows, cols, A,
+                                      lda, x, y, accumulate, partials, cps)
+              : launch_split_clusters(gemv_rows_kernel<T, 4, false, true>, grid, kRowsThreads, stream, rows, cols, A,
+                                      lda, x, y, accumulate, partials, cps);
+    else
+      e = vec ? launch_split_clusters(gemv_rows_kernel<T, 1, true, true>, grid, kRowsThreads, stream, rows, cols, A,
+                                      lda, x, y, accumulate, partials, cps)
+              : launch_split_clusters(gemv_rows_kernel<T, 1, false, true>, grid, kRowsThreads, stream, rows, cols, A,
+                                      lda, x, y, accumulate, partials, cps);
+    if (e == cudaSuccess) return check_launch("gemv_rows_kernel (split clusters)");
+    cudaGetLastError();  // the cluster launch was refused: partials in scratch instead
+  }
   if (ksplit > 1) {
     void* s = nullptr;
     GB_TRY(get_scratch(c, stream, kScratchZeroBytes + sizeof(T) * ksplit * rows, &s));
     partials = reinterpret_cast<T*>(static_cast<char*>(s) + kScratchZeroBytes);
   }
-  dim3 grid((unsigned)groups, (unsigned)ksplit);
   if (R == 4) {
     if (vec)
-      gemv_rows_kernel<T, 4, true><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
-                                                                      partials, cps);
+      gemv_rows_kernel<T, 4, true, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
+                                                                             partials, cps);
     else
-      gemv_rows_kernel<T, 4, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
-                                                                       partials, cps);
+      gemv_rows_kernel<T, 4, false, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
+                                                                              partials, cps);
   } else {
     if (vec)
-      gemv_rows_kernel<T, 1, true><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
-                                                                      partials, cps);
+      gemv_rows_kernel<T, 1, true, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
+                                                                             partials, cps);
     else
-      gemv_rows_kernel<T, 1, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
-                                                                       partials, cps);
+      gemv_rows_kernel<T, 1, false, false><<<grid, kRowsThreads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate,
+                                                                              partials, cps);
   }
   GB_TRY(check_launch("gemv_rows_kernel"));
   if (ksplit > 1) {
@@ -279,17 +364,27 @@ gbblas_status launch_gemv_cols(DeviceCtx* c, int64_t rows, int64_t cols, const T
   int64_t cps = cdiv(cols, ksplit);
   ksplit = cdiv(cols, cps);
   if (ksplit < 1) ksplit = 1;
+  dim3 grid((unsigned)rblocks, (unsigned)ksplit);
   T* partials = nullptr;
+  if (cluster_splits(ksplit, rows, cols, sizeof(T))) {
+    const cudaError_t e = vec ? launch_split_clusters(gemv_cols_kernel<T, true, true>, grid, threads, stream, rows,
+                                                      cols, A, lda, x, y, accumulate, partials, cps)
+                              : launch_split_clusters(gemv_cols_kernel<T, false, true>, grid, threads, stream, rows,
+                                                      cols, A, lda, x, y, accumulate, partials, cps);
+    if (e == cudaSuccess) return check_launch("gemv_cols_kernel (split clusters)");
+    cudaGetLastError();  // the cluster launch was refused: partials in scratch instead
+  }
   if (ksplit > 1) {
     void* s = nullptr;
     GB_TRY(get_scratch(c, stream, kScratchZeroBytes + sizeof(T) * ksplit * rows, &s));
     partials = reinterpret_cast<T*>(static_cast<char*>(s) + kScratchZeroBytes);
   }
-  dim3 grid((unsigned)rblocks, (unsigned)ksplit);
   if (vec)
-    gemv_cols_kernel<T, true><<<grid, threads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate, partials, cps);
+    gemv_cols_kernel<T, true, false><<<grid, threads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate, partials,
+                                                                   cps);
   else
-    gemv_cols_kernel<T, false><<<grid, threads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate, partials, cps);
+    gemv_cols_kernel<T, false, false><<<grid, threads, 0, stream>>>(rows, cols, A, lda, x, y, accumulate, partials,
+                                                                    cps);
   GB_TRY(check_launch("gemv_cols_kernel"));
   if (ksplit > 1) {
     finish_splits_kernel<T><<<(unsigned)cdiv(rows, 256), 256, 0, stream>>>(rows, (int)ksplit, partials, y,
