@@ -254,6 +254,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def fma_peak_tflops(clocks=None):
+    """Nominal FP32 FMA-pipe peak of this GPU: SMs x 128 lanes x 2 flop x the
+    maximum SM clock (from the clock samples, else the device property)."""
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def gemm_headline(dev, sp):
     """The first part of the headline metric beside the bandwidth line
     (outside the timed region): C = A*B at M = N = K = 8192 from float32
@@ -296,6 +305,7 @@ def gemm_headline(dev, sp):
         rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
         out[path] = {"value": round(2.0 * n ** 3 / (ms / 1e3) / 1e12, 2), "ms": round(ms, 3),
                      "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean())}
+    out["fp32"]["fma_frac"] = round(out["fp32"]["value"] / fma_peak_tflops(), 4)
     out["bf16x6_over_fp32"] = round(out["bf16x6"]["value"] / out["fp32"]["value"], 2)
     out["bf16x3_over_fp32"] = round(out["bf16x3"]["value"] / out["fp32"]["value"], 2)
     del A, B, C
@@ -595,6 +605,11 @@ def run_precision(args):
                 line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
                 line["tensor_peak"] = (f"{products} BF16 products per algorithmic flop vs bf16_tflops "
                                        f"{peaks['bf16_tflops']} (measured, burst)")
+            if path == "fp32":
+                fma_peak = fma_peak_tflops(line["clocks"])
+                line["fma_frac"] = round(tf / fma_peak, 4)
+                line["fma_peak"] = (f"{fma_peak:.1f} TFLOP/s: SMs x 128 FP32 FMA lanes x 2 flop x max SM clock "
+                                    "(nominal; no FMA peak is measured)")
             if path == "fp8" and peaks.get("bf16_tflops"):
                 line["tensor_frac"] = round(tf / (2 * peaks["bf16_tflops"]), 4)
                 line["tensor_peak"] = (f"2 x bf16_tflops {peaks['bf16_tflops']} (measured BF16 burst times the "
