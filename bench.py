@@ -306,6 +306,12 @@ def gemm_headline(dev, sp):
         out[path] = {"value": round(2.0 * n ** 3 / (ms / 1e3) / 1e12, 2), "ms": round(ms, 3),
                      "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean())}
     out["fp32"]["fma_frac"] = round(out["fp32"]["value"] / fma_peak_tflops(), 4)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        bf16 = json.load(open(peaks_path)).get("bf16_tflops")
+        if bf16:  # BF16 products per algorithmic flop against the measured BF16 burst
+            out["bf16x6"]["tensor_frac"] = round(6 * out["bf16x6"]["value"] / bf16, 4)
+            out["bf16x3"]["tensor_frac"] = round(3 * out["bf16x3"]["value"] / bf16, 4)
     out["bf16x6_over_fp32"] = round(out["bf16x6"]["value"] / out["fp32"]["value"], 2)
     out["bf16x3_over_fp32"] = round(out["bf16x3"]["value"] / out["fp32"]["value"], 2)
     del A, B, C
