@@ -134,6 +134,7 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
 // multiple of 4 elements.
 bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa, const float* B,
                         int64_t rsb, int64_t csb);
+void sgemm_tma_prepare(DeviceCtx* c);  // kernel attributes, before any stream capture
 gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                                int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
                                int64_t csc, cudaStream_t stream, int max_ctas = 0);

@@ -26,6 +26,8 @@
 // from tile to tile.  Roofline: the FMA pipes, 2*M*N*K flops.
 #include <cuda.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "tc_ptx.cuh"
 #include "tma_map.cuh"
@@ -272,14 +274,24 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// The four kernels' shared-memory attribute, once per device (before any
+// stream capture: tc_prepare calls this too).
+void set_attributes(DeviceCtx* c) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[c->device & 63]) return;
+  cudaFuncSetAttribute(sgemm_tma_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  cudaFuncSetAttribute(sgemm_tma_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  cudaFuncSetAttribute(sgemm_tma_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  cudaFuncSetAttribute(sgemm_tma_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  done[c->device & 63] = true;
+}
+
 template <bool AK, bool BK>
 gbblas_status launch_cfg(DeviceCtx* c, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t N,
                          int64_t K, float* C, int64_t rsc, int64_t csc, int* err, cudaStream_t stream, int max_ctas) {
-  static bool attr_set[64] = {false};
-  if (!attr_set[c->device & 63]) {
-    cudaFuncSetAttribute(sgemm_tma_kernel<AK, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
-    attr_set[c->device & 63] = true;
-  }
+  set_attributes(c);
   const int tiles_m = (int)((M + kBM - 1) / kBM), tiles_n = (int)((N + kBN - 1) / kBN);
   int64_t grid = std::min<int64_t>((int64_t)tiles_m * tiles_n, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
@@ -289,6 +301,8 @@ gbblas_status launch_cfg(DeviceCtx* c, const CUtensorMap& ma, const CUtensorMap&
 }
 
 }  // namespace
+
+void sgemm_tma_prepare(DeviceCtx* c) { set_attributes(c); }
 
 bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa, const float* B,
                         int64_t rsb, int64_t csb) {

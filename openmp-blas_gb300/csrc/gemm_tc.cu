@@ -1149,6 +1149,7 @@ size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
 }
 
 void tc_prepare(DeviceCtx* c) {
+  sgemm_tma_prepare(c);
   kernel_setup<2, false>(c);
   kernel_setup<3, false>(c);
   kernel_setup<kModeFp8, false>(c);
