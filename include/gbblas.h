@@ -101,6 +101,13 @@ uint64_t gbblas_kernel_launches(void);
  * do this check themselves. */
 gbblas_status gbblas_check_stream(void* stream);
 
+/* Failure-detection self-test: one kernel on `stream` waits, bounded by
+ * limit_us microseconds (1 .. 2,000,000), on a device barrier that nothing
+ * completes, gives up and records GBBLAS_STATUS_TIMEOUT the way the
+ * tensor-core kernels do.  The next gbblas_check_stream(stream) reports it;
+ * the context stays usable.  Returns the launch status. */
+gbblas_status gbblas_selftest_bounded_wait(int64_t limit_us, void* stream);
+
 /* Release cached device and pinned-host memory held by the library for the
  * current device.  Safe to call at any time no call is in flight. */
 gbblas_status gbblas_release_cache(void);

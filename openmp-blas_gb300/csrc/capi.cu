@@ -7,6 +7,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "tc_ptx.cuh"
 
 namespace gbblas {
 
@@ -498,6 +499,20 @@ gbblas_status ew_host(gbblas_ew_op op, int64_t n, const T* a, const T* b, T* out
   return GBBLAS_STATUS_SUCCESS;
 }
 
+// Waits on a barrier nothing arrives on, bounded by limit_ns, and records
+// GBBLAS_STATUS_TIMEOUT in the stream's error word when the wait gives up.
+__global__ void selftest_wait_kernel(uint64_t limit_ns, int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int never = 0;
+    if (!tc::mbar_wait_bounded(&bar, 0, &never, limit_ns)) atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
+  }
+}
 }  // namespace
 }  // namespace gbblas
 
@@ -534,6 +549,19 @@ gbblas_status gbblas_check_stream(void* stream) {
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
   return check_stream_errors(c, as_stream(stream));
+}
+
+
+gbblas_status gbblas_selftest_bounded_wait(int64_t limit_us, void* stream) {
+  if (limit_us < 1 || limit_us > 2000000) return bad(GBBLAS_STATUS_INVALID_VALUE, "selftest: limit out of range");
+  DeviceCtx* c;
+  GB_TRY(get_ctx(&c));
+  cudaStream_t s = as_stream(stream);
+  void* scratch = nullptr;
+  GB_TRY(get_scratch(c, s, kScratchZeroBytes, &scratch));
+  int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) + kErrWordOffset);
+  selftest_wait_kernel<<<1, 32, 0, s>>>((uint64_t)limit_us * 1000ull, err);
+  return check_launch("selftest_wait_kernel");
 }
 
 gbblas_status gbblas_release_cache(void) {

@@ -42,6 +42,7 @@ SIGNATURES = {
     "gbblas_init": (_int, []),
     "gbblas_kernel_launches": (ctypes.c_uint64, []),
     "gbblas_check_stream": (_int, [_vp]),
+    "gbblas_selftest_bounded_wait": (_int, [ctypes.c_int64, _vp]),
     "gbblas_release_cache": (_int, []),
     "gbblas_sgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _vp]),
     "gbblas_dgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp]),

@@ -61,6 +61,8 @@ def test_status_strings():
     ("gbblas_sew", (4, 8, 16, 16, 16, None)),
     ("gbblas_dew", (0, -8, 16, 16, 16, None)),
     ("gbblas_sew_host", (1, 8, None, 16, 16)),
+    ("gbblas_selftest_bounded_wait", (0, None)),
+    ("gbblas_selftest_bounded_wait", (2000001, None)),
 ])
 def test_invalid_arguments_rejected_without_device(fn, args):
     assert gbblas.status_of(fn, *args) == 1  # GBBLAS_STATUS_INVALID_VALUE
