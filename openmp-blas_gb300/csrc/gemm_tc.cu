@@ -37,7 +37,7 @@
 //      itself (UE8M0 scales copied from the stage into TMEM by tcgen05.cp
 //      ahead of each slice's MMAs); chunks of 512 K as for the split.
 //
-// Warp roles (192 threads):
+// Warp roles (320 threads; FP8: 192):
 //   warp 0      tile scheduler + TMA producer: takes the next tile from the
 //               global counter, publishes it in a shared-memory tile ring,
 //               then streams its K slices (128 bytes of K of all P pieces of
@@ -47,9 +47,10 @@
 //   warp 1      allocates TMEM and issues the MMAs (one elected lane);
 //               tcgen05.commit frees a stage once its MMAs have read it and
 //               signals a TMEM chunk buffer as full;
-//   warps 2-5   epilogue: tcgen05.ld each finished chunk (warp w reads TMEM
-//               lanes 32*(w%4)..+31 = tile rows) into FP32 registers,
-//               release the buffer, add the registers into C.
+//   warps 2-9   epilogue: tcgen05.ld each finished chunk (warp w reads TMEM
+//   (FP8: 2-5)  lanes 32*(w%4)..+31 = tile rows; with 8 warps, warps 2-5
+//               take the first 64 columns, 6-9 the other 64) into FP32
+//               registers, release the buffer, add the registers into C.
 // Every mbarrier wait is bounded (2 s by %globaltimer); a wait that gives up
 // records GBBLAS_STATUS_TIMEOUT in the stream's error word, the CTA drains
 // its in-flight copies (bounded again), lets its MMAs finish, frees TMEM and
@@ -81,7 +82,7 @@ using namespace tc;
 
 constexpr int kBM = 128;
 constexpr int kBN = 128;
-constexpr int kBK = 64;  // 64 bf16 = one 128-byte swizzle row
+constexpr int kBK = 64;  // K padding of the BF16 arenas: 64 bf16 = one 128-byte row
 // K slices folded into FP32 registers per chunk: three-product split every
 // 512 of K, six-product split every 128 (the tensor core's accumulation over
 // a 512-K chunk made the six-product result's max relative error worse than
@@ -103,15 +104,22 @@ template <int MODE>
 struct ModeTraits {
   static constexpr bool fp8 = MODE == kModeFp8;
   static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
-  // 128-byte K sub-tiles per stage: one for the split (64 BF16 of every
-  // piece), two for FP8 (256 E4M3: twice the MMAs per barrier round trip,
-  // the per-stage hand-offs being what bounds the four-MMA FP8 stage).
+  // Bytes of K per operand row in one K sub-tile (128-byte swizzle).  The
+  // six-product split measured slower with 64-byte rows (32-K stages, 4 in
+  // shared memory instead of 2): 245 vs 269 TFLOP/s at 8192^3.
+  static constexpr int kRowBytes = 128;
+  static constexpr int kKSteps = kRowBytes / 32;  // MMAs of 32 bytes of K per sub-tile
+  // K sub-tiles per stage: one for the split, two for FP8 (256 E4M3: twice
+  // the MMAs per barrier round trip, the per-stage hand-offs being what
+  // bounds the four-MMA FP8 stage).
   static constexpr int kSub = fp8 ? 2 : 1;
-  static constexpr int kBKe = fp8 ? 128 * kSub : kBK;  // K elements per stage
+  static constexpr int kBKe = fp8 ? 128 * kSub : kRowBytes / 2;  // K elements per stage
   static constexpr int kChunk = fp8 ? kChunkTilesFp8 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
-  // Epilogue warps: 4, each 32 tile rows x 128 columns.
-  static constexpr int kEpiWarps = 4;
-  static constexpr int kCols = kBN;  // tile columns per epilogue thread
+  // Epilogue warps: 8 for the split, each 32 tile rows x 64 columns (with
+  // 128 FP32 accumulators per thread the kernel ran out of registers and
+  // spilled); 4 for FP8, each 32 rows x 128 columns (no spills).
+  static constexpr int kEpiWarps = fp8 ? 4 : 8;
+  static constexpr int kCols = kBN * 4 / kEpiWarps;  // tile columns per epilogue thread
   static constexpr int kThreads = 64 + 32 * kEpiWarps;
   // TMEM: two chunk buffers (the MMAs may run one chunk ahead of the
   // epilogue), main + correction accumulators for the split (2 x 256
@@ -125,8 +133,9 @@ struct ModeTraits {
 template <int MODE, bool PAIR>
 struct TcCfg {
   static constexpr int P = ModeTraits<MODE>::P;
-  static constexpr uint32_t kABytes = kBM * 128;  // one 128-byte-wide operand tile of A (this CTA's rows)
-  static constexpr uint32_t kBBytes = (PAIR ? kBN / 2 : kBN) * 128;  // B^T rows this CTA stages
+  static constexpr uint32_t kRow = ModeTraits<MODE>::kRowBytes;
+  static constexpr uint32_t kABytes = kBM * kRow;  // one K sub-tile of A (this CTA's rows)
+  static constexpr uint32_t kBBytes = (PAIR ? kBN / 2 : kBN) * kRow;  // B^T rows this CTA stages
   static constexpr int kSub = ModeTraits<MODE>::kSub;
   // FP8: the stage's scale atoms (512 bytes per 128-K block) of A, then of B
   static constexpr uint32_t kSfBytes = ModeTraits<MODE>::fp8 ? 2 * 512 * kSub : 0;
@@ -145,7 +154,7 @@ struct TcCfg {
   static_assert(kStages >= 2, "need at least a double-buffered stage ring");
   static_assert(kSmem <= kSmemLimit, "exceeds the 227 KB per-CTA shared memory limit");
   static_assert(kStageBytes % 1024 == 0 && kABytes % 1024 == 0 && kBBytes % 1024 == 0,
-                "operand tiles must stay 1024-byte aligned for the 128-byte swizzle");
+                "operand tiles must stay 1024-byte aligned for the 128- / 64-byte swizzle");
   static_assert(kTmemCols <= 512, "TMEM has 512 columns");
 };
 
@@ -580,9 +589,9 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
               mma_f16(d, sw128_kmajor_desc(ad), sw128_kmajor_desc(bd), idesc, accumulate);
           };
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            // 32 bytes along K per MMA inside the swizzled 128-byte row:
-            // 16 bf16 (kind::f16) or 32 e4m3 (kind::mxf8f6f4)
+          for (int kk = 0; kk < MT::kKSteps; ++kk) {
+            // 32 bytes along K per MMA inside the swizzled 128- / 64-byte
+            // row: 16 bf16 (kind::f16) or 32 e4m3 (kind::mxf8f6f4)
             const uint32_t off = kk * 32;
             const uint32_t acc = (chunk_first && kk == 0) ? 0u : 1u;
             if constexpr (MT::fp8) {
@@ -701,31 +710,30 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         const bool vec =
             (pr.csc == 1) && ((pr.rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(pr.C) & 15) == 0);
         const int cn = n0 + col0;
-        if (pr.overwrite) {  // split-K partial: dense, 16-byte-aligned rows
-          if (cn + kCols <= pr.N) {
-#pragma unroll
-            for (int j = 0; j < kCols; j += 4)
-              *reinterpret_cast<float4*>(crow + cn + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < kCols; ++j)
-              if (cn + j < pr.N) crow[cn + j] = acc[j];
-          }
-        } else if (vec && cn + kCols <= pr.N) {
+        // C += acc; a split-K partial (overwrite) is stored instead, into
+        // dense 16-byte-aligned rows
+        const bool add = !pr.overwrite;
+        if (vec && cn + kCols <= pr.N) {
 #pragma unroll
           for (int j = 0; j < kCols; j += 4) {
             float4* p = reinterpret_cast<float4*>(crow + cn + j);
-            float4 cv = *p;
-            cv.x += acc[j];
-            cv.y += acc[j + 1];
-            cv.z += acc[j + 2];
-            cv.w += acc[j + 3];
+            float4 cv = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+            if (add) {
+              const float4 old = *p;
+              cv.x = old.x + cv.x;
+              cv.y = old.y + cv.y;
+              cv.z = old.z + cv.z;
+              cv.w = old.w + cv.w;
+            }
             *p = cv;
           }
         } else {
 #pragma unroll
           for (int j = 0; j < kCols; ++j)
-            if (cn + j < pr.N) crow[(int64_t)(cn + j) * pr.csc] += acc[j];
+            if (cn + j < pr.N) {
+              float* q = crow + (int64_t)(cn + j) * pr.csc;
+              *q = add ? *q + acc[j] : acc[j];
+            }
         }
       }
     }
@@ -793,10 +801,10 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 3-D tensor map over `planes` planes of rows x cols (cols contiguous) BF16
-// or 8-bit elements, planes one after another; box of box_rows x 128 bytes x
-// all planes, 128-byte swizzle.
+// or 8-bit elements, planes one after another; box of box_rows x row_bytes
+// (128 or 64) x all planes, with the swizzle of that row width.
 gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint64_t planes,
-                       uint32_t box_rows, bool bytes) {
+                       uint32_t box_rows, bool bytes, uint32_t row_bytes) {
   auto fn = encode_fn();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -805,11 +813,12 @@ gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64
   const uint64_t esize = bytes ? 1 : 2;
   cuuint64_t dims[3] = {cols, rows, planes};
   cuuint64_t strides[2] = {cols * esize, rows * cols * esize};
-  cuuint32_t box[3] = {(cuuint32_t)(128 / esize), box_rows, (cuuint32_t)planes};
+  cuuint32_t box[3] = {(cuuint32_t)(row_bytes / esize), box_rows, (cuuint32_t)planes};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
                   const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                  row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d) for %llu x %llu x %llu", (int)r, (unsigned long long)planes,
               (unsigned long long)rows, (unsigned long long)cols);
@@ -874,7 +883,11 @@ struct TcGroupPlan {
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool fp8() const { return mode == kModeFp8; }
   int planes() const { return fp8() ? 1 : mode; }
-  int slice_k() const { return fp8() ? ModeTraits<kModeFp8>::kBKe : kBK; }  // K elements per stage
+  int slice_k() const {  // K elements per stage
+    return fp8() ? ModeTraits<kModeFp8>::kBKe : (mode == 3 ? ModeTraits<3>::kBKe : ModeTraits<2>::kBKe);
+  }
+  int pad_k() const { return fp8() ? ModeTraits<kModeFp8>::kBKe : kBK; }  // K padding (multiple of stage and prep tile)
+  int row_bytes() const { return mode == 3 ? ModeTraits<3>::kRowBytes : 128; }  // bytes of K per row per sub-tile
   int job_k() const { return fp8() ? 128 : 64; }     // K extent of one preparation tile (PrepTile::TK)
 };
 
@@ -893,7 +906,7 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     return GBBLAS_STATUS_INVALID_VALUE;
   }
   pl.mode = mode;
-  const int64_t sk = pl.slice_k(), jk = pl.job_k(), jr = 4096 / jk;
+  const int64_t sk = pl.slice_k(), pk = pl.pad_k(), jk = pl.job_k(), jr = 4096 / jk;
   std::vector<int64_t> order;
   order.reserve(count);
   for (int64_t i = 0; i < count; ++i) {
@@ -916,7 +929,7 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   if (want_pair && mode != kModeFp8) {
     double w1 = 0, w2 = 0;
     for (int64_t i : order) {
-      const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, sk);
+      const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, pk);
       w1 += (double)round_up(d[i].M, kBM) * nk;
       w2 += (double)round_up(d[i].M, 2 * kBM) * nk;
     }
@@ -926,13 +939,13 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   pl.njobs = (int)order.size();
   pl.ajobs.resize(pl.njobs);
   pl.bjobs.resize(pl.njobs);
-  for (int i = 0; i < pl.njobs; ++i) pl.kpad = std::max<int64_t>(pl.kpad, round_up(d[order[i]].K, sk));
+  for (int i = 0; i < pl.njobs; ++i) pl.kpad = std::max<int64_t>(pl.kpad, round_up(d[order[i]].K, pk));
   pl.pitch = pl.kpad + kPitchPadBytes / (pl.fp8() ? 1 : (int64_t)sizeof(__nv_bfloat16));
   int64_t ws = 0;  // partial workspace bytes
   for (int i = 0; i < pl.njobs; ++i) {
     const gbblas_gemm_desc& g = d[order[i]];
-    const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, sk);
-    const int num_kt = (int)(Kp / sk);
+    const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, pk);
+    const int num_kt = (int)(Kp / sk);  // pk is a multiple of sk
     const int parts = std::max(1, std::min(opt.split, num_kt));
     const int64_t ppitch = round_up(g.N, 4);  // partial rows stay 16-byte aligned
     if (parts > 1) {
@@ -1015,9 +1028,9 @@ gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
     GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_red, pl.reds.data(), sizeof(SplitReduce) * pl.reds.size(),
                                 cudaMemcpyHostToDevice, stream));
   GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)pl.a_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(), kBM,
-                  pl.fp8()));
+                  pl.fp8(), pl.row_bytes()));
   GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)pl.b_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(),
-                  pl.pair ? kBN / 2 : kBN, pl.fp8()));
+                  pl.pair ? kBN / 2 : kBN, pl.fp8(), pl.row_bytes()));
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -1130,7 +1143,9 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
 
 }  // namespace
 
-int tc_stage_k(int mode) { return mode == kModeFp8 ? ModeTraits<kModeFp8>::kBKe : kBK; }
+int tc_stage_k(int mode) {
+  return mode == kModeFp8 ? ModeTraits<kModeFp8>::kBKe : (mode == 3 ? ModeTraits<3>::kBKe : ModeTraits<2>::kBKe);
+}
 
 int tc_mode(gbblas_accuracy acc) {
   switch (acc) {
