@@ -101,3 +101,41 @@ def test_large_against_fp64(cuda, monkeypatch):
     ref = A.double() @ B.double()
     bound = 2 * 2500 * EPS32 * (A.double().abs() @ B.double().abs())
     assert bool(((C.double() - ref).abs() <= bound).all())
+
+
+@pytest.mark.parametrize("la,lb", [(1, 1), (0, 0), (1, 0), (0, 1)])
+def test_padded_pitch_takes_tma_path(cuda, monkeypatch, la, lb):
+    """K = 301 with row / column pitches padded to 304 elements (16-byte
+    multiples): the TMA-fed kernel runs; the box's K tail past 301 reads as
+    zeros.  Same bits as the register-staged kernel, oracle bound."""
+    import gbblas
+    torch = cuda
+    M, N, K, P = 130, 150, 301, 304
+    rng = np.random.default_rng(11 + la + 2 * lb)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    # padding holds NaN: any read past K (or past M, N) would show
+    if la == 1:
+        abuf = np.full((M, P), np.nan, np.float32); abuf[:, :K] = A; rsa, csa = P, 1
+    else:
+        PA = 144  # >= M = 130, multiple of 4
+        abuf = np.full((K, PA), np.nan, np.float32); abuf[:, :M] = A.T; rsa, csa = 1, PA
+    if lb == 1:
+        PB = 152  # >= N = 150
+        bbuf = np.full((K, PB), np.nan, np.float32); bbuf[:, :N] = B; rsb, csb = PB, 1
+    else:
+        bbuf = np.full((N, P), np.nan, np.float32); bbuf[:, :K] = B.T; rsb, csb = 1, P
+    tA, tB = torch.from_numpy(abuf).cuda(), torch.from_numpy(bbuf).cuda()
+    outs = []
+    for tile in (2, 0):
+        monkeypatch.setenv("GBBLAS_FMA_TILE", str(tile))
+        tC = torch.from_numpy(C0.copy()).cuda()
+        gbblas.call("gbblas_sgemm", M, N, K, tA.data_ptr(), rsa, csa, tB.data_ptr(), rsb, csb, tC.data_ptr(), N, 1,
+                    0, None)
+        gbblas.call("gbblas_check_stream", None)
+        outs.append(tC.cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+    exact = A.astype(np.float64) @ B.astype(np.float64) + C0
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
+    assert np.all(np.abs(outs[0] - exact) <= 2 * K * EPS32 * scale)
