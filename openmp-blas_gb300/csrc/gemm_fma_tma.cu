@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         const float* As = reinterpret_cast<const float*>(a_tile(s));
         const float* Bs = reinterpret_cast<const float*>(b_tile(s));
-#pragma unroll 2
+#pragma unroll
         for (int kq = 0; kq < kBK / 4; ++kq) {
           float a[8][4], b[8][4];
           load_frag<A_KMAJ>(As, ty, kq, a);
