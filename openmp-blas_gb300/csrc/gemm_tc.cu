@@ -120,7 +120,12 @@ struct ModeTraits {
   // spilled); 4 for FP8, each 32 rows x 128 columns (no spills).
   static constexpr int kEpiWarps = fp8 ? 4 : 8;
   static constexpr int kCols = kBN * 4 / kEpiWarps;  // tile columns per epilogue thread
-  static constexpr int kThreads = 64 + 32 * kEpiWarps;
+  // Single CTAs load B with a second producer warp (after the epilogue
+  // warps): one thread issuing every copy caps what TMA delivers into the
+  // SM (measured 43-46 B/cycle for 64 KB stages from one issuing thread,
+  // 66-68 from two).  CTA pairs keep one producer; the warp then idles.
+  static constexpr int kBProdWarp = 2 + kEpiWarps;
+  static constexpr int kThreads = 64 + 32 * kEpiWarps + 32;
   // TMEM: two chunk buffers (the MMAs may run one chunk ahead of the
   // epilogue), main + correction accumulators for the split (2 x 256
   // columns), one accumulator for FP8 (2 x 128 columns, then one 8-column
@@ -140,6 +145,9 @@ struct TcCfg {
   // FP8: the stage's scale atoms (512 bytes per 128-K block) of A, then of B
   static constexpr uint32_t kSfBytes = ModeTraits<MODE>::fp8 ? 2 * 512 * kSub : 0;
   static constexpr uint32_t kStageBytes = P * kSub * (kABytes + kBBytes) + kSfBytes;
+  // what each producer of a single CTA brings per stage (A part, B part)
+  static constexpr uint32_t kAStageBytes = P * kSub * kABytes + kSfBytes / 2;
+  static constexpr uint32_t kBStageBytes = P * kSub * kBBytes + kSfBytes / 2;
   static constexpr uint32_t kTmemCols = 512;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
   static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
@@ -413,7 +421,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < ST; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&full[s], PAIR ? 1 : 2);  // single CTAs: the A and the B producer
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < MT::kBufs; ++b) {
@@ -422,7 +430,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     }
     for (int r = 0; r < kTileRing; ++r) {
       mbar_init(&ring_full[r], 1);
-      mbar_init(&ring_empty[r], 1 + MT::kEpiWarps);  // MMA lane + the epilogue warps
+      mbar_init(&ring_empty[r], 1 + MT::kEpiWarps + (PAIR ? 0 : 1));  // MMA lane, epilogue warps, B producer
     }
     mbar_init(accf, 1);
     *abort_flag = 0;
@@ -493,26 +501,62 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
               tma_load_3d_pair(b_tile(s, 0), &tm_b, fb, kx, pr.b_row + n0 + kBN / 2, 0);
             }
           } else {
-            mbar_arrive_expect_tx(&full[s], CF::kStageBytes);
+            // A's part of the stage; the B producer warp brings the rest
+            mbar_arrive_expect_tx(&full[s], CF::kAStageBytes);
             if constexpr (MT::fp8) {
 #pragma unroll
-              for (int u = 0; u < MT::kSub; ++u) {
+              for (int u = 0; u < MT::kSub; ++u)
                 tma_load_3d(a_tile(s, u), &tm_a, &full[s], kx + u * 128, pr.a_row + own_m0, 0);
-                tma_load_3d(b_tile(s, u), &tm_b, &full[s], kx + u * 128, pr.b_row + n0, 0);
-              }
-              // the stage's K-blocks' scale atoms of these 128 rows of A and
-              // of B^T: consecutive in the scale arrays (one run each)
+              // the stage's K-blocks' scale atoms of these 128 rows of A:
+              // consecutive in the scale array (one run)
               const int64_t kb0 = kx;  // 128 words per K-block of 128 = one word per K element
               bulk_load(sf_atom(s, 0), sa + (int64_t)((pr.a_row + own_m0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
                         &full[s]);
-              bulk_load(sf_atom(s, 1), sb + (int64_t)((pr.b_row + n0) >> 7) * sf_stride + kb0, 512 * MT::kSub,
-                        &full[s]);
             } else {
               tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kx, pr.a_row + own_m0, 0);
-              tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kx, pr.b_row + n0, 0);
             }
           }
           ++issued;
+        }
+      }
+    }
+  } else if (warp == MT::kBProdWarp) {
+    // B producer (single CTAs): follows the tile ring and loads B^T's part
+    // of every stage into the same ring slots as the A producer.
+    if (lane == 0 && !PAIR) {
+      int bissued = 0;
+      bool stop = false;
+      for (int it = 0; !stop; ++it) {
+        const int slot = it % kTileRing, use = it / kTileRing;
+        if (!mbar_wait_bounded(&ring_full[slot], use & 1, abort_flag, kWaitLimitNs)) {
+          fail();
+          break;
+        }
+        const int t = ring[slot];
+        mbar_arrive(&ring_empty[slot]);
+        if (t < 0) break;
+        const TcProblem& pr = probs[find_problem(probs, nprob, t)];
+        int m0, n0;
+        tile_coords<BMT>(pr, t, m0, n0);
+        for (int kt = 0; kt < pr.num_kt; ++kt) {
+          const int s = bissued % ST, round = bissued / ST;
+          if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
+            fail();
+            stop = true;
+            break;
+          }
+          const int kx = (pr.kt0 + kt) * MT::kBKe;
+          mbar_arrive_expect_tx(&full[s], CF::kBStageBytes);
+          if constexpr (MT::fp8) {
+#pragma unroll
+            for (int u = 0; u < MT::kSub; ++u)
+              tma_load_3d(b_tile(s, u), &tm_b, &full[s], kx + u * 128, pr.b_row + n0, 0);
+            bulk_load(sf_atom(s, 1), sb + (int64_t)((pr.b_row + n0) >> 7) * sf_stride + (int64_t)kx, 512 * MT::kSub,
+                      &full[s]);
+          } else {
+            tma_load_3d(b_tile(s, 0), &tm_b, &full[s], kx, pr.b_row + n0, 0);
+          }
+          ++bissued;
         }
       }
     }
