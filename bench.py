@@ -27,6 +27,11 @@ calls) per second, whole job.
 workload instead (the compiled reference where it exists, otherwise the
 oracle port) and prints the same line with "impl": "reference".
 
+Other workloads (`--workload`, one JSON line per result): precision (the
+8192^3 GEMM paths and their errors against FP64), batching, serving,
+stream_ops, sweep (the reference's size sweeps in its metric formats) and mtm
+(the plain 1024^3 single-precision mtm against the FMA-pipe peak).
+
 Multi-GPU: the path does not shard; `--gpus N` under torchrun runs N
 independent replicas (weak scaling), max time over ranks.
 """
@@ -989,6 +994,101 @@ def run_stream_ops(args):
         torch.cuda.empty_cache()
 
 
+def run_mtm(args):
+    """The plain single-precision mtm configuration: C = A*B, M = N = K = 1024,
+    row-major float32, A then B U[-1,1) from seed 0, C zeroed; FP32 on the FMA
+    pipes (the default accuracy).  TFLOP/s with 2*M*N*K flops (and the
+    reference's M*N*(2K-1) count beside it), CUDA events over 20 calls after 3
+    warm-ups, against the FMA-pipe peak; max normwise / relative error against
+    FP64 and against the reference's own mtm (the oracle's compiled reference
+    where it exists here, else its restatement); the same call from host
+    buffers (gbblas_sgemm_host) for e2e; the CPU baseline is the reference
+    algorithm on all host cores, mean of 10 after 2 warm-ups."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    n = 1024
+    rng = np.random.default_rng(0)
+    A = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    B = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    tA, tB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    tC = torch.zeros(n, n, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream or None
+
+    def call():
+        gbblas.call("gbblas_sgemm", n, n, n, tA.data_ptr(), n, 1, tB.data_ptr(), n, 1, tC.data_ptr(), n, 1, 0, sp)
+    for _ in range(max(3, args.warmup)):
+        call()
+    torch.cuda.synchronize()
+    iters = 20
+    launches0 = gbblas.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        t0 = time.time()
+        e0.record()
+        for _ in range(iters):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        clk.mark(t0, time.time())
+    launches = gbblas.kernel_launches() - launches0
+    gbblas.call("gbblas_check_stream", sp)
+    ms = e0.elapsed_time(e1) / iters
+    tC.zero_()
+    call()
+    got = tC.cpu().numpy().astype(np.float64)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    absx = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    ref_kind = "reference" if O.ref_available() else "port"
+    ref = (O.ref_gemm(A, B, np.zeros((n, n), np.float32), 1, 1, 1) if ref_kind == "reference"
+           else O.gemm(A, B, np.zeros((n, n), np.float32), 1, 1, 1)).astype(np.float64)
+    tf = 2.0 * n ** 3 / (ms / 1e3) / 1e12
+    peak = fma_peak_tflops(clk.summary())
+    # e2e: host buffers through the drop-in's C call (copies in and out inside the call)
+    Ch = np.zeros((n, n), np.float32)
+    for _ in range(2):
+        gbblas.call("gbblas_sgemm_host", n, n, n, A.ctypes.data, n, 1, B.ctypes.data, n, 1, Ch.ctypes.data, n, 1, 0)
+    reps = 10
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        gbblas.call("gbblas_sgemm_host", n, n, n, A.ctypes.data, n, 1, B.ctypes.data, n, 1, Ch.ctypes.data, n, 1, 0)
+    e2e_s = (time.perf_counter() - t0) / reps
+    line = {"metric": "plain mtm TFLOP/s (float32, FMA pipes)", "value": round(tf, 3), "unit": "TFLOP/s",
+            "n_gpus": 1, "steps": iters, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "mtm C = A*B, M = N = K = 1024, row-major float32, U[-1,1) seed 0 (A then B)",
+                       "flops": "2*M*N*K", "l2": "operands fit in L2 (12 MB); repeated calls"},
+            "reference_gflops_count": round(n * n * (2 * n - 1) / (ms / 1e3) / 1e9, 1),
+            "roofline": {"bound": "fma", "achieved": round(tf, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
+                         "frac": round(tf / peak, 4),
+                         "peak_source": "SMs x 128 FP32 FMA lanes x 2 flop x max SM clock (nominal)"},
+            "max_normwise_err_vs_fp64": float(np.max(np.abs(got - exact) / absx)),
+            "max_rel_err_vs_fp64": float(np.max(np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300))),
+            "max_normwise_diff_vs_reference": float(np.max(np.abs(got - ref) / absx)),
+            "reference_kind": ref_kind,
+            "e2e": {"value": round(2.0 * n ** 3 / e2e_s / 1e12, 3), "unit": "TFLOP/s",
+                    "h2d_bytes_per_step": 3 * n * n * 4, "d2h_bytes_per_step": n * n * 4,
+                    "api": "gbblas_sgemm_host (host buffers)"},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if not args.no_cpu:
+        O.set_threads(os.cpu_count() or 1)
+        fn = O.ref_gemm if ref_kind == "reference" else O.gemm
+        Z = np.zeros((n, n), np.float32)
+        for _ in range(2):
+            fn(A, B, Z, 1, 1, 1)
+        t0 = time.perf_counter()
+        for _ in range(10):
+            fn(A, B, Z, 1, 1, 1)
+        cpu_s = (time.perf_counter() - t0) / 10
+        line["cpu_baseline"] = {"value": round(2.0 * n ** 3 / cpu_s / 1e12, 4), "unit": "TFLOP/s",
+                                "cores": os.cpu_count(), "kind": ref_kind,
+                                "sample": f"the full 1024^3 mtm, mean of 10 after 2 warm-ups ({cpu_s * 1e3:.1f} ms)"}
+    print(json.dumps(line), flush=True)
+
+
 def run_sweep(args):
     """The reference's benchmark drivers (src/mtm.cpp:355-372, src/mtv.cpp:326-345,
     src/dot.cpp:198-205) on the GPU: the same size sweeps, ones-filled
@@ -1102,7 +1202,7 @@ def run_sweep(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="bandwidth",
-                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops", "sweep"])
+                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops", "sweep", "mtm"])
     ap.add_argument("--sweep-op", default="mtm", choices=["mtm", "mtv", "dot"])
     ap.add_argument("--sweep-cpu-max", type=int, default=1024,
                     help="sweep workload: largest size the CPU series runs (0 beyond)")
@@ -1150,6 +1250,8 @@ def main():
         run_stream_ops(args)
     elif args.workload == "sweep":
         run_sweep(args)
+    elif args.workload == "mtm":
+        run_mtm(args)
     else:
         run_gpu(args)
 
