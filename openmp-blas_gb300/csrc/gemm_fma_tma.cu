@@ -23,7 +23,11 @@
 //
 // Persistent: grid = min(tiles, SMs or the caller's cap), tiles in grouped
 // raster order (8 tile rows per band) for L2 reuse; the ring carries over
-// from tile to tile.  Roofline: the FMA pipes, 2*M*N*K flops.
+// from tile to tile.  Split-K (parts > 1, for shapes whose tiles leave SMs
+// idle): each unit = (tile, K part) adds its K range into a zeroed partial,
+// then the partials are added into C in part order - within the same bound,
+// not the same bits as the unsplit kernels.  Roofline: the FMA pipes,
+// 2*M*N*K flops.
 #include <cuda.h>
 
 #include <mutex>
@@ -106,7 +110,7 @@ template <bool A_KMAJ, bool B_KMAJ>
 __global__ void __launch_bounds__(kThreads, 1)
     sgemm_tma_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b, int M, int N,
                      int K, float* __restrict__ C, int64_t rsc, int64_t csc, int tiles_m, int tiles_n,
-                     int* __restrict__ err) {
+                     int parts, float* __restrict__ part_buf, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -133,17 +137,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     *abort_flag = 1;
     atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
   };
-  const int ntiles = tiles_m * tiles_n;
+  // work unit u = (tile u / parts, K part u % parts); parts > 1 (split-K):
+  // each unit adds its K range into its own zeroed M x N partial
+  const int nunits = tiles_m * tiles_n * parts;
   const int nk = (K + kBK - 1) / kBK;
   int issued = 0;
 
   if (warp == kComputeWarps) {
     if (lane == 0) {
       bool stop = false;
-      for (int t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+      for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x) {
+        const int t = u / parts, pp = u % parts;
         int m0, n0;
         tile_origin(t, tiles_m, tiles_n, m0, n0);
-        for (int kt = 0; kt < nk; ++kt) {
+        const int kb = (int)((int64_t)nk * pp / parts), ke = (int)((int64_t)nk * (pp + 1) / parts);
+        for (int kt = kb; kt < ke; ++kt) {
           const int s = issued % kStages, round = issued / kStages;
           if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
             fail();
@@ -167,15 +175,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
     int consumed = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+      const int t = u / parts, pp = u % parts;
       int m0, n0;
       tile_origin(t, tiles_m, tiles_n, m0, n0);
+      const int kb = (int)((int64_t)nk * pp / parts), ke = (int)((int64_t)nk * (pp + 1) / parts);
       float acc[8][8];
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-      for (int kt = 0; kt < nk; ++kt, ++consumed) {
+      for (int kt = kb; kt < ke; ++kt, ++consumed) {
         const int s = consumed % kStages, round = consumed / kStages;
         // warp-uniform decision: every lane leaves the loop together
         if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[s], round & 1, abort_flag, kWaitLimitNs))) {
@@ -228,15 +238,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&empty[s]);
       }
       if (!ok) break;
-      // C += acc (rows / columns outside the matrix dropped)
+      // C += acc (rows / columns outside the matrix dropped); split-K: into
+      // this part's dense partial
+      float* Ct = parts > 1 ? part_buf + (int64_t)pp * M * N : C;
+      const int64_t rs = parts > 1 ? (int64_t)N : rsc, cs = parts > 1 ? 1 : csc;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int m = m0 + owned<A_KMAJ>(ty, i);
         if (m >= M) continue;
-        float* crow = C + (int64_t)m * rsc;
+        float* crow = Ct + (int64_t)m * rs;
         if constexpr (!B_KMAJ) {
           // columns tx*4 + {0..3} and 64 + tx*4 + {0..3}: two float4 when C rows are contiguous
-          const bool vec = csc == 1 && ((rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+          const bool vec = cs == 1 && ((rs & 3) == 0) && ((reinterpret_cast<uintptr_t>(Ct) & 15) == 0);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const int n = n0 + tx * 4 + 64 * h;
@@ -251,14 +264,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             } else {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
-                if (n + q < N) crow[(int64_t)(n + q) * csc] += acc[i][4 * h + q];
+                if (n + q < N) crow[(int64_t)(n + q) * cs] += acc[i][4 * h + q];
             }
           }
         } else {
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int n = n0 + owned<true>(tx, j);
-            if (n < N) crow[(int64_t)n * csc] += acc[i][j];
+            if (n < N) crow[(int64_t)n * cs] += acc[i][j];
           }
         }
       }
@@ -271,6 +284,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int from = issued > kStages ? issued - kStages : 0;
     for (int k = from; k < issued; ++k)
       (void)mbar_wait_bounded(&full[k % kStages], (k / kStages) & 1, &never, kWaitLimitNs / 2);
+  }
+}
+
+// Split-K: C += part[0] + part[1] + ... (parts in order), grid-stride.
+__global__ void __launch_bounds__(256) sgemm_parts_reduce_kernel(float* __restrict__ C, int64_t rsc, int64_t csc,
+                                                                 const float* __restrict__ part, int M, int N,
+                                                                 int parts) {
+  const int64_t total = (int64_t)M * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    float s = part[e];
+    for (int p = 1; p < parts; ++p) s += part[(int64_t)p * total + e];
+    const int64_t r = e / N, c = e % N;
+    C[r * rsc + c * csc] += s;
   }
 }
 
@@ -290,13 +316,14 @@ void set_attributes(DeviceCtx* c) {
 
 template <bool AK, bool BK>
 gbblas_status launch_cfg(DeviceCtx* c, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t N,
-                         int64_t K, float* C, int64_t rsc, int64_t csc, int* err, cudaStream_t stream, int max_ctas) {
+                         int64_t K, float* C, int64_t rsc, int64_t csc, int* err, cudaStream_t stream, int max_ctas,
+                         int parts, float* part_buf) {
   set_attributes(c);
   const int tiles_m = (int)((M + kBM - 1) / kBM), tiles_n = (int)((N + kBN - 1) / kBN);
-  int64_t grid = std::min<int64_t>((int64_t)tiles_m * tiles_n, c->num_sms);
+  int64_t grid = std::min<int64_t>((int64_t)tiles_m * tiles_n * parts, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
   sgemm_tma_kernel<AK, BK><<<(unsigned)grid, kThreads, kSmem, stream>>>(ma, mb, (int)M, (int)N, (int)K, C, rsc, csc,
-                                                                      tiles_m, tiles_n, err);
+                                                                      tiles_m, tiles_n, parts, part_buf, err);
   return check_launch("sgemm_tma_kernel");
 }
 
@@ -316,7 +343,7 @@ bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t
 
 gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                                int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
-                               int64_t csc, cudaStream_t stream, int max_ctas) {
+                               int64_t csc, cudaStream_t stream, int max_ctas, int parts) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if (!sgemm_tma_eligible(M, N, K, A, rsa, csa, B, rsb, csb)) {
     set_error("TMA-fed sgemm: operands not 16-byte aligned with 16-byte-multiple strides");
@@ -333,13 +360,36 @@ gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, co
     GB_TRY(make_map_f32_2d(&mb, B, (uint64_t)K, (uint64_t)N, (uint64_t)csb, kBK, kBN, true));
   else
     GB_TRY(make_map_f32_2d(&mb, B, (uint64_t)N, (uint64_t)K, (uint64_t)rsb, kBN, kBK, false));
+  const int nk = (int)((K + kBK - 1) / kBK);
+  if (parts < 1) parts = 1;
+  if (parts > nk) parts = nk;
+  const size_t part_bytes = parts > 1 ? sizeof(float) * (size_t)parts * (size_t)M * (size_t)N : 0;
   void* s = nullptr;
-  GB_TRY(get_scratch(c, stream, kScratchZeroBytes, &s));
+  GB_TRY(get_scratch(c, stream, kScratchZeroBytes + part_bytes, &s));
   int* err = reinterpret_cast<int*>(static_cast<char*>(s) + kErrWordOffset);
-  if (ak && bk) return launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas);
-  if (ak) return launch_cfg<true, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas);
-  if (bk) return launch_cfg<false, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas);
-  return launch_cfg<false, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas);
+  float* part_buf = parts > 1 ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
+  if (parts > 1) GB_CUDA_TRY(cudaMemsetAsync(part_buf, 0, part_bytes, stream));
+  gbblas_status st;
+  if (ak && bk)
+    st = launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
+  else if (ak)
+    st = launch_cfg<true, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
+  else if (bk)
+    st = launch_cfg<false, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
+  else
+    st = launch_cfg<false, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
+  if (st != GBBLAS_STATUS_SUCCESS || parts == 1) return st;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M * N + 255) / 256, 4 * (int64_t)c->num_sms));
+  sgemm_parts_reduce_kernel<<<blocks, 256, 0, stream>>>(C, rsc, csc, part_buf, (int)M, (int)N, parts);
+  return check_launch("sgemm_parts_reduce_kernel");
+}
+
+int sgemm_tma_split_parts(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN);
+  const int64_t nk = (K + kBK - 1) / kBK;
+  for (int p = 4; p >= 2; --p)
+    if (tiles * p <= (int64_t)c->num_sms && nk >= 8 * p) return p;
+  return 1;
 }
 
 }  // namespace gbblas

@@ -25,8 +25,9 @@
 //                    form (single CTAs or CTA pairs, split-BF16 only);
 //                    GBBLAS_TC_SPLITK=n forces n parts;
 //   gemm_fma_tile    FP32 FMA kernel and CTA tile per bucket: 64 x 64 or
-//                    128 x 128 register-staged, or the TMA-fed 128 x 128;
-//                    GBBLAS_FMA_TILE=0 / 1 / 2 forces one.
+//                    128 x 128 register-staged, the TMA-fed 128 x 128, or
+//                    that with split-K where its tiles leave SMs idle;
+//                    GBBLAS_FMA_TILE=0 / 1 / 2 / 3 forces one.
 // Nothing is timed while the caller's stream is being captured into a graph
 // (the defaults apply); single-call paths consult the tuner, grouped,
 // batched and served launches use the defaults.
@@ -368,7 +369,7 @@ TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t
 }
 
 int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t stream) {
-  if (const char* e = std::getenv("GBBLAS_FMA_TILE"); e && e[0] >= '0' && e[0] <= '2') return e[0] - '0';
+  if (const char* e = std::getenv("GBBLAS_FMA_TILE"); e && e[0] >= '0' && e[0] <= '3') return e[0] - '0';
   Tuner& t = Tuner::get();
   const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
   const std::string key = "gemm_fma_tile|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
@@ -381,11 +382,13 @@ int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t s
   GemmBench b(c, m, n, k);
   if (!b.ok()) return -1;
   const gbblas_gemm_desc d = b.desc();
-  // 0 = 64 x 64, 1 = 128 x 128 (register-staged), 2 = TMA-fed 128 x 128 (its
-  // eligibility is the caller's operands': an ineligible call falls back)
+  // 0 = 64 x 64, 1 = 128 x 128 (register-staged), 2 = TMA-fed 128 x 128,
+  // 3 = TMA-fed with split-K, offered where the tiles leave SMs idle (the TMA
+  // kernels' eligibility is the caller's operands': an ineligible call falls back)
+  const int ntile = sgemm_tma_split_parts(c, m, n, k) > 1 ? 4 : 3;
   int best = -1;
   float best_ms = 1e30f;
-  for (int tile = 0; tile < 3; ++tile) {
+  for (int tile = 0; tile < ntile; ++tile) {
     const float ms = b.time([&](cudaStream_t s) {
       return launch_gemm_fma<float>(c, d.M, d.N, d.K, d.A, d.rsa, d.csa, d.B, d.rsb, d.csb, d.C, d.rsc, d.csc, s, 0,
                                     tile);

@@ -139,3 +139,22 @@ def test_padded_pitch_takes_tma_path(cuda, monkeypatch, la, lb):
     exact = A.astype(np.float64) @ B.astype(np.float64) + C0
     scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
     assert np.all(np.abs(outs[0] - exact) <= 2 * K * EPS32 * scale)
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024, 1024), (300, 200, 4000), (129, 257, 65), (700, 130, 3000)])
+@pytest.mark.parametrize("la,lb,lc", [(1, 1, 1), (0, 1, 1), (1, 0, 0), (0, 0, 1)])
+def test_split_k_within_bound(cuda, monkeypatch, shape, la, lb, lc):
+    """GBBLAS_FMA_TILE=3: the TMA-fed kernel cut along K where its tiles leave
+    SMs idle (K ranges added into zeroed partials, then into C in order):
+    within the same bound as the unsplit kernels and the same bits on every
+    run.  Shapes too short in K for a split run unsplit."""
+    M, N, K = shape
+    rng = np.random.default_rng(M + N + K + la + 2 * lb + 4 * lc)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    got = run(cuda, A, B, C0, la, lb, lc, 3, monkeypatch)
+    np.testing.assert_array_equal(run(cuda, A, B, C0, la, lb, lc, 3, monkeypatch), got)
+    exact = A.astype(np.float64) @ B.astype(np.float64) + C0
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
+    assert np.all(np.abs(got.astype(np.float64) - exact) <= 2 * (K + 4) * EPS32 * scale)
