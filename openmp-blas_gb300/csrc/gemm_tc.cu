@@ -150,9 +150,12 @@ struct TcCfg {
   static constexpr uint32_t kBStageBytes = P * kSub * kBBytes + kSfBytes / 2;
   static constexpr uint32_t kTmemCols = 512;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
-  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
+  // FP8: per epilogue warp one 32 x 32 float block (4 KB, 1024-aligned) that
+  // a TMA reduce-add store adds into C
+  static constexpr size_t kEpiScratch = ModeTraits<MODE>::fp8 ? (size_t)ModeTraits<MODE>::kEpiWarps * 4096 : 0;
+  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kEpiScratch) / kStageBytes);
   static constexpr int kStages = kStagesFit > kMaxStages ? kMaxStages : kStagesFit;
-  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kBarBytes;
+  static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kEpiScratch + kBarBytes;
   static_assert(!(PAIR && ModeTraits<MODE>::fp8), "FP8 runs on single CTAs");
   static_assert(ModeTraits<MODE>::kBufs * ModeTraits<MODE>::kBufCols <= kTmemCols, "chunk buffers exceed TMEM");
   static_assert(!ModeTraits<MODE>::fp8 || ModeTraits<MODE>::kSfCol0 + 8 * kSub * kStages <= kTmemCols,
@@ -168,6 +171,8 @@ struct TcCfg {
 
 // One GEMM of a group, as the kernel sees it (device memory).
 struct TcProblem {
+  CUtensorMap c_map;  // FP8 with c_tma: C as a float tensor, 32 x 32 boxes, 128-byte swizzle
+  int c_tma;          // 1: the epilogue adds into C with TMA reduce-add stores
   int M, N;
   int num_kt;      // K stages of this (sub)problem: 64 of K (BF16) or 256 (FP8) each
   int kt0;         // its first K stage (a split-K part covers stages kt0 .. kt0 + num_kt - 1)
@@ -404,7 +409,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     return smem + (size_t)s * CF::kStageBytes + (size_t)NT * (CF::kABytes + CF::kBBytes) +
            (size_t)op * 512 * MT::kSub;
   };
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
+  float* epi_scratch = reinterpret_cast<float*>(smem + (size_t)ST * CF::kStageBytes);  // FP8, 1024-aligned
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes + CF::kEpiScratch);
   uint64_t* full = bars;                   // [ST]  TMA -> MMA
   uint64_t* empty = full + ST;             // [ST]  MMA -> TMA
   uint64_t* tfull = empty + ST;            // [kBufs] MMA -> epilogue: chunk in TMEM buffer b
@@ -748,6 +754,30 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       if (!ok) break;
       const int aborted = __shfl_sync(0xffffffffu, *abort_flag, 0);
       if (aborted) break;
+      if constexpr (MT::fp8) {
+        if (pr.c_tma) {
+          // C += the warp's 32 rows, 32 columns at a time, by TMA reduce-add
+          // from a 128-byte-swizzled block (16-byte chunk c of row r at c ^ (r % 8))
+          float* scr = epi_scratch + (warp - 2) * 1024;
+#pragma unroll
+          for (int cb = 0; cb < kCols; cb += 32) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+              *reinterpret_cast<float4*>(scr + lane * 32 + ((c ^ (lane & 7)) * 4)) =
+                  make_float4(acc[cb + 4 * c], acc[cb + 4 * c + 1], acc[cb + 4 * c + 2], acc[cb + 4 * c + 3]);
+            fence_proxy_async_shared();
+            __syncwarp();
+            const int bx = n0 + col0 + cb, by = m0 + q * 32;
+            if (lane == 0 && bx < pr.N && by < pr.M) {  // boxes wholly outside C are skipped
+              tma_reduce_add_2d(&pr.c_map, smem_u32(scr), bx, by);
+              bulk_commit_group();
+              bulk_wait_group_read0();  // the block is read before the next one overwrites it
+            }
+            __syncwarp();
+          }
+          continue;
+        }
+      }
       const int row = m0 + q * 32 + lane;
       if (row < pr.M) {
         float* crow = pr.C + (int64_t)row * pr.rsc;
@@ -800,6 +830,10 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       while (global_timer_ns() - t0 < 100000ull) {
       }
     }
+  }
+  // FP8: the epilogue's TMA reduce-add stores into C have completed
+  if constexpr (MT::fp8) {
+    if (warp >= 2 && warp < 2 + MT::kEpiWarps && lane == 0) bulk_wait_group0();
   }
   tc_fence_before();
   __syncthreads();
@@ -1011,6 +1045,14 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
       p.C = parts > 1 ? nullptr : g.C;  // partials: pointed into the workspace when bound
       p.rsc = parts > 1 ? ppitch : g.rsc;
       p.csc = parts > 1 ? 1 : g.csc;
+      p.c_tma = 0;
+      // FP8 adds its results into C with TMA reduce-add stores where C rows
+      // are contiguous, 16-byte aligned and 16-byte-multiple apart
+      if (pl.fp8() && parts == 1 && g.csc == 1 && g.rsc >= g.N && (g.rsc % 4) == 0 &&
+          (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+          make_map_f32_2d(&p.c_map, g.C, (uint64_t)g.N, (uint64_t)g.M, (uint64_t)g.rsc, 32, 32, true) ==
+              GBBLAS_STATUS_SUCCESS)
+        p.c_tma = 1;
       pl.probs.push_back(p);
       pl.part_off.push_back(parts > 1 ? ws : -1);
       if (parts > 1) ws += (int64_t)g.M * ppitch * (int64_t)sizeof(float);
