@@ -803,7 +803,7 @@ def run_serving(args):
     pool32 = torch.empty(int(args.pool_gb * (1 << 30)) // 8, device=dev).uniform_(-1, 1, generator=gen)
     pool64 = torch.empty(int(args.pool_gb * (1 << 30)) // 16, dtype=torch.float64, device=dev).uniform_(
         -1, 1, generator=gen)
-    srv = gbblas.Server(budget_bytes=64 << 30)
+    srv = gbblas.Server(budget_bytes=64 << 30, heavy_streams=args.heavy_streams, heavy_us=args.heavy_us)
 
     def lu(lo, hi):
         return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
@@ -880,7 +880,8 @@ def run_serving(args):
                                           "mean_round_size")},
             "config": {"workload": "Poisson 60% mtm / 30% mtv / 10% dot, dims log-uniform [64,4096], "
                                    "dot n log-uniform [1k,64M], 80% f32 (FP32-accurate) / 20% f64, seed 5",
-                       "budget_GiB": 64, "streams": 4}}
+                       "budget_GiB": 64, "streams": 4, "heavy_streams": args.heavy_streams or 2,
+                       "heavy_us": args.heavy_us or 1000}}
     print(json.dumps(line), flush=True)
     for p in outs:
         srv.free(p)
@@ -1212,6 +1213,10 @@ def main():
     ap.add_argument("--min-requests", type=int, default=400)
     ap.add_argument("--max-requests", type=int, default=4000)
     ap.add_argument("--lone-requests", type=int, default=200)
+    ap.add_argument("--heavy-streams", type=int, default=0,
+                    help="serving: heavy requests in flight at once (0: the library default)")
+    ap.add_argument("--heavy-us", type=int, default=0,
+                    help="serving: estimated GPU time (us) above which a request is heavy (0: default)")
     ap.add_argument("--pool-gb", type=float, default=48.0)
     ap.add_argument("--batch-accuracy", default="bf16x3", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--gemm-n", type=int, default=8192)
