@@ -581,6 +581,10 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       }
     } else if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16_f32(BMT, kBN);  // split-BF16; M = 256 for a pair
+      // single CTAs: p0*[q0; q1] as one N = 256 MMA - the q0 and q1 tiles of
+      // B^T lie back to back in the stage and the main and correction
+      // accumulators side by side in TMEM, so A's p0 is read once for both
+      constexpr uint32_t idesc_n256 = idesc_bf16_f32(kBM, 2 * kBN);
       int consumed = 0;  // K slices consumed (all tiles)
       int chunk_g = 0;   // chunks started (all tiles)
       bool stop = false;
@@ -652,9 +656,14 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
                          idesc_mxe4m3(kBM, kBN, kk, kk), sf_slot + 8u * u, sf_slot + 8u * u + 4u,
                          u == 0 ? acc : 1u);
             } else {
-              mma(acc_main, a[0] + off, bb[0] + off, acc);
               // corrections, largest first: p0p1, p1p0 (+ p0p2, p1p1, p2p0)
-              mma(acc_corr, a[0] + off, bb[1] + off, acc);
+              if constexpr (PAIR) {
+                mma(acc_main, a[0] + off, bb[0] + off, acc);
+                mma(acc_corr, a[0] + off, bb[1] + off, acc);
+              } else {
+                static_assert(CF::kBBytes == kBN * 128, "q1 must follow q0 directly");
+                mma_f16(acc_main, sw128_kmajor_desc(a[0] + off), sw128_kmajor_desc(bb[0] + off), idesc_n256, acc);
+              }
               mma(acc_corr, a[1] + off, bb[0] + off, 1u);
               if constexpr (P == 3) {
                 mma(acc_corr, a[0] + off, bb[2] + off, 1u);
