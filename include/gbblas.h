@@ -71,8 +71,18 @@ typedef enum gbblas_accuracy {
                                  values below 2^-9 of their block's max flush to 0 */
   GBBLAS_ACCURACY_AUTO = 3,   /* BF16X6 where the shape suits the tensor-core tiles,
                                  FP32 otherwise */
-  GBBLAS_ACCURACY_BF16X6 = 4  /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
+  GBBLAS_ACCURACY_BF16X6 = 4, /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
                                  the six products p_i*p_j with i + j < 3 on tcgen05 */
+  /* Double-precision GEMM (gbblas_dgemm_ex) only: */
+  GBBLAS_ACCURACY_FP64 = 5,         /* FP64 FMA on the CUDA cores (the reference's arithmetic) */
+  GBBLAS_ACCURACY_FP64_DIGITS7 = 6, /* Ozaki scheme on the BF16 tensor cores: every element
+                                       scaled by a power of two per row of A / column of B
+                                       and cut into 7 signed 8-bit digits, the 28 digit
+                                       products of weight < 7 summed exactly; error at most
+                                       about 4 K 2^-53 max_k|a_ik| max_k|b_kj| (the FP64
+                                       bound has sum_k |a_ik||b_kj| there); K <= 2^20 */
+  GBBLAS_ACCURACY_FP64_DIGITS8 = 7  /* the same with 8 digits (36 products): 2^-8 of that
+                                       error; K <= 2^20 */
 } gbblas_accuracy;
 
 /* ---------------------------------------------------------------- library */
@@ -131,6 +141,14 @@ gbblas_status gbblas_sgemm(int64_t M, int64_t N, int64_t K, const float* A, int6
 gbblas_status gbblas_dgemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                            const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
                            void* stream);
+
+/* gbblas_dgemm with a choice of arithmetic: GBBLAS_ACCURACY_FP64 (the same
+ * as gbblas_dgemm), GBBLAS_ACCURACY_FP64_DIGITS7 or _DIGITS8 (the tensor-core
+ * Ozaki scheme; NOT_SUPPORTED beyond its K limit).  Rows of A or columns of B
+ * holding Inf or NaN make their outputs NaN on the digit paths. */
+gbblas_status gbblas_dgemm_ex(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                              const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
+                              gbblas_accuracy accuracy, void* stream);
 
 /* ------------------------------------------------------------------ mtv */
 

@@ -204,6 +204,11 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
                        const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc,
                        cudaStream_t s) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
+  if constexpr (std::is_same_v<T, double>) {
+    // FP64_DIGITS7 / 8: the Ozaki scheme on the BF16 tensor cores
+    if (const int digits = dgemm_digits_count(acc))
+      return launch_dgemm_digits(c, digits, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+  }
   if constexpr (std::is_same_v<T, float>) {
     // BF16X3 / BF16X6 / FP8 always take the tensor cores.  AUTO: whichever
     // FP32-accurate path the autotuner measured faster for this shape bucket
@@ -330,7 +335,12 @@ template <typename T>
 gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
                        int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc, void* stream) {
   GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
-  if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+  if constexpr (std::is_same_v<T, float>) {
+    if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+  } else {
+    if (acc != GBBLAS_ACCURACY_FP64 && !dgemm_digits_count(acc))
+      return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, FP64_DIGITS7 or FP64_DIGITS8", (int)acc);
+  }
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
   return gemm_any<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, acc, as_stream(stream));
@@ -593,7 +603,15 @@ gbblas_status gbblas_sgemm(int64_t M, int64_t N, int64_t K, const float* A, int6
 gbblas_status gbblas_dgemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                            const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
                            void* stream) {
-  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP32, stream);
+  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP64, stream);
+}
+
+/* Double-precision GEMM with a choice of arithmetic (FP64 FMA or the
+ * tensor-core digit scheme). */
+gbblas_status gbblas_dgemm_ex(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                              const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
+                              gbblas_accuracy accuracy, void* stream) {
+  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, accuracy, stream);
 }
 
 gbblas_status gbblas_smtv(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y,
@@ -677,7 +695,7 @@ gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A,
 }
 gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                                 const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc) {
-  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP32);
+  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP64);
 }
 gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y) {
   return gemv_host<float>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y);

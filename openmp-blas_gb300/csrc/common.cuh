@@ -187,6 +187,17 @@ int* tc_group_error_word(const TcGroupPlan* plan);
 // Set the tensor-core kernels' launch attributes (before any stream capture).
 void tc_prepare(DeviceCtx* c);
 
+// Double-precision GEMM on the BF16 tensor cores (Ozaki scheme, 7 or 8
+// digits per element; gemm_f64_tc.cu): C += A * B.  The digit count of an
+// accuracy (0 if it is not a digit mode), the longest K a digit count takes,
+// and the kernels' launch attributes (set by tc_prepare).
+int dgemm_digits_count(gbblas_accuracy acc);
+int64_t dgemm_digits_max_k(int digits);
+void dgemm_digits_prepare(DeviceCtx* c);
+gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, int64_t M, int64_t N, int64_t K, const double* A,
+                                  int64_t rsa, int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C,
+                                  int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas = 0);
+
 // Grouped GEMV: row-streaming problems in one persistent launch, the rest
 // per problem (batch.cu).
 gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s);

@@ -1,0 +1,592 @@
+// gemm_f64_tc.cu - double-precision C += A * B on the BF16 tensor cores
+// (Ozaki scheme: exact integer digit products).
+//
+// GB300's FP64 pipes deliver about 1.25 TFLOP/s; its BF16 tensor cores more
+// than a thousand times that.  This path turns one FP64 GEMM into integer
+// GEMMs the tensor cores compute exactly:
+//
+//   1. Scales: every row i of A gets e_i with max_k |a_ik| < 2^e_i (the
+//      exponent frexp gives), every column j of B likewise f_j.  A row or
+//      column holding Inf or NaN is marked; its outputs become NaN.
+//   2. Digits: x = a_ik / 2^e_i lies in (-1, 1).  F = round(x * 2^(8S-1)) is
+//      an integer below 2^(8S-1) in magnitude (|x - F 2^(1-8S)| <= 2^-8S),
+//      written in balanced base 256: F = sum_s D_s 256^(S-1-s) with
+//      D_1..D_{S-1} in [-128, 127] and D_0 in [-128, 128], so every digit is
+//      an integer a BF16 holds exactly.  S digit planes per operand, K-major
+//      (A as M x K, B as its transpose N x K), zero-padded, in one arena.
+//      Integer arithmetic on the FP64 bit pattern: no FP64 instructions.
+//   3. GEMM: C_ij += 2^(e_i + f_j) sum_{w<S} 2^(-14-8w) G_w(i,j), where
+//      G_w = sum_k sum_{s+t=w} D_s(a_ik) E_t(b_kj) - every digit product of
+//      weight w (s + t > S-1 dropped).  The products are integers of at most
+//      2^14, so a group's sum over 128 of K is at most 7 * 128 * 2^14 < 2^24
+//      in magnitude and the FP32 accumulation in TMEM is exact.  Every 128 of
+//      K the epilogue converts each group to an integer and adds it, shifted
+//      by its weight, into two 64-bit accumulators per output (exact for K
+//      up to 2^20); at the end of the tile it converts them once to FP64,
+//      scales by the power of two and adds into C.
+//
+// Error: the only roundings are the digit truncation (2^-8S of the scale),
+// the dropped digit products and the final conversion and addition, so
+// |C_ij - exact| <= (S+1) 2^-8S K 2^(e_i+f_j) + 2 ulp, i.e. with S = 7
+// about 4 K 2^-53 max_k|a_ik| max_k|b_kj|.  The FP64 pipe's own bound is
+// K 2^-53 sum_k |a_ik| |b_kj|: the two agree where each row's and column's
+// magnitudes are comparable; rows mixing very large and very small values
+// lose relative accuracy in their small entries (use the FP64 pipes there).
+//
+// Kernel (persistent, one CTA per SM, tiles of 128 x 32 in static
+// round-robin order): per 32-K stage one 3-D TMA copy per operand brings all
+// S digit planes (64-byte rows, 64-byte swizzle).  Per 16 of K the MMA lane
+// issues S tcgen05.mma kind::f16: digit s of A against digits 0..S-1-s of B
+// (stacked in shared memory, so one MMA with N = 32 (S - s)) into the
+// accumulator columns of groups s..S-1 (group w at column 32 w of a
+// 256-column TMEM buffer; two buffers, so the epilogue folds one 128-K chunk
+// while the MMAs fill the next).  Warp roles as in gemm_tc.cu: warp 0
+// streams A, warp 10 B, warp 1 allocates TMEM and issues the MMAs, warps
+// 2-9 fold (warp w: TMEM lane quarter w % 4 = 32 tile rows, 16 of the 32
+// columns).  Every wait is bounded; a wait that gives up records
+// GBBLAS_STATUS_TIMEOUT, and the CTA drains its copies and MMAs, frees TMEM
+// and returns.
+//
+// Replaces the double-precision mtm of the reference (include/mtm.hpp:
+// 208-267 with include/simd_loop.hpp:132-158) when the caller asks for
+// GBBLAS_ACCURACY_FP64_DIGITS.  Roofline: the tensor pipe and shared-memory
+// bandwidth; 2*M*N*K algorithmic flops (the tensor cores execute
+// S(S+1)/2 times that in BF16 products).
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <climits>
+#include <cstdlib>
+#include <mutex>
+
+#include "common.cuh"
+#include "tc_ptx.cuh"
+#include "tma_map.cuh"
+
+namespace gbblas {
+namespace {
+
+using namespace tc;
+
+constexpr int kBM = 128;  // tile rows (TMEM lanes)
+constexpr int kBN = 32;   // tile columns per digit group
+constexpr int kBK = 32;   // K per stage: one 64-byte row of BF16
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 32 * (3 + kEpiWarps);  // A producer, MMA, 8 epilogue, B producer
+constexpr int kBProdWarp = 2 + kEpiWarps;
+constexpr uint32_t kBufCols = 256;  // one TMEM buffer: S <= 8 groups x 32 columns
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
+constexpr int kBadExp = INT_MIN;                  // scale marker: the row / column holds Inf or NaN
+
+template <int S>
+struct DgCfg {
+  static_assert(S >= 4 && S <= 8, "4 to 8 digits");
+  static constexpr uint32_t kATile = kBM * 64;  // one digit plane of A: 128 rows x 64 bytes
+  static constexpr uint32_t kBTile = kBN * 64;  // one of B^T: 32 rows x 64 bytes
+  static constexpr uint32_t kAStage = S * kATile;
+  static constexpr uint32_t kBStage = S * kBTile;
+  static constexpr uint32_t kStageBytes = kAStage + kBStage;
+  // stages per TMEM chunk: a group's sum over the chunk stays below 2^24
+  // (S * chunk * 2^14 with chunk = 128 K for S <= 7, 64 K for S = 8)
+  static constexpr int kChunk = S <= 7 ? 4 : 2;
+  // longest K: the 64-bit accumulators stay below 2^62 (each chunk adds
+  // less than 2^48 to hi and to lo)
+  static constexpr int64_t kMaxK = 1 << 20;
+  static constexpr size_t kBarBytes = 256;
+  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
+  static constexpr int kStages = kStagesFit > 4 ? 4 : kStagesFit;
+  static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + kBarBytes;
+  static_assert(kStages >= 2, "need a double-buffered stage ring");
+  static_assert((uint64_t)S * kChunk * kBK * 16384 < (1u << 24), "chunk sums must stay exact in FP32");
+  static_assert(kStageBytes % 1024 == 0, "stages stay 1024-byte aligned");
+  static_assert((2 * 4 + 2 * 2 + 1) * 8 + 8 <= kBarBytes, "barrier area too small");
+};
+
+// One GEMM (device-side view).
+struct DgProblem {
+  int M, N, num_kt, tiles_m, tiles_n, total_tiles;
+  double* C;
+  int64_t rsc, csc;
+  const int* ea;  // [rows of A, padded] row scales
+  const int* eb;  // [columns of B, padded] column scales
+};
+
+// ------------------------------------------------------ operand preparation
+// e[r] for r < rows_pad: the exponent of max_k |src(r, k)| (frexp's, so the
+// row's magnitudes lie below 2^e), 0 for an all-zero or padding row,
+// kBadExp for a row holding Inf or NaN.  Element (r, k) at src[r*rs + k*cs].
+// K contiguous (cs == 1): a warp per row; otherwise a thread per row (rows
+// contiguous when rs == 1, so a warp reads 32 consecutive rows).
+__global__ void __launch_bounds__(256) row_scale_kernel(const double* __restrict__ src, int64_t rows, int64_t K,
+                                                         int64_t rs, int64_t cs, int64_t rows_pad,
+                                                         int* __restrict__ e_out) {
+  const int lane = threadIdx.x & 31;
+  const bool warp_rows = cs == 1;
+  const int64_t r = warp_rows ? ((int64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) : ((int64_t)blockIdx.x * 256 + threadIdx.x);
+  if (r >= rows_pad) return;
+  double amax = 0.0;
+  bool bad = false;
+  if (r < rows) {
+    const double* p = src + r * rs;
+    if (warp_rows) {
+      for (int64_t k = lane; k < K; k += 32) {
+        const double v = __ldg(p + k);
+        bad |= !isfinite(v);
+        amax = fmax(amax, fabs(v));
+      }
+    } else {
+      for (int64_t k = 0; k < K; ++k) {
+        const double v = __ldg(p + k * cs);
+        bad |= !isfinite(v);
+        amax = fmax(amax, fabs(v));
+      }
+    }
+  }
+  if (warp_rows) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      bad = __shfl_xor_sync(0xffffffffu, (int)bad, o) != 0 || bad;
+    }
+    if (lane != 0) return;
+  }
+  int e = 0;
+  if (bad)
+    e = kBadExp;
+  else if (amax > 0.0)
+    (void)frexp(amax, &e);  // amax = m 2^e, m in [0.5, 1)
+  e_out[r] = e;
+}
+
+// Balanced base-256 digits of round(a * 2^(8S-1-e)), most significant first,
+// from the bit pattern of a (|a| < 2^e; integer operations only).
+template <int S>
+__device__ __forceinline__ void f64_digits(double a, int e, int (&d)[S]) {
+  if (e == kBadExp) {  // the row's outputs become NaN; its digits do not matter
+#pragma unroll
+    for (int s = 0; s < S; ++s) d[s] = 0;
+    return;
+  }
+  const long long bits = __double_as_longlong(a);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  long long m = bits & ((1ll << 52) - 1);
+  int p2;  // a = +-m * 2^p2
+  if (ex != 0) {
+    m |= 1ll << 52;
+    p2 = ex - 1075;
+  } else {
+    p2 = -1074;
+  }
+  const int sh = p2 + 8 * S - 1 - e;  // F = m * 2^sh, rounded; sh <= 8S - 54 for |a| < 2^e
+  long long F;
+  if (m == 0)
+    F = 0;
+  else if (sh >= 0)
+    F = m << sh;
+  else if (sh > -63)
+    F = (m + (1ll << (-sh - 1))) >> (-sh);
+  else
+    F = 0;
+  if (bits < 0) F = -F;
+#pragma unroll
+  for (int s = S - 1; s > 0; --s) {
+    const int lo = (int)(((F & 0xff) ^ 0x80) - 0x80);  // in [-128, 127]
+    d[s] = lo;
+    F = (F - lo) >> 8;  // exact: the low byte is now zero
+  }
+  d[0] = (int)F;  // in [-128, 128]
+}
+
+// Digit planes of one operand, written K-major into the arena: plane s of
+// row r at out[s * plane_stride + r * pitch + k], for every padded row
+// (< rows_pad) and padded k (< k_pad); zero outside rows x K.  A CTA takes
+// 32 rows x 32 K (8 KB of FP64 staged in shared memory, read along whichever
+// side is contiguous); thread t then makes the digits of 4 consecutive K of
+// one row and writes 8 bytes per plane.
+template <int S>
+__global__ void __launch_bounds__(256) digits_kernel(const double* __restrict__ src, int64_t rows, int64_t K,
+                                                     int64_t rs, int64_t cs, const int* __restrict__ e_row,
+                                                     __nv_bfloat16* __restrict__ out, int64_t plane_stride,
+                                                     int64_t pitch, int tiles_k) {
+  __shared__ double tile[32][33];
+  const int tid = threadIdx.x;
+  const int64_t r0 = (int64_t)(blockIdx.x / tiles_k) * 32, k0 = (int64_t)(blockIdx.x % tiles_k) * 32;
+  if (cs == 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = tid + 256 * i, r = idx >> 5, k = idx & 31;
+      tile[r][k] = (r0 + r < rows && k0 + k < K) ? __ldg(src + (r0 + r) * rs + k0 + k) : 0.0;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = tid + 256 * i, r = idx & 31, k = idx >> 5;
+      tile[r][k] = (r0 + r < rows && k0 + k < K) ? __ldg(src + (r0 + r) * rs + (k0 + k) * cs) : 0.0;
+    }
+  }
+  __syncthreads();
+  const int r = tid >> 3, kq = (tid & 7) * 4;
+  const int e = e_row[r0 + r];
+  int d[4][S];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) f64_digits<S>(tile[r][kq + j], e, d[j]);
+  __nv_bfloat16* o = out + (r0 + r) * pitch + k0 + kq;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const __nv_bfloat162 h01 = __floats2bfloat162_rn((float)d[0][s], (float)d[1][s]);  // exact: |d| <= 128
+    const __nv_bfloat162 h23 = __floats2bfloat162_rn((float)d[2][s], (float)d[3][s]);
+    uint2 w;
+    w.x = *reinterpret_cast<const uint32_t*>(&h01);
+    w.y = *reinterpret_cast<const uint32_t*>(&h23);
+    *reinterpret_cast<uint2*>(o + s * plane_stride) = w;
+  }
+}
+
+// ---------------------------------------------------------------- GEMM
+// Output tile t (static round-robin over the CTAs): grouped raster, 8 tile
+// rows per band, so the CTAs running at one time share A's and B's digit
+// tiles in L2.
+__device__ __forceinline__ void dg_tile(const DgProblem& p, int t, int& m0, int& n0) {
+  constexpr int kGroup = 8;
+  const int group_span = kGroup * p.tiles_n;
+  const int g = t / group_span;
+  const int first_m = g * kGroup;
+  const int gm = min(p.tiles_m - first_m, kGroup);
+  const int in_g = t % group_span;
+  m0 = (first_m + in_g % gm) * kBM;
+  n0 = (in_g / gm) * kBN;
+}
+
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1)
+    dgemm_digits_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
+                        const DgProblem p, int* __restrict__ err) {
+  using CF = DgCfg<S>;
+  constexpr int ST = CF::kStages;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  // stage st: A digit planes 0..S-1 (8 KB each), then B's (2 KB each)
+  auto a_tile = [&](int st, int d) { return smem + (size_t)st * CF::kStageBytes + (size_t)d * CF::kATile; };
+  auto b_tile = [&](int st) { return smem + (size_t)st * CF::kStageBytes + CF::kAStage; };
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
+  uint64_t* full = bars;        // [ST]  TMA -> MMA (both producers)
+  uint64_t* empty = full + 4;   // [ST]  MMA -> TMA
+  uint64_t* tfull = empty + 4;  // [2]   MMA -> epilogue: chunk in TMEM buffer b
+  uint64_t* tempty = tfull + 2;  // [2]  epilogue -> MMA: buffer b drained
+  uint64_t* accf = tempty + 2;   // [1]  every MMA of this CTA finished
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accf + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(&full[s], 2);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiWarps);
+    }
+    mbar_init(accf, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+    prefetch_tensormap(&tm_a);
+    prefetch_tensormap(&tm_b);
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_slot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  auto fail = [&]() {
+    *abort_flag = 1;
+    atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
+  };
+
+  int issued = 0;  // A producer: stages whose copies were issued
+  if ((warp == 0 || warp == kBProdWarp) && lane == 0) {
+    // producers: warp 0 brings A's digit planes, warp 10 B's, into the same stages
+    const bool is_a = warp == 0;
+    int n_issued = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
+      int m0, n0;
+      dg_tile(p, t, m0, n0);
+      for (int kt = 0; kt < p.num_kt; ++kt) {
+        const int s = n_issued % ST, round = n_issued / ST;
+        if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
+          fail();
+          stop = true;
+          break;
+        }
+        if (is_a) {
+          mbar_arrive_expect_tx(&full[s], CF::kAStage);
+          tma_load_3d(a_tile(s, 0), &tm_a, &full[s], kt * kBK, m0, 0);
+        } else {
+          mbar_arrive_expect_tx(&full[s], CF::kBStage);
+          tma_load_3d(b_tile(s), &tm_b, &full[s], kt * kBK, n0, 0);
+        }
+        ++n_issued;
+      }
+    }
+    if (is_a) issued = n_issued;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int consumed = 0, chunk_g = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
+        for (int kt = 0; kt < p.num_kt; ++kt) {
+          const int s = consumed % ST, round = consumed / ST;
+          const bool chunk_first = (kt % CF::kChunk) == 0;
+          const bool chunk_last = ((kt + 1) % CF::kChunk) == 0 || kt + 1 == p.num_kt;
+          if (chunk_first) ++chunk_g;
+          const int chunk = chunk_g - 1, b = chunk & 1;
+          if (chunk_first && chunk >= 2) {  // buffer b drained by the epilogue
+            if (!mbar_wait_bounded(&tempty[b], ((chunk >> 1) - 1) & 1, abort_flag, kWaitLimitNs)) {
+              fail();
+              stop = true;
+              break;
+            }
+            tc_fence_after();
+          }
+          if (!mbar_wait_bounded(&full[s], round & 1, abort_flag, kWaitLimitNs)) {
+            fail();
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t acc = tmem + (uint32_t)b * kBufCols;
+          const uint32_t b0 = smem_u32(b_tile(s));
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; ++kk) {
+            const uint32_t off = kk * 32;  // 16 BF16 of K inside the swizzled 64-byte row
+#pragma unroll
+            for (int d = 0; d < S; ++d) {
+              // digit d of A x digits 0..S-1-d of B (stacked: N = 32 (S - d))
+              // -> groups d..S-1; the first MMA of a chunk (N = 32 S) clears all
+              mma_f16(acc + 32u * d, sw64_kmajor_desc(smem_u32(a_tile(s, d)) + off), sw64_kmajor_desc(b0 + off),
+                      idesc_bf16_f32(kBM, kBN * (S - d)), (chunk_first && kk == 0 && d == 0) ? 0u : 1u);
+            }
+          }
+          mma_commit(&empty[s]);
+          if (chunk_last) mma_commit(&tfull[b]);
+          ++consumed;
+        }
+      }
+      mma_commit(accf);
+      if (*abort_flag) {
+        int never = 0;
+        (void)mbar_wait_bounded(accf, 0, &never, kWaitLimitNs);
+      }
+    }
+  } else if (warp >= 2 && warp < 2 + kEpiWarps) {
+    // epilogue: TMEM lane quarter q = warp % 4 (tile rows 32q..32q+31), 16
+    // columns (half h) of each group's 32
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * h);
+    const int nchunks = (p.num_kt + CF::kChunk - 1) / CF::kChunk;
+    int chunk_g = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+      int m0, n0;
+      dg_tile(p, t, m0, n0);
+      // sum_w G_w 2^(8(S-1-w)) = hi 2^32 + lo, exactly: groups w < S-4 go
+      // into hi (shifted by 8(S-5-w)), the last four into lo (8(S-1-w))
+      long long hi[16], lo[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0;
+      auto fold = [&](int d, const float (&v)[16]) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long g = (long long)__float2int_rn(v[j]);  // exact: an integer below 2^24
+          if (d < S - 4)
+            hi[j] += g << (8 * (S - 5 - d));
+          else
+            lo[j] += g << (8 * (S - 1 - d));
+        }
+      };
+      for (int c = 0; c < nchunks; ++c, ++chunk_g) {
+        const int b = chunk_g & 1;
+        const bool ready =
+            __all_sync(0xffffffffu, mbar_wait_bounded(&tfull[b], (chunk_g >> 1) & 1, abort_flag, kWaitLimitNs));
+        if (!ready) {
+          if (lane == 0) fail();
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t tb = trow + (uint32_t)b * kBufCols;
+#pragma unroll
+        for (int d = 0; d < S; d += 2) {
+          float v0[16], v1[16];
+          tmem_ld16(tb + 32u * d, v0);
+          if (d + 1 < S) tmem_ld16(tb + 32u * (d + 1), v1);
+          tmem_ld_wait();
+          fold(d, v0);
+          if (d + 1 < S) fold(d + 1, v1);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[b]);
+      }
+      if (!ok) break;
+      if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
+      const int row = m0 + q * 32 + lane;
+      if (row < p.M) {
+        const int ei = p.ea[row];
+        double* crow = p.C + (int64_t)row * p.rsc;
+        const int cn = n0 + 16 * h;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (cn + j >= p.N) continue;
+          const int ej = p.eb[cn + j];
+          // hi 2^32 + lo in units of 2^(e_i + f_j - 14 - 8(S-1))
+          double r;
+          if (ei == kBadExp || ej == kBadExp)
+            r = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+          else
+            r = ldexp((double)hi[j] * 4294967296.0 + (double)lo[j], ei + ej - 14 - 8 * (S - 1));
+          double* cp = crow + (int64_t)(cn + j) * p.csc;
+          *cp += r;
+        }
+      }
+    }
+  }
+
+  // ---- teardown: drain in-flight copies if the pipeline stopped early, make
+  // sure every MMA finished (warp 1 waited on accf after an abort), free TMEM
+  if (warp == 0 && lane == 0 && *abort_flag) {
+    int never = 0;
+    const int from = issued > ST ? issued - ST : 0;
+    for (int k = from; k < issued; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
+    // copies of B the A producer did not match complete on no barrier it
+    // waits for: give them 100 us to land
+    const uint64_t t0 = global_timer_ns();
+    while (global_timer_ns() - t0 < 100000ull) {
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// ------------------------------------------------------------ host side
+inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <int S>
+void dg_setup(DeviceCtx* c) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  std::lock_guard<std::mutex> lk(mu);
+  if (!done[c->device & 63]) {
+    cudaFuncSetAttribute(dgemm_digits_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DgCfg<S>::kSmem);
+    done[c->device & 63] = true;
+  }
+}
+
+template <int S>
+gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa,
+                            int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
+                            int64_t csc, cudaStream_t stream, int max_ctas) {
+  using CF = DgCfg<S>;
+  if (K > CF::kMaxK) {
+    set_error("dgemm (FP64 digits): K = %lld exceeds %lld", (long long)K, (long long)CF::kMaxK);
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  if (M > (1 << 30) || N > (1 << 30)) {
+    set_error("dgemm (FP64 digits): problem too large for the tile grid");
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  const int64_t Mp = round_up(M, kBM), Np = round_up(N, kBN), Kp = round_up(K, kBK);
+  const size_t off_ea = kScratchZeroBytes;
+  const size_t off_eb = off_ea + align256(sizeof(int) * (size_t)Mp);
+  const size_t off_a = off_eb + align256(sizeof(int) * (size_t)Np);
+  const size_t a_plane = (size_t)(Mp * Kp), b_plane = (size_t)(Np * Kp);
+  const size_t off_b = off_a + align256((size_t)S * a_plane * sizeof(__nv_bfloat16));
+  const size_t bytes = off_b + align256((size_t)S * b_plane * sizeof(__nv_bfloat16));
+  void* scratch = nullptr;
+  GB_TRY(get_scratch(c, stream, bytes, &scratch));
+  char* base = static_cast<char*>(scratch);
+  int* ea = reinterpret_cast<int*>(base + off_ea);
+  int* eb = reinterpret_cast<int*>(base + off_eb);
+  auto* da = reinterpret_cast<__nv_bfloat16*>(base + off_a);
+  auto* db = reinterpret_cast<__nv_bfloat16*>(base + off_b);
+  int* err = reinterpret_cast<int*>(base + kErrWordOffset);
+
+  // scales: rows of A over K; columns of B (element (n, k) = B[k*rsb + n*csb])
+  row_scale_kernel<<<(unsigned)(csa == 1 ? Mp / 8 : (Mp + 255) / 256), 256, 0, stream>>>(A, M, K, rsa, csa, Mp, ea);
+  GB_TRY(check_launch("row_scale_kernel(A)"));
+  row_scale_kernel<<<(unsigned)(rsb == 1 ? Np / 8 : (Np + 255) / 256), 256, 0, stream>>>(B, N, K, csb, rsb, Np, eb);
+  GB_TRY(check_launch("row_scale_kernel(B)"));
+  const int tiles_k = (int)(Kp / 32);
+  digits_kernel<S><<<(unsigned)((Mp / 32) * tiles_k), 256, 0, stream>>>(A, M, K, rsa, csa, ea, da, (int64_t)a_plane,
+                                                                       Kp, tiles_k);
+  GB_TRY(check_launch("digits_kernel(A)"));
+  digits_kernel<S><<<(unsigned)((Np / 32) * tiles_k), 256, 0, stream>>>(B, N, K, csb, rsb, eb, db, (int64_t)b_plane,
+                                                                       Kp, tiles_k);
+  GB_TRY(check_launch("digits_kernel(B)"));
+
+  CUtensorMap ma, mb;
+  GB_TRY(make_map(&ma, da, (uint64_t)Mp, (uint64_t)Kp, (uint64_t)S, kBM, false, 64));
+  GB_TRY(make_map(&mb, db, (uint64_t)Np, (uint64_t)Kp, (uint64_t)S, kBN, false, 64));
+  DgProblem p;
+  p.M = (int)M;
+  p.N = (int)N;
+  p.num_kt = (int)(Kp / kBK);
+  p.tiles_m = (int)(Mp / kBM);
+  p.tiles_n = (int)(Np / kBN);
+  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+  if (tiles >= (1ll << 31)) {
+    set_error("dgemm (FP64 digits): too many tiles");
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  p.total_tiles = (int)tiles;
+  p.C = C;
+  p.rsc = rsc;
+  p.csc = csc;
+  p.ea = ea;
+  p.eb = eb;
+  dg_setup<S>(c);
+  int grid = (int)std::min<int64_t>(tiles, c->num_sms);
+  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+  dgemm_digits_kernel<S><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, p, err);
+  return check_launch("dgemm_digits_kernel");
+}
+
+}  // namespace
+
+int dgemm_digits_count(gbblas_accuracy acc) {
+  return acc == GBBLAS_ACCURACY_FP64_DIGITS7 ? 7 : (acc == GBBLAS_ACCURACY_FP64_DIGITS8 ? 8 : 0);
+}
+
+int64_t dgemm_digits_max_k(int digits) { return digits == 8 ? DgCfg<8>::kMaxK : DgCfg<7>::kMaxK; }
+
+void dgemm_digits_prepare(DeviceCtx* c) {
+  dg_setup<7>(c);
+  dg_setup<8>(c);
+}
+
+gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, int64_t M, int64_t N, int64_t K, const double* A,
+                                  int64_t rsa, int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C,
+                                  int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas) {
+  if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
+  switch (digits) {
+    case 7: return launch_digits<7>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    case 8: return launch_digits<8>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    default:
+      set_error("dgemm (FP64 digits): %d digits not supported (7 or 8)", digits);
+      return GBBLAS_STATUS_INVALID_VALUE;
+  }
+}
+
+}  // namespace gbblas

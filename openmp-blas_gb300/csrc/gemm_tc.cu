@@ -872,6 +872,8 @@ __global__ void __launch_bounds__(256) splitk_reduce_kernel(const SplitReduce* _
   }
 }
 
+}  // namespace
+
 // ------------------------------------------------------------ host side
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -913,6 +915,8 @@ gbblas_status make_map(CUtensorMap* map, const void* base, uint64_t rows, uint64
   }
   return GBBLAS_STATUS_SUCCESS;
 }
+
+namespace {
 
 inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
@@ -1260,6 +1264,7 @@ size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
 
 void tc_prepare(DeviceCtx* c) {
   sgemm_tma_prepare(c);
+  dgemm_digits_prepare(c);
   kernel_setup<2, false>(c);
   kernel_setup<3, false>(c);
   kernel_setup<kModeFp8, false>(c);

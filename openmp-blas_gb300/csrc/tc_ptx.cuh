@@ -225,6 +225,18 @@ __device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t smem_addr) {
   return d;
 }
 
+// The same for a 64-byte-swizzled box: rows of 64 bytes, 8-row groups 512
+// bytes apart, tile base 512-byte aligned, swizzle mode 4 = 64B.
+__device__ __forceinline__ uint64_t sw64_kmajor_desc(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((smem_addr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>(1u) << 16;
+  d |= static_cast<uint64_t>(512u >> 4) << 32;
+  d |= static_cast<uint64_t>(1u) << 46;
+  d |= static_cast<uint64_t>(4u) << 61;
+  return d;
+}
+
 // Instruction descriptor for kind::f16 with BF16 A/B, F32 D, both K-major.
 // bits 4-5 D format (1 = F32), 7-9 A format (1 = BF16), 10-12 B format
 // (1 = BF16), 15/16 A/B major (0 = K), 17-22 N >> 3, 24-28 M >> 4.

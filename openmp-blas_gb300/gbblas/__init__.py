@@ -23,6 +23,9 @@ ACCURACY_BF16X3 = 1
 ACCURACY_FP8 = 2
 ACCURACY_AUTO = 3
 ACCURACY_BF16X6 = 4
+ACCURACY_FP64 = 5          # double GEMM on the FP64 pipes
+ACCURACY_FP64_DIGITS7 = 6  # double GEMM, Ozaki scheme on the BF16 tensor cores, 7 digits
+ACCURACY_FP64_DIGITS8 = 7  # the same with 8 digits
 
 STATUS = {
     0: "SUCCESS", 1: "INVALID_VALUE", 2: "SHAPE_MISMATCH", 3: "ALLOC_FAILED",
@@ -46,6 +49,7 @@ SIGNATURES = {
     "gbblas_release_cache": (_int, []),
     "gbblas_sgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _vp]),
     "gbblas_dgemm": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp]),
+    "gbblas_dgemm_ex": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _vp]),
     "gbblas_smtv": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
     "gbblas_dmtv": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
     "gbblas_svtm": (_int, [_int, _i64, _i64, _vp, _vp, _vp, _vp]),
@@ -173,15 +177,20 @@ def _dev(t) -> int:
 
 
 def gemm(A, B, C, accuracy: int = ACCURACY_FP32, stream=None):
-    """C += A @ B on device tensors of any strides (2-D torch tensors)."""
+    """C += A @ B on device tensors of any strides (2-D torch tensors).
+    float32: `accuracy` is one of ACCURACY_FP32 .. ACCURACY_BF16X6; float64:
+    ACCURACY_FP32 or ACCURACY_FP64 (the FP64 pipes) or ACCURACY_FP64_DIGITS7 / 8."""
     M, K = A.shape
     N = B.shape[1]
     p = _pfx(A)
     args = [M, N, K, _dev(A), A.stride(0), A.stride(1), _dev(B), B.stride(0), B.stride(1),
             _dev(C), C.stride(0), C.stride(1)]
     if p == "s":
-        args.append(accuracy)
-    call(f"gbblas_{p}gemm", *args, _stream_ptr(stream))
+        call("gbblas_sgemm", *args, accuracy, _stream_ptr(stream))
+    elif accuracy in (ACCURACY_FP32, ACCURACY_FP64):
+        call("gbblas_dgemm", *args, _stream_ptr(stream))
+    else:
+        call("gbblas_dgemm_ex", *args, accuracy, _stream_ptr(stream))
     return C
 
 
