@@ -28,7 +28,8 @@ workload instead (the compiled reference where it exists, otherwise the
 oracle port) and prints the same line with "impl": "reference".
 
 Other workloads (`--workload`, one JSON line per result): precision (the
-8192^3 GEMM paths and their errors against FP64), batching, serving,
+8192^3 GEMM paths and their errors against FP64), f64 (8192^3 double-precision
+GEMM on the FP64 pipes and as the tensor-core Ozaki scheme), batching, serving,
 stream_ops, sweep (the reference's size sweeps in its metric formats) and mtm
 (the plain 1024^3 single-precision mtm against the FMA-pipe peak).
 
@@ -629,6 +630,87 @@ def run_precision(args):
         del A, B
 
 
+def run_f64(args):
+    """Double-precision GEMM, M = N = K = --gemm-n (8192) from float64
+    operands on two input sets (U[-1,1) and wide-range s*m*2^e, e in
+    [-10, 10]): the FP64 pipes (FMA kernel) and the Ozaki scheme on the BF16
+    tensor cores with 7 and 8 digits.  TFLOP/s of 2*M*N*K algorithmic flops,
+    max / mean relative and normwise error against long-double dots on
+    sampled entries.  One JSON line per (path, set)."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    n = args.gemm_n
+    flops = 2.0 * n ** 3
+    g = torch.Generator(device="cuda").manual_seed(4)
+    rng = np.random.default_rng(4)
+    sample = 1024
+    rows = rng.integers(0, n, sample)
+    cols = rng.integers(0, n, sample)
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(pp)) if os.path.exists(pp) else {}
+    for set_name in ("uniform", "wide"):
+        if set_name not in args.sets.split(","):
+            continue
+        if set_name == "uniform":
+            A = torch.rand(n, n, generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+            B = torch.rand(n, n, generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+        else:
+            def wide():
+                s = torch.where(torch.rand(n, n, generator=g, device="cuda") < 0.5, -1.0, 1.0).double()
+                m = torch.rand(n, n, generator=g, device="cuda", dtype=torch.float64) + 1.0
+                e = torch.randint(-10, 11, (n, n), generator=g, device="cuda").double()
+                return s * m * torch.exp2(e)
+            A, B = wide(), wide()
+        An, Bn = A.cpu().numpy(), B.cpu().numpy()
+        exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
+        for path, acc, products in (("digits7", 6, 28), ("digits8", 7, 36), ("fp64", 5, None)):
+            if path not in args.f64_paths.split(","):
+                continue
+            C = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+            sp = torch.cuda.current_stream().cuda_stream or None
+
+            def call():
+                gbblas.call("gbblas_dgemm_ex", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1,
+                            acc, sp)
+            slow = path == "fp64"
+            for _ in range(1 if slow else args.warmup):
+                call()
+            torch.cuda.synchronize()
+            iters = 2 if slow else args.gemm_iters
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(0) as clk:
+                t0 = time.time()
+                e0.record()
+                for _ in range(iters):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                clk.mark(t0, time.time())
+            gbblas.call("gbblas_check_stream", sp)
+            ms = e0.elapsed_time(e1) / iters
+            C.zero_()
+            call()
+            got = C.cpu().numpy()[rows, cols]
+            rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
+            normwise = np.abs(got - exact) / absx
+            tf = flops / (ms / 1e3) / 1e12
+            line = {"metric": "GEMM TFLOP/s (float64 operands)", "path": path, "input_set": set_name,
+                    "value": round(tf, 3), "unit": "TFLOP/s", "ms_per_gemm": round(ms, 3), "M": n, "N": n, "K": n,
+                    "flops": "2*M*N*K algorithmic", "dtype": "f64", "max_rel_err": float(rel.max()),
+                    "mean_rel_err": float(rel.mean()), "max_normwise_err": float(normwise.max()),
+                    "error_sample": f"{sample} entries vs long double", "clocks": clk.summary()}
+            if products and peaks.get("bf16_tflops"):
+                line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
+                line["tensor_peak"] = (f"{products} BF16 digit products per algorithmic flop vs bf16_tflops "
+                                       f"{peaks['bf16_tflops']} (measured, burst)")
+            print(json.dumps(line), flush=True)
+        del A, B
+
+
 def batching_shapes(seed=3):
     """512 GEMM shapes (M, N, K log-uniform in [32, 2048], multiples of 8) and
     4096 GEMV shapes (rows, cols log-uniform in [256, 16384])."""
@@ -804,6 +886,9 @@ def run_serving(args):
     pool64 = torch.empty(int(args.pool_gb * (1 << 30)) // 16, dtype=torch.float64, device=dev).uniform_(
         -1, 1, generator=gen)
     srv = gbblas.Server(budget_bytes=64 << 30, heavy_streams=args.heavy_streams, heavy_us=args.heavy_us)
+    # float64 GEMMs: AUTO (the library default: guarded tensor-core digits
+    # where the shape suits) or the FP64 pipes
+    f64_acc = 5 if args.f64_accuracy == "fp64" else 3
 
     def lu(lo, hi):
         return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
@@ -824,7 +909,9 @@ def run_serving(args):
             M, N, K = lu(64, 4096), lu(64, 4096), lu(64, 4096)
             out = srv.alloc(M * N * es)
             outs.append(out)
-            return "mtm", gbblas.Request(gbblas.OP_MTM, dt, 3, 1, M, N, K, window(pool, M * K), window(pool, K * N), out)
+            acc = f64_acc if f64 else 3
+            return "mtm", gbblas.Request(gbblas.OP_MTM, dt, acc, 1, M, N, K, window(pool, M * K), window(pool, K * N),
+                                         out)
         if u < 0.9:
             M, N = lu(64, 4096), lu(64, 4096)
             out = srv.alloc(M * es)
@@ -880,6 +967,8 @@ def run_serving(args):
                                           "mean_round_size")},
             "config": {"workload": "Poisson 60% mtm / 30% mtv / 10% dot, dims log-uniform [64,4096], "
                                    "dot n log-uniform [1k,64M], 80% f32 (FP32-accurate) / 20% f64, seed 5",
+                       "f64_gemm": ("FP64 pipes" if f64_acc == 5 else
+                                    "AUTO: guarded 7-digit tensor-core scheme from 2^21 multiply-adds, FP64 pipes below"),
                        "budget_GiB": 64, "streams": 4, "heavy_streams": args.heavy_streams or 2,
                        "heavy_us": args.heavy_us or 1000}}
     print(json.dumps(line), flush=True)
@@ -1203,7 +1292,7 @@ def run_sweep(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="bandwidth",
-                    choices=["bandwidth", "precision", "batching", "serving", "stream_ops", "sweep", "mtm"])
+                    choices=["bandwidth", "precision", "f64", "batching", "serving", "stream_ops", "sweep", "mtm"])
     ap.add_argument("--sweep-op", default="mtm", choices=["mtm", "mtv", "dot"])
     ap.add_argument("--sweep-cpu-max", type=int, default=1024,
                     help="sweep workload: largest size the CPU series runs (0 beyond)")
@@ -1218,12 +1307,16 @@ def main():
     ap.add_argument("--heavy-us", type=int, default=0,
                     help="serving: estimated GPU time (us) above which a request is heavy (0: default)")
     ap.add_argument("--pool-gb", type=float, default=48.0)
+    ap.add_argument("--f64-accuracy", default="auto", choices=["auto", "fp64"],
+                    help="serving: arithmetic of the float64 GEMM requests")
     ap.add_argument("--batch-accuracy", default="bf16x3", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--gemm-n", type=int, default=8192)
     ap.add_argument("--gemm-iters", type=int, default=5)
     ap.add_argument("--paths", default="bf16x3,bf16x6,fp8,fp32",
                     help="precision workload: comma-separated GEMM paths to run")
     ap.add_argument("--sets", default="uniform,wide", help="precision workload: input sets to run")
+    ap.add_argument("--f64-paths", default="digits7,digits8,fp64",
+                    help="f64 workload: comma-separated double-precision GEMM paths to run")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
@@ -1247,6 +1340,8 @@ def main():
         run_reference(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "f64":
+        run_f64(args)
     elif args.workload == "batching":
         run_batching(args)
     elif args.workload == "serving":

@@ -356,7 +356,9 @@ typedef enum gbblas_dtype { GBBLAS_F32 = 0, GBBLAS_F64 = 1 } gbblas_dtype;
 typedef struct gbblas_request {
   int32_t op;       /* gbblas_op */
   int32_t dtype;    /* gbblas_dtype */
-  int32_t accuracy; /* gbblas_accuracy, float MTM only (AUTO = six-product split-BF16) */
+  int32_t accuracy; /* gbblas_accuracy of an MTM: float - AUTO = six-product split-BF16;
+                       double - FP64 = the FP64 pipes, FP64_DIGITS7 / 8 = unguarded
+                       tensor-core digits, any other value gbblas_dgemm's default */
   int32_t layout;   /* gbblas_layout of the matrices */
   int64_t M, N, K;
   const void* A; /* MTM: A;  MTV/VTM: matrix;  DOT: a */

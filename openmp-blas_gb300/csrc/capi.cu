@@ -199,15 +199,46 @@ gbblas_status gemv_any(DeviceCtx* c, gbblas_layout la, bool transpose, int64_t M
   return launch_gemv_cols<T>(c, out_len, red_len, A, lda, x, y, accumulate, s);
 }
 
+}  // namespace
+
+// Shapes where AUTO takes the guarded tensor-core digits for a double GEMM:
+// K of at least 32 (and within the digit kernels' limit) where the digits'
+// estimated time is the shorter.  FP64 pipes: about 4000 multiply-adds per
+// us per SM (GB300: 2 DFMA per cycle per SM), over as many SMs as there are
+// 64 x 64 tiles; measured 0.27 ms at 256^3 (16 tiles).  Digits: about 50 us
+// of operand preparation and launches, then ~38 TFLOP/s.
+bool dgemm_auto_digits(int64_t M, int64_t N, int64_t K, int num_sms) {
+  if (K < 32 || K > dgemm_digits_max_k(7)) return false;
+  const double macs = (double)M * (double)N * (double)K;
+  const double tiles = (double)((M + 63) / 64) * (double)((N + 63) / 64);
+  const double pipes_us = 5.0 + macs / (4000.0 * std::min(tiles, (double)std::max(num_sms, 1)));
+  const double digits_us = 50.0 + 2.0 * macs / 38e6;
+  return digits_us < pipes_us;
+}
+
+namespace {
+
+// The arithmetic of gbblas_dgemm / _host (the reference's double mtm): AUTO,
+// or the FP64 pipes throughout when GBBLAS_DGEMM_FP64=1.
+gbblas_accuracy dgemm_default_accuracy() {
+  const char* e = std::getenv("GBBLAS_DGEMM_FP64");
+  return (e && e[0] == '1') ? GBBLAS_ACCURACY_FP64 : GBBLAS_ACCURACY_AUTO;
+}
+
 template <typename T>
 gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa,
                        const T* B, int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc,
                        cudaStream_t s) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if constexpr (std::is_same_v<T, double>) {
-    // FP64_DIGITS7 / 8: the Ozaki scheme on the BF16 tensor cores
+    // FP64_DIGITS7 / 8: the Ozaki scheme on the BF16 tensor cores.  AUTO:
+    // its guarded form (the FP64 pipes' error bound, blocks that could miss
+    // it recomputed on the pipes) where the shape amortises the operand
+    // preparation, the FP64 pipes elsewhere.
     if (const int digits = dgemm_digits_count(acc))
-      return launch_dgemm_digits(c, digits, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+      return launch_dgemm_digits(c, digits, false, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    if (acc == GBBLAS_ACCURACY_AUTO && dgemm_auto_digits(M, N, K, c->num_sms))
+      return launch_dgemm_digits(c, 7, true, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
   }
   if constexpr (std::is_same_v<T, float>) {
     // BF16X3 / BF16X6 / FP8 always take the tensor cores.  AUTO: whichever
@@ -338,8 +369,9 @@ gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa,
   if constexpr (std::is_same_v<T, float>) {
     if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
   } else {
-    if (acc != GBBLAS_ACCURACY_FP64 && !dgemm_digits_count(acc))
-      return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, FP64_DIGITS7 or FP64_DIGITS8", (int)acc);
+    if (acc != GBBLAS_ACCURACY_FP64 && acc != GBBLAS_ACCURACY_AUTO && !dgemm_digits_count(acc))
+      return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, AUTO, FP64_DIGITS7 or FP64_DIGITS8",
+                 (int)acc);
   }
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
@@ -603,7 +635,7 @@ gbblas_status gbblas_sgemm(int64_t M, int64_t N, int64_t K, const float* A, int6
 gbblas_status gbblas_dgemm(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                            const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
                            void* stream) {
-  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP64, stream);
+  return gemm_dev<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, dgemm_default_accuracy(), stream);
 }
 
 /* Double-precision GEMM with a choice of arithmetic (FP64 FMA or the
@@ -695,7 +727,7 @@ gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A,
 }
 gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                                 const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc) {
-  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, GBBLAS_ACCURACY_FP64);
+  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, dgemm_default_accuracy());
 }
 gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y) {
   return gemv_host<float>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y);

@@ -188,15 +188,21 @@ int* tc_group_error_word(const TcGroupPlan* plan);
 void tc_prepare(DeviceCtx* c);
 
 // Double-precision GEMM on the BF16 tensor cores (Ozaki scheme, 7 or 8
-// digits per element; gemm_f64_tc.cu): C += A * B.  The digit count of an
-// accuracy (0 if it is not a digit mode), the longest K a digit count takes,
-// and the kernels' launch attributes (set by tc_prepare).
+// digits per element; gemm_f64_tc.cu): C += A * B.  guarded (7 digits):
+// every 32 x 16 output block whose digit error could exceed the FP64 pipes'
+// bound is recomputed on the FP64 pipes.  The digit count of an accuracy (0
+// if it is not a digit mode), the longest K a digit count takes, and the
+// kernels' launch attributes (set by tc_prepare).
 int dgemm_digits_count(gbblas_accuracy acc);
 int64_t dgemm_digits_max_k(int digits);
+size_t dgemm_digits_scratch_bytes(int digits, bool guarded, int64_t M, int64_t N, int64_t K);
+// AUTO for a double GEMM: the guarded digits for this shape (else the FP64 pipes).
+bool dgemm_auto_digits(int64_t M, int64_t N, int64_t K, int num_sms);
 void dgemm_digits_prepare(DeviceCtx* c);
-gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, int64_t M, int64_t N, int64_t K, const double* A,
-                                  int64_t rsa, int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C,
-                                  int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas = 0);
+gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, bool guarded, int64_t M, int64_t N, int64_t K,
+                                  const double* A, int64_t rsa, int64_t csa, const double* B, int64_t rsb,
+                                  int64_t csb, double* C, int64_t rsc, int64_t csc, cudaStream_t stream,
+                                  int max_ctas = 0);
 
 // Grouped GEMV: row-streaming problems in one persistent launch, the rest
 // per problem (batch.cu).

@@ -77,15 +77,20 @@ constexpr int kBProdWarp = 2 + kEpiWarps;
 constexpr uint32_t kBufCols = 256;  // one TMEM buffer: S <= 8 groups x 32 columns
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
-constexpr int kBadExp = INT_MIN;                  // scale marker: the row / column holds Inf or NaN
+constexpr int kBadExp = INT_MAX;                  // scale marker: the row / column holds Inf or NaN
+constexpr int kZeroExp = (int)0x80808080;          // scale of an all-zero row (the fill byte 0x80)
 
-template <int S>
+// S digits; G = 1 adds the guard plane (P = max(|D_0| - 1, 0), whose
+// product sum bounds sum_k |a_ik||b_kj| from below) and its accumulator in
+// TMEM column slot S.
+template <int S, int G>
 struct DgCfg {
-  static_assert(S >= 4 && S <= 8, "4 to 8 digits");
-  static constexpr uint32_t kATile = kBM * 64;  // one digit plane of A: 128 rows x 64 bytes
+  static_assert(S >= 4 && S + G <= 8, "4 to 8 digits, and a free TMEM slot for the guard");
+  static constexpr int NP = S + G;              // planes per operand
+  static constexpr uint32_t kATile = kBM * 64;  // one plane of A: 128 rows x 64 bytes
   static constexpr uint32_t kBTile = kBN * 64;  // one of B^T: 32 rows x 64 bytes
-  static constexpr uint32_t kAStage = S * kATile;
-  static constexpr uint32_t kBStage = S * kBTile;
+  static constexpr uint32_t kAStage = NP * kATile;
+  static constexpr uint32_t kBStage = NP * kBTile;
   static constexpr uint32_t kStageBytes = kAStage + kBStage;
   // stages per TMEM chunk: a group's sum over the chunk stays below 2^24
   // (S * chunk * 2^14 with chunk = 128 K for S <= 7, 64 K for S = 8)
@@ -110,54 +115,134 @@ struct DgProblem {
   int64_t rsc, csc;
   const int* ea;  // [rows of A, padded] row scales
   const int* eb;  // [columns of B, padded] column scales
+  // guarded form: the 32 x 16 blocks the guard rejected (block b of tile t
+  // = t * 8 + epilogue warp), recomputed on the FP64 pipes from A and B
+  int* fix_count;
+  int* fix_list;
+  const double* A;
+  const double* B;
+  int64_t rsa, csa, rsb, csb;
+  int64_t K;
 };
 
+// Guard: a block's digit result is kept when every output has
+// sum_k P(a_ik) P(b_kj) >= 2^14, i.e. sum_k |a_ik||b_kj| >= 2^(e_i + f_j):
+// the digit error (at most 9 2^-56 K 2^(e_i + f_j) with 7 digits) is then
+// below 0.3 K eps sum_k |a_ik||b_kj| and, with the two final roundings,
+// inside the FP64 pipes' bound 2 K eps (|A||B| + |C|).
+constexpr int kGuardMin = 1 << 14;
+constexpr int kGuardCap = 1 << 30;  // the guard sums saturate here (int32)
+
 // ------------------------------------------------------ operand preparation
-// e[r] for r < rows_pad: the exponent of max_k |src(r, k)| (frexp's, so the
-// row's magnitudes lie below 2^e), 0 for an all-zero or padding row,
-// kBadExp for a row holding Inf or NaN.  Element (r, k) at src[r*rs + k*cs].
-// K contiguous (cs == 1): a warp per row; otherwise a thread per row (rows
-// contiguous when rs == 1, so a warp reads 32 consecutive rows).
-__global__ void __launch_bounds__(256) row_scale_kernel(const double* __restrict__ src, int64_t rows, int64_t K,
-                                                         int64_t rs, int64_t cs, int64_t rows_pad,
-                                                         int* __restrict__ e_out) {
-  const int lane = threadIdx.x & 31;
-  const bool warp_rows = cs == 1;
-  const int64_t r = warp_rows ? ((int64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) : ((int64_t)blockIdx.x * 256 + threadIdx.x);
-  if (r >= rows_pad) return;
-  double amax = 0.0;
-  bool bad = false;
-  if (r < rows) {
-    const double* p = src + r * rs;
-    if (warp_rows) {
-      for (int64_t k = lane; k < K; k += 32) {
-        const double v = __ldg(p + k);
-        bad |= !isfinite(v);
-        amax = fmax(amax, fabs(v));
-      }
-    } else {
-      for (int64_t k = 0; k < K; ++k) {
-        const double v = __ldg(p + k * cs);
-        bad |= !isfinite(v);
-        amax = fmax(amax, fabs(v));
-      }
-    }
-  }
-  if (warp_rows) {
+// Row scales: e[r] = the exponent frexp gives for max_k |src(r, k)| (so the
+// row's magnitudes lie below 2^e), element (r, k) at src[r*rs + k*cs].  The
+// array starts filled with the byte 0x80 (kZeroExp: an all-zero row); every
+// CTA takes 32 rows x 256 K, reads them along whichever side is contiguous,
+// and atomicMax-es its rows' exponents in - kBadExp (INT_MAX) for a row
+// holding Inf or NaN, which then stays.
+// One launch serves both operands: CTAs below a.blocks take A, the rest B
+// (B^T: rows = columns of B); block 0 also clears the fix-up count.
+constexpr int kScaleTK = 256;
+
+// One operand of the preparation kernels (A, or B read as its transpose).
+struct DgOperand {
+  const double* src;
+  int64_t rows, K, rs, cs;  // element (r, k) at src[r*rs + k*cs]
+  int* e;                   // row scales
+  __nv_bfloat16* out;       // digit planes
+  int64_t plane_stride, pitch;
+  int tiles_k;              // CTAs per 32 rows (K tiles of the kernel at hand)
+  int blocks;               // CTAs of this operand
+};
+
+__global__ void __launch_bounds__(256) row_scale_kernel(const DgOperand oa, const DgOperand ob, int* fix_count) {
+  __shared__ double part_max[8][33];
+  __shared__ int part_bad[8][33];
+  const bool is_a = (int)blockIdx.x < oa.blocks;
+  const DgOperand& o = is_a ? oa : ob;
+  const int blk = is_a ? (int)blockIdx.x : (int)blockIdx.x - oa.blocks;
+  const double* __restrict__ src = o.src;
+  const int64_t rows = o.rows, K = o.K, rs = o.rs, cs = o.cs;
+  int* __restrict__ e_out = o.e;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (blockIdx.x == 0 && tid == 0 && fix_count) *fix_count = 0;
+  const int64_t r0 = (int64_t)(blk / o.tiles_k) * 32, k0 = (int64_t)(blk % o.tiles_k) * kScaleTK;
+  if (cs == 1) {
+    // warp w: rows w, w+8, w+16, w+24; lanes along K
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-      bad = __shfl_xor_sync(0xffffffffu, (int)bad, o) != 0 || bad;
+    for (int i = 0; i < 4; ++i) {
+      const int r = warp + 8 * i;
+      double amax = 0.0;
+      int bad = 0;
+      if (r0 + r < rows) {
+        const double* p = src + (r0 + r) * rs + k0;
+        double v[kScaleTK / 32];
+#pragma unroll
+        for (int j = 0; j < kScaleTK / 32; ++j) v[j] = (k0 + lane + 32 * j < K) ? __ldg(p + lane + 32 * j) : 0.0;
+#pragma unroll
+        for (int j = 0; j < kScaleTK / 32; ++j) {
+          bad |= !isfinite(v[j]);
+          amax = fmax(amax, fabs(v[j]));
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+      }
+      if (lane == 0) {
+        part_max[0][r] = amax;
+        part_bad[0][r] = bad;
+      }
     }
-    if (lane != 0) return;
+    __syncthreads();
+    if (tid >= 32) return;
+  } else {
+    // thread (slice w, row lane): 32 consecutive K of row lane; a warp reads
+    // 32 consecutive rows at each k
+    const int r = lane;
+    double amax = 0.0;
+    int bad = 0;
+    if (r0 + r < rows) {
+      const double* p = src + (r0 + r) * rs;
+      double v[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int64_t k = k0 + warp * 32 + j;
+        v[j] = k < K ? __ldg(p + k * cs) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        bad |= !isfinite(v[j]);
+        amax = fmax(amax, fabs(v[j]));
+      }
+    }
+    part_max[warp][r] = amax;
+    part_bad[warp][r] = bad;
+    __syncthreads();
+    if (tid >= 32) return;
+    for (int w = 1; w < 8; ++w) {
+      amax = fmax(amax, part_max[w][lane]);
+      bad |= part_bad[w][lane];
+    }
+    part_max[0][lane] = amax;
+    part_bad[0][lane] = bad;
   }
-  int e = 0;
-  if (bad)
-    e = kBadExp;
-  else if (amax > 0.0)
+  // warp 0: one row per lane
+  const double amax = part_max[0][lane];
+  if (r0 + lane >= rows) return;
+  if (part_bad[0][lane]) {
+    atomicMax(e_out + r0 + lane, kBadExp);
+  } else if (amax > 0.0) {
+    int e;
     (void)frexp(amax, &e);  // amax = m 2^e, m in [0.5, 1)
-  e_out[r] = e;
+    atomicMax(e_out + r0 + lane, e);
+  }
 }
+
+// The scale of a row as the digit and GEMM kernels use it (kBadExp aside):
+// an all-zero (or padding) row keeps kZeroExp and gets 0.
+__device__ __forceinline__ int used_exp(int e) { return e == kZeroExp ? 0 : e; }
 
 // Balanced base-256 digits of round(a * 2^(8S-1-e)), most significant first,
 // from the bit pattern of a (|a| < 2^e; integer operations only).
@@ -200,18 +285,24 @@ __device__ __forceinline__ void f64_digits(double a, int e, int (&d)[S]) {
 
 // Digit planes of one operand, written K-major into the arena: plane s of
 // row r at out[s * plane_stride + r * pitch + k], for every padded row
-// (< rows_pad) and padded k (< k_pad); zero outside rows x K.  A CTA takes
+// (< rows_pad) and padded k (< k_pad); zero outside rows x K.  G = 1 adds
+// plane S, the guard plane max(|D_0| - 1, 0).  One launch for both
+// operands (CTAs below a.blocks: A).  A CTA takes
 // 32 rows x 32 K (8 KB of FP64 staged in shared memory, read along whichever
 // side is contiguous); thread t then makes the digits of 4 consecutive K of
 // one row and writes 8 bytes per plane.
-template <int S>
-__global__ void __launch_bounds__(256) digits_kernel(const double* __restrict__ src, int64_t rows, int64_t K,
-                                                     int64_t rs, int64_t cs, const int* __restrict__ e_row,
-                                                     __nv_bfloat16* __restrict__ out, int64_t plane_stride,
-                                                     int64_t pitch, int tiles_k) {
+template <int S, int G>
+__global__ void __launch_bounds__(256) digits_kernel(const DgOperand oa, const DgOperand ob) {
   __shared__ double tile[32][33];
+  const bool is_a = (int)blockIdx.x < oa.blocks;
+  const DgOperand& o = is_a ? oa : ob;
+  const int blk = is_a ? (int)blockIdx.x : (int)blockIdx.x - oa.blocks;
+  const double* __restrict__ src = o.src;
+  const int64_t rows = o.rows, K = o.K, rs = o.rs, cs = o.cs, plane_stride = o.plane_stride, pitch = o.pitch;
+  const int* __restrict__ e_row = o.e;
+  __nv_bfloat16* __restrict__ out = o.out;
   const int tid = threadIdx.x;
-  const int64_t r0 = (int64_t)(blockIdx.x / tiles_k) * 32, k0 = (int64_t)(blockIdx.x % tiles_k) * 32;
+  const int64_t r0 = (int64_t)(blk / o.tiles_k) * 32, k0 = (int64_t)(blk % o.tiles_k) * 32;
   if (cs == 1) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -227,11 +318,11 @@ __global__ void __launch_bounds__(256) digits_kernel(const double* __restrict__ 
   }
   __syncthreads();
   const int r = tid >> 3, kq = (tid & 7) * 4;
-  const int e = e_row[r0 + r];
+  const int e = e_row[r0 + r] == kBadExp ? kBadExp : used_exp(e_row[r0 + r]);
   int d[4][S];
 #pragma unroll
   for (int j = 0; j < 4; ++j) f64_digits<S>(tile[r][kq + j], e, d[j]);
-  __nv_bfloat16* o = out + (r0 + r) * pitch + k0 + kq;
+  __nv_bfloat16* dst = out + (r0 + r) * pitch + k0 + kq;
 #pragma unroll
   for (int s = 0; s < S; ++s) {
     const __nv_bfloat162 h01 = __floats2bfloat162_rn((float)d[0][s], (float)d[1][s]);  // exact: |d| <= 128
@@ -239,7 +330,16 @@ __global__ void __launch_bounds__(256) digits_kernel(const double* __restrict__ 
     uint2 w;
     w.x = *reinterpret_cast<const uint32_t*>(&h01);
     w.y = *reinterpret_cast<const uint32_t*>(&h23);
-    *reinterpret_cast<uint2*>(o + s * plane_stride) = w;
+    *reinterpret_cast<uint2*>(dst + s * plane_stride) = w;
+  }
+  if constexpr (G) {  // guard plane: max(|D_0| - 1, 0) <= |x| 2^7
+    auto g = [](int d) { return (float)max(abs(d) - 1, 0); };
+    const __nv_bfloat162 h01 = __floats2bfloat162_rn(g(d[0][0]), g(d[1][0]));
+    const __nv_bfloat162 h23 = __floats2bfloat162_rn(g(d[2][0]), g(d[3][0]));
+    uint2 w;
+    w.x = *reinterpret_cast<const uint32_t*>(&h01);
+    w.y = *reinterpret_cast<const uint32_t*>(&h23);
+    *reinterpret_cast<uint2*>(dst + S * plane_stride) = w;
   }
 }
 
@@ -258,16 +358,16 @@ __device__ __forceinline__ void dg_tile(const DgProblem& p, int t, int& m0, int&
   n0 = (in_g / gm) * kBN;
 }
 
-template <int S>
+template <int S, int G>
 __global__ void __launch_bounds__(kThreads, 1)
     dgemm_digits_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                         const DgProblem p, int* __restrict__ err) {
-  using CF = DgCfg<S>;
+  using CF = DgCfg<S, G>;
   constexpr int ST = CF::kStages;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // stage st: A digit planes 0..S-1 (8 KB each), then B's (2 KB each)
+  // stage st: A planes 0..NP-1 (8 KB each), then B's (2 KB each)
   auto a_tile = [&](int st, int d) { return smem + (size_t)st * CF::kStageBytes + (size_t)d * CF::kATile; };
   auto b_tile = [&](int st) { return smem + (size_t)st * CF::kStageBytes + CF::kAStage; };
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
@@ -372,6 +472,10 @@ __global__ void __launch_bounds__(kThreads, 1)
               mma_f16(acc + 32u * d, sw64_kmajor_desc(smem_u32(a_tile(s, d)) + off), sw64_kmajor_desc(b0 + off),
                       idesc_bf16_f32(kBM, kBN * (S - d)), (chunk_first && kk == 0 && d == 0) ? 0u : 1u);
             }
+            if constexpr (G)  // guard plane x guard plane -> slot S
+              mma_f16(acc + 32u * S, sw64_kmajor_desc(smem_u32(a_tile(s, S)) + off),
+                      sw64_kmajor_desc(b0 + S * CF::kBTile + off), idesc_bf16_f32(kBM, kBN),
+                      (chunk_first && kk == 0) ? 0u : 1u);
           }
           mma_commit(&empty[s]);
           if (chunk_last) mma_commit(&tfull[b]);
@@ -398,8 +502,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       // sum_w G_w 2^(8(S-1-w)) = hi 2^32 + lo, exactly: groups w < S-4 go
       // into hi (shifted by 8(S-5-w)), the last four into lo (8(S-1-w))
       long long hi[16], lo[16];
+      int gsum[16];  // guard: sum of P(a) P(b) (saturating)
 #pragma unroll
-      for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0;
+      for (int j = 0; j < 16; ++j) {
+        hi[j] = lo[j] = 0;
+        gsum[j] = 0;
+      }
       auto fold = [&](int d, const float (&v)[16]) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -408,6 +516,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             hi[j] += g << (8 * (S - 5 - d));
           else
             lo[j] += g << (8 * (S - 1 - d));
+        }
+      };
+      auto take = [&](int slot, const float (&v)[16]) {
+        if (slot < S) {
+          fold(slot, v);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) gsum[j] = min(gsum[j] + __float2int_rn(v[j]), kGuardCap);
         }
       };
       for (int c = 0; c < nchunks; ++c, ++chunk_g) {
@@ -422,13 +538,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         const uint32_t tb = trow + (uint32_t)b * kBufCols;
 #pragma unroll
-        for (int d = 0; d < S; d += 2) {
+        for (int d = 0; d < S + G; d += 2) {  // slots d, d + 1 (slot S: the guard)
           float v0[16], v1[16];
           tmem_ld16(tb + 32u * d, v0);
-          if (d + 1 < S) tmem_ld16(tb + 32u * (d + 1), v1);
+          if (d + 1 < S + G) tmem_ld16(tb + 32u * (d + 1), v1);
           tmem_ld_wait();
-          fold(d, v0);
-          if (d + 1 < S) fold(d + 1, v1);
+          take(d, v0);
+          if (d + 1 < S + G) take(d + 1, v1);
         }
         tc_fence_before();
         __syncwarp();
@@ -437,14 +553,28 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ok) break;
       if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
       const int row = m0 + q * 32 + lane;
+      if constexpr (G) {
+        // every output of this warp's 32 x 16 block must pass, else the
+        // block goes to the FP64 fix-up and C is left alone here
+        bool pass = true;
+        if (row < p.M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (n0 + 16 * h + j < p.N && gsum[j] < kGuardMin) pass = false;
+        }
+        if (!__all_sync(0xffffffffu, pass)) {
+          if (lane == 0) p.fix_list[atomicAdd(p.fix_count, 1)] = t * kEpiWarps + (warp - 2);
+          continue;
+        }
+      }
       if (row < p.M) {
-        const int ei = p.ea[row];
+        const int ei = p.ea[row] == kBadExp ? kBadExp : used_exp(p.ea[row]);
         double* crow = p.C + (int64_t)row * p.rsc;
         const int cn = n0 + 16 * h;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           if (cn + j >= p.N) continue;
-          const int ej = p.eb[cn + j];
+          const int ej = p.eb[cn + j] == kBadExp ? kBadExp : used_exp(p.eb[cn + j]);
           // hi 2^32 + lo in units of 2^(e_i + f_j - 14 - 8(S-1))
           double r;
           if (ei == kBadExp || ej == kBadExp)
@@ -479,26 +609,60 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// FP64-pipe recomputation of the blocks the guard rejected: CTA i takes
+// list entries i, i + grid, ...; block (tile t, epilogue warp w) covers tile
+// rows 32 (w % 4) .. +31 and columns 16 ((w - 2) / 4) .. +15; thread
+// (row lane, column pair) sums its two outputs over k in order with fused
+// multiply-adds and adds them into C (the FP64 FMA kernel's arithmetic).
+__global__ void __launch_bounds__(256) dgemm_fixup_kernel(const DgProblem p) {
+  const int n = *p.fix_count;
+  const int lane = threadIdx.x & 31, pair = threadIdx.x >> 5;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const int id = p.fix_list[i];
+    const int t = id / kEpiWarps, w = 2 + id % kEpiWarps;
+    int m0, n0;
+    dg_tile(p, t, m0, n0);
+    const int row = m0 + 32 * (w & 3) + lane;
+    const int c0 = n0 + 16 * ((w - 2) >> 2) + 2 * pair;
+    if (row >= p.M) continue;
+    const double* a = p.A + (int64_t)row * p.rsa;
+    double s0 = 0.0, s1 = 0.0;
+    const bool has1 = c0 + 1 < p.N;
+    if (c0 < p.N) {
+      const double* b0 = p.B + (int64_t)c0 * p.csb;
+      for (int64_t k = 0; k < p.K; ++k) {
+        const double av = a[k * p.csa];
+        s0 = fma(av, b0[k * p.rsb], s0);
+        if (has1) s1 = fma(av, b0[k * p.rsb + p.csb], s1);
+      }
+      p.C[(int64_t)row * p.rsc + (int64_t)c0 * p.csc] += s0;
+      if (has1) p.C[(int64_t)row * p.rsc + (int64_t)(c0 + 1) * p.csc] += s1;
+    }
+  }
+}
+
 // ------------------------------------------------------------ host side
 inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-template <int S>
+template <int S, int G>
 void dg_setup(DeviceCtx* c) {
   static std::mutex mu;
   static bool done[64] = {false};
   std::lock_guard<std::mutex> lk(mu);
   if (!done[c->device & 63]) {
-    cudaFuncSetAttribute(dgemm_digits_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DgCfg<S>::kSmem);
+    cudaFuncSetAttribute(dgemm_digits_kernel<S, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DgCfg<S, G>::kSmem);
     done[c->device & 63] = true;
   }
 }
 
-template <int S>
+template <int S, int G>
 gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa,
                             int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
                             int64_t csc, cudaStream_t stream, int max_ctas) {
-  using CF = DgCfg<S>;
+  using CF = DgCfg<S, G>;
+  constexpr int NP = CF::NP;
   if (K > CF::kMaxK) {
     set_error("dgemm (FP64 digits): K = %lld exceeds %lld", (long long)K, (long long)CF::kMaxK);
     return GBBLAS_STATUS_NOT_SUPPORTED;
@@ -512,8 +676,10 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   const size_t off_eb = off_ea + align256(sizeof(int) * (size_t)Mp);
   const size_t off_a = off_eb + align256(sizeof(int) * (size_t)Np);
   const size_t a_plane = (size_t)(Mp * Kp), b_plane = (size_t)(Np * Kp);
-  const size_t off_b = off_a + align256((size_t)S * a_plane * sizeof(__nv_bfloat16));
-  const size_t bytes = off_b + align256((size_t)S * b_plane * sizeof(__nv_bfloat16));
+  const size_t off_b = off_a + align256((size_t)NP * a_plane * sizeof(__nv_bfloat16));
+  const int64_t tiles = (Mp / kBM) * (Np / kBN);
+  const size_t off_fix = off_b + align256((size_t)NP * b_plane * sizeof(__nv_bfloat16));
+  const size_t bytes = off_fix + (G ? align256(sizeof(int) * (size_t)(1 + tiles * kEpiWarps)) : 0);
   void* scratch = nullptr;
   GB_TRY(get_scratch(c, stream, bytes, &scratch));
   char* base = static_cast<char*>(scratch);
@@ -524,29 +690,34 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   int* err = reinterpret_cast<int*>(base + kErrWordOffset);
 
   // scales: rows of A over K; columns of B (element (n, k) = B[k*rsb + n*csb])
-  row_scale_kernel<<<(unsigned)(csa == 1 ? Mp / 8 : (Mp + 255) / 256), 256, 0, stream>>>(A, M, K, rsa, csa, Mp, ea);
-  GB_TRY(check_launch("row_scale_kernel(A)"));
-  row_scale_kernel<<<(unsigned)(rsb == 1 ? Np / 8 : (Np + 255) / 256), 256, 0, stream>>>(B, N, K, csb, rsb, Np, eb);
-  GB_TRY(check_launch("row_scale_kernel(B)"));
+  int* fix_count = G ? reinterpret_cast<int*>(base + off_fix) : nullptr;
+  GB_CUDA_TRY(cudaMemsetAsync(ea, 0x80, off_a - off_ea, stream));  // kZeroExp everywhere (ea and eb)
+  const int stk = (int)((K + kScaleTK - 1) / kScaleTK);
   const int tiles_k = (int)(Kp / 32);
-  digits_kernel<S><<<(unsigned)((Mp / 32) * tiles_k), 256, 0, stream>>>(A, M, K, rsa, csa, ea, da, (int64_t)a_plane,
-                                                                       Kp, tiles_k);
-  GB_TRY(check_launch("digits_kernel(A)"));
-  digits_kernel<S><<<(unsigned)((Np / 32) * tiles_k), 256, 0, stream>>>(B, N, K, csb, rsb, eb, db, (int64_t)b_plane,
-                                                                       Kp, tiles_k);
-  GB_TRY(check_launch("digits_kernel(B)"));
+  DgOperand oa{A, M, K, rsa, csa, ea, da, (int64_t)a_plane, Kp, stk, (int)((Mp / 32) * stk)};
+  DgOperand ob{B, N, K, csb, rsb, eb, db, (int64_t)b_plane, Kp, stk, (int)((Np / 32) * stk)};
+  if ((double)(Mp + Np) / 32 * tiles_k >= 2.0e9) {
+    set_error("dgemm (FP64 digits): operands too large for one preparation launch");
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  row_scale_kernel<<<(unsigned)(oa.blocks + ob.blocks), 256, 0, stream>>>(oa, ob, fix_count);
+  GB_TRY(check_launch("row_scale_kernel"));
+  oa.tiles_k = ob.tiles_k = tiles_k;
+  oa.blocks = (int)((Mp / 32) * tiles_k);
+  ob.blocks = (int)((Np / 32) * tiles_k);
+  digits_kernel<S, G><<<(unsigned)(oa.blocks + ob.blocks), 256, 0, stream>>>(oa, ob);
+  GB_TRY(check_launch("digits_kernel"));
 
   CUtensorMap ma, mb;
-  GB_TRY(make_map(&ma, da, (uint64_t)Mp, (uint64_t)Kp, (uint64_t)S, kBM, false, 64));
-  GB_TRY(make_map(&mb, db, (uint64_t)Np, (uint64_t)Kp, (uint64_t)S, kBN, false, 64));
+  GB_TRY(make_map(&ma, da, (uint64_t)Mp, (uint64_t)Kp, (uint64_t)NP, kBM, false, 64));
+  GB_TRY(make_map(&mb, db, (uint64_t)Np, (uint64_t)Kp, (uint64_t)NP, kBN, false, 64));
   DgProblem p;
   p.M = (int)M;
   p.N = (int)N;
   p.num_kt = (int)(Kp / kBK);
   p.tiles_m = (int)(Mp / kBM);
   p.tiles_n = (int)(Np / kBN);
-  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
-  if (tiles >= (1ll << 31)) {
+  if (tiles * kEpiWarps >= (1ll << 31)) {
     set_error("dgemm (FP64 digits): too many tiles");
     return GBBLAS_STATUS_NOT_SUPPORTED;
   }
@@ -556,11 +727,27 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   p.csc = csc;
   p.ea = ea;
   p.eb = eb;
-  dg_setup<S>(c);
+  p.fix_count = fix_count;  // cleared by row_scale_kernel
+  p.fix_list = G ? fix_count + 1 : nullptr;
+  p.A = A;
+  p.B = B;
+  p.rsa = rsa;
+  p.csa = csa;
+  p.rsb = rsb;
+  p.csb = csb;
+  p.K = K;
+  dg_setup<S, G>(c);
   int grid = (int)std::min<int64_t>(tiles, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  dgemm_digits_kernel<S><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, p, err);
-  return check_launch("dgemm_digits_kernel");
+  dgemm_digits_kernel<S, G><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, p, err);
+  GB_TRY(check_launch("dgemm_digits_kernel"));
+  if constexpr (G) {
+    // the rejected blocks (usually none: the kernel reads the count and returns)
+    dgemm_fixup_kernel<<<(unsigned)(max_ctas > 0 ? std::min(max_ctas, 2 * c->num_sms) : 2 * c->num_sms), 256, 0,
+                         stream>>>(p);
+    GB_TRY(check_launch("dgemm_fixup_kernel"));
+  }
+  return GBBLAS_STATUS_SUCCESS;
 }
 
 }  // namespace
@@ -569,24 +756,36 @@ int dgemm_digits_count(gbblas_accuracy acc) {
   return acc == GBBLAS_ACCURACY_FP64_DIGITS7 ? 7 : (acc == GBBLAS_ACCURACY_FP64_DIGITS8 ? 8 : 0);
 }
 
-int64_t dgemm_digits_max_k(int digits) { return digits == 8 ? DgCfg<8>::kMaxK : DgCfg<7>::kMaxK; }
+int64_t dgemm_digits_max_k(int digits) { return digits == 8 ? DgCfg<8, 0>::kMaxK : DgCfg<7, 0>::kMaxK; }
 
-void dgemm_digits_prepare(DeviceCtx* c) {
-  dg_setup<7>(c);
-  dg_setup<8>(c);
+// Scratch one call takes (scales, digit planes, fix-up list), as launch_digits lays it out.
+size_t dgemm_digits_scratch_bytes(int digits, bool guarded, int64_t M, int64_t N, int64_t K) {
+  const int64_t Mp = round_up(M, kBM), Np = round_up(N, kBN), Kp = round_up(K, kBK);
+  const int64_t np = digits + (guarded ? 1 : 0);
+  const int64_t tiles = (Mp / kBM) * (Np / kBN);
+  return kScratchZeroBytes + align256(sizeof(int) * (size_t)Mp) + align256(sizeof(int) * (size_t)Np) +
+         align256((size_t)(np * Mp * Kp) * 2) + align256((size_t)(np * Np * Kp) * 2) +
+         (guarded ? align256(sizeof(int) * (size_t)(1 + tiles * kEpiWarps)) : 0);
 }
 
-gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, int64_t M, int64_t N, int64_t K, const double* A,
-                                  int64_t rsa, int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C,
-                                  int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas) {
+void dgemm_digits_prepare(DeviceCtx* c) {
+  dg_setup<7, 0>(c);
+  dg_setup<8, 0>(c);
+  dg_setup<7, 1>(c);
+}
+
+gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, bool guarded, int64_t M, int64_t N, int64_t K,
+                                  const double* A, int64_t rsa, int64_t csa, const double* B, int64_t rsb,
+                                  int64_t csb, double* C, int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
-  switch (digits) {
-    case 7: return launch_digits<7>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
-    case 8: return launch_digits<8>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
-    default:
-      set_error("dgemm (FP64 digits): %d digits not supported (7 or 8)", digits);
-      return GBBLAS_STATUS_INVALID_VALUE;
-  }
+  if (guarded && digits == 7)
+    return launch_digits<7, 1>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+  if (!guarded && digits == 7)
+    return launch_digits<7, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+  if (!guarded && digits == 8)
+    return launch_digits<8, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+  set_error("dgemm (FP64 digits): %d digits%s not supported", digits, guarded ? " with the guard" : "");
+  return GBBLAS_STATUS_INVALID_VALUE;
 }
 
 }  // namespace gbblas

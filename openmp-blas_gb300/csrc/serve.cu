@@ -39,6 +39,8 @@ struct Req {
   int64_t bytes = 0;
   double est_us = 0.0;  // estimated GPU time
   bool heavy = false;
+  int f64_digits = 0;         // double GEMM on tensor-core digits (0: the FP64 pipes)
+  bool f64_guarded = false;   // ... in the guarded form
   Clock::time_point t_submit, t_done;
   bool done = false;
   gbblas_status status = GBBLAS_STATUS_SUCCESS;
@@ -62,15 +64,31 @@ int server_mode(int32_t acc) {
   return acc == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode((gbblas_accuracy)acc);
 }
 
+// Tensor-core digits of a double GEMM request (0: the FP64 pipes): FP64 means
+// the pipes, FP64_DIGITS7 / 8 those digits, anything else (the float-only
+// modes included) the library default - gbblas_dgemm's guarded 7-digit
+// scheme where the shape suits.
+int server_f64_digits(const gbblas_request& r, int sms, bool* guarded) {
+  *guarded = false;
+  if (r.op != GBBLAS_OP_MTM || r.dtype != GBBLAS_F64) return 0;
+  if (const int d = dgemm_digits_count((gbblas_accuracy)r.accuracy)) return d;
+  if (r.accuracy != GBBLAS_ACCURACY_FP64 && dgemm_auto_digits(r.M, r.N, r.K, sms)) {
+    *guarded = true;
+    return 7;
+  }
+  return 0;
+}
+
 // Device bytes a request holds while in flight: operands, result, and the
 // operand arena (BF16 pieces or FP8 values and scales) of a tensor-core GEMM.
-int64_t working_set(const gbblas_request& r) {
+int64_t working_set(const gbblas_request& r, int f64_digits, bool f64_guarded) {
   const int64_t s = r.dtype == GBBLAS_F64 ? 8 : 4;
   switch (r.op) {
     case GBBLAS_OP_MTM: {
       int64_t b = (r.M * r.K + r.K * r.N + r.M * r.N) * s;
       if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32)
         b += (int64_t)tc_arena_bytes(server_mode(r.accuracy), r.M, r.N, r.K);
+      if (f64_digits) b += (int64_t)dgemm_digits_scratch_bytes(f64_digits, f64_guarded, r.M, r.N, r.K);
       return b;
     }
     case GBBLAS_OP_MTV:
@@ -83,14 +101,16 @@ int64_t working_set(const gbblas_request& r) {
 
 // Estimated GPU time (us) of a request from its flops / bytes and the rate of
 // the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP8
-// ~600, FP32 FMA ~55, FP64 ~1.2 TFLOP/s; streaming ~6 TB/s; FP64 GEMV ~1.1
-// TFLOP/s).
-double estimate_us(const gbblas_request& r) {
+// ~600, FP32 FMA ~55, FP64 pipes ~1.2 TFLOP/s, FP64 as tensor-core digits
+// ~38 TFLOP/s after ~50 us of operand preparation and launches; streaming
+// ~6 TB/s; FP64 GEMV ~1.1 TFLOP/s).
+double estimate_us(const gbblas_request& r, int f64_digits) {
   const double launch = 5.0;
   switch (r.op) {
     case GBBLAS_OP_MTM: {
       const double fl = 2.0 * (double)r.M * (double)r.N * (double)r.K;
       double rate;  // flop per us
+      if (f64_digits) return 50.0 + fl / 38e6;
       if (r.dtype == GBBLAS_F64)
         rate = 1.2e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP32)
@@ -176,7 +196,11 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
     if (r.op == GBBLAS_OP_MTM) {
       const int64_t rsa = row ? r.K : 1, csa = row ? 1 : r.M, rsb = row ? r.N : 1, csb = row ? 1 : r.K,
                     rsc = row ? r.N : 1, csc = row ? 1 : r.M;
-      if (r.dtype == GBBLAS_F64) {
+      if (q->f64_digits) {
+        note(launch_dgemm_digits(c, q->f64_digits, q->f64_guarded, r.M, r.N, r.K,
+                                 static_cast<const double*>(r.A), rsa, csa, static_cast<const double*>(r.B), rsb, csb,
+                                 static_cast<double*>(r.C), rsc, csc, st, cap));
+      } else if (r.dtype == GBBLAS_F64) {
         note(launch_gemm_fma<double>(c, r.M, r.N, r.K, static_cast<const double*>(r.A), rsa, csa,
                                      static_cast<const double*>(r.B), rsb, csb, static_cast<double*>(r.C), rsc,
                                      csc, st, cap));
@@ -419,7 +443,8 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
     return GBBLAS_STATUS_INVALID_VALUE;
   }
   if (r->op < GBBLAS_OP_MTM || r->op > GBBLAS_OP_DOT || (r->dtype != GBBLAS_F32 && r->dtype != GBBLAS_F64) ||
-      (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 || r->accuracy > 4) {
+      (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 ||
+      r->accuracy > (r->dtype == GBBLAS_F64 ? 7 : 4)) {
     set_error("gbblas_server_submit: bad op, dtype, layout or accuracy");
     return GBBLAS_STATUS_INVALID_VALUE;
   }
@@ -429,8 +454,9 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
   }
   auto q = std::make_unique<Req>();
   q->r = *r;
-  q->bytes = working_set(*r);
-  q->est_us = estimate_us(*r);
+  q->f64_digits = server_f64_digits(*r, s->ctx->num_sms, &q->f64_guarded);
+  q->bytes = working_set(*r, q->f64_digits, q->f64_guarded);
+  q->est_us = estimate_us(*r, q->f64_digits);
   q->heavy = q->est_us > (double)s->cfg.heavy_us;
   if (q->bytes > s->cfg.budget_bytes) {
     set_error("gbblas_server_submit: request needs %lld bytes, the budget is %lld", (long long)q->bytes,

@@ -179,7 +179,8 @@ def _dev(t) -> int:
 def gemm(A, B, C, accuracy: int = ACCURACY_FP32, stream=None):
     """C += A @ B on device tensors of any strides (2-D torch tensors).
     float32: `accuracy` is one of ACCURACY_FP32 .. ACCURACY_BF16X6; float64:
-    ACCURACY_FP32 or ACCURACY_FP64 (the FP64 pipes) or ACCURACY_FP64_DIGITS7 / 8."""
+    ACCURACY_FP32 (gbblas_dgemm, the library default), ACCURACY_AUTO,
+    ACCURACY_FP64 (the FP64 pipes) or ACCURACY_FP64_DIGITS7 / 8."""
     M, K = A.shape
     N = B.shape[1]
     p = _pfx(A)
@@ -187,7 +188,7 @@ def gemm(A, B, C, accuracy: int = ACCURACY_FP32, stream=None):
             _dev(C), C.stride(0), C.stride(1)]
     if p == "s":
         call("gbblas_sgemm", *args, accuracy, _stream_ptr(stream))
-    elif accuracy in (ACCURACY_FP32, ACCURACY_FP64):
+    elif accuracy == ACCURACY_FP32:
         call("gbblas_dgemm", *args, _stream_ptr(stream))
     else:
         call("gbblas_dgemm_ex", *args, accuracy, _stream_ptr(stream))

@@ -92,6 +92,8 @@ def lib():
             f.restype = None
         L.orc_sgemm_sample_exact.argtypes = [_c_size, _vp, _c_pd, _c_pd, _vp, _c_pd, _c_pd, _c_size, _vp, _vp, _vp, _vp]
         L.orc_sgemm_sample_exact.restype = None
+        L.orc_dgemm_sample_exact.argtypes = [_c_size, _vp, _c_pd, _c_pd, _vp, _c_pd, _c_pd, _c_size, _vp, _vp, _vp, _vp]
+        L.orc_dgemm_sample_exact.restype = None
         L.orc_cache_info.argtypes = [_vp, _vp, _vp]
         L.orc_partition.argtypes = [_c_size, ctypes.c_int, _vp]
         L.orc_max_threads.restype = ctypes.c_int
@@ -241,12 +243,13 @@ def dot_exact(a: np.ndarray, b: np.ndarray):
 
 
 def gemm_sample_exact(K, a, rsa, csa, b, rsb, csb, rows, cols):
-    """Sampled entries of A@B and |A|@|B| in long double (float inputs)."""
+    """Sampled entries of A@B and |A|@|B| in long double (float or double inputs)."""
     rows = np.ascontiguousarray(rows, dtype=np.int64)
     cols = np.ascontiguousarray(cols, dtype=np.int64)
     out = np.empty(rows.size, np.float64)
     aout = np.empty(rows.size, np.float64)
-    lib().orc_sgemm_sample_exact(K, _ptr(a), rsa, csa, _ptr(b), rsb, csb, rows.size, _ptr(rows), _ptr(cols), _ptr(out), _ptr(aout))
+    fn = lib().orc_dgemm_sample_exact if a.dtype == np.float64 else lib().orc_sgemm_sample_exact
+    fn(K, _ptr(a), rsa, csa, _ptr(b), rsb, csb, rows.size, _ptr(rows), _ptr(cols), _ptr(out), _ptr(aout))
     return out, aout
 
 

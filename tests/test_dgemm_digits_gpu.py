@@ -210,3 +210,95 @@ def test_k_limit_and_bad_accuracy(cuda):
         gbblas.call("gbblas_dgemm_ex", 1, 1, (1 << 20) + 1, p, 0, 0, p, 0, 0, p, 1, 1, D7, None)
     with pytest.raises(gbblas.GbblasError):
         gbblas.call("gbblas_dgemm_ex", 1, 1, 1, p, 1, 1, p, 1, 1, p, 1, 1, 4, None)
+
+
+# ------------------------------------------------- guarded form (AUTO, the default)
+AUTO = 3
+FP64 = 5
+
+
+def run_any(torch, A, B, C0, accuracy, fn="gbblas_dgemm_ex"):
+    import gbblas
+    M, K = A.shape
+    N = B.shape[1]
+    tA = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    tB = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    tC = torch.from_numpy(C0.copy()).cuda()
+    args = [M, N, K, tA.data_ptr(), K, 1, tB.data_ptr(), N, 1, tC.data_ptr(), N, 1]
+    if fn == "gbblas_dgemm_ex":
+        args.append(accuracy)
+    gbblas.call(fn, *args, None)
+    gbblas.call("gbblas_check_stream", None)
+    return tC.cpu().numpy()
+
+
+def fp64_tol(A, B, C0):
+    K = A.shape[1]
+    return 2 * max(K, 1) * np.finfo(np.float64).eps * (np.abs(A) @ np.abs(B) + np.abs(C0)) + np.finfo(np.float64).tiny
+
+
+def test_auto_equals_digits_where_the_guard_passes(cuda):
+    """U[-1,1), K >= 32: every block passes, and the guarded result is the
+    7-digit result bit for bit (the same digit products in the same order)."""
+    rng = np.random.default_rng(21)
+    M, N, K = 300, 170, 600  # 2^24.9 multiply-adds: AUTO takes the digits
+    A = rng.uniform(-1, 1, (M, K))
+    B = rng.uniform(-1, 1, (K, N))
+    C0 = rng.uniform(-1, 1, (M, N))
+    np.testing.assert_array_equal(run_any(cuda, A, B, C0, AUTO), run_any(cuda, A, B, C0, D7))
+
+
+def test_guard_recomputes_blocks_the_digits_would_get_wrong(cuda):
+    """Rows 0..39 of A carry one huge entry (2^40) against a zero row of B:
+    the row scale 2^41 leaves those rows' other entries only their last
+    digits, so the unguarded digits miss the FP64 bound there; the guard
+    sends exactly those blocks to the FP64 pipes."""
+    rng = np.random.default_rng(22)
+    M, N, K = 256, 96, 512
+    A = rng.uniform(-1, 1, (M, K))
+    B = rng.uniform(-1, 1, (K, N))
+    A[:40, 0] = 2.0 ** 40
+    B[0, :] = 0.0
+    C0 = np.zeros((M, N))
+    tol = fp64_tol(A, B, C0)
+    ref = O.gemm(A, B, C0, 1, 1, 1)
+    raw = run_any(cuda, A, B, C0, D7)
+    assert (np.abs(raw - ref)[:40] > tol[:40]).any(), "the case must defeat the unguarded digits"
+    got = run_any(cuda, A, B, C0, AUTO)
+    assert (np.abs(got - ref) <= tol).all()
+    # rows 64.. (whole blocks without a huge entry) keep the digit result
+    np.testing.assert_array_equal(got[64:], raw[64:])
+
+
+def test_small_k_and_small_shapes_use_fp64_pipes(cuda):
+    rng = np.random.default_rng(23)
+    # K < 32, or shapes the FP64 pipes finish before the digit path's ~50 us
+    # of preparation (few multiply-adds per 64 x 64 tile)
+    for (M, N, K) in [(300, 200, 31), (64, 64, 40), (32, 32, 64), (1, 5, 3)]:
+        A = rng.uniform(-1, 1, (M, K))
+        B = rng.uniform(-1, 1, (K, N))
+        C0 = rng.uniform(-1, 1, (M, N))
+        np.testing.assert_array_equal(run_any(cuda, A, B, C0, AUTO), run_any(cuda, A, B, C0, FP64))
+
+
+def test_dgemm_default_is_auto_and_env_forces_fp64(cuda, monkeypatch):
+    rng = np.random.default_rng(24)
+    M, N, K = 256, 128, 256
+    A = rng.uniform(-1, 1, (M, K))
+    B = rng.uniform(-1, 1, (K, N))
+    C0 = np.zeros((M, N))
+    np.testing.assert_array_equal(run_any(cuda, A, B, C0, None, fn="gbblas_dgemm"), run_any(cuda, A, B, C0, AUTO))
+    monkeypatch.setenv("GBBLAS_DGEMM_FP64", "1")
+    np.testing.assert_array_equal(run_any(cuda, A, B, C0, None, fn="gbblas_dgemm"), run_any(cuda, A, B, C0, FP64))
+
+
+@pytest.mark.parametrize("la,lb,lc", [(0, 0, 0), (1, 0, 1), (0, 1, 0)])
+def test_auto_layouts_within_fp64_bound(cuda, la, lb, lc):
+    rng = np.random.default_rng(25 + la + 2 * lb + 4 * lc)
+    M, N, K = 257, 95, 700
+    A = rng.uniform(-1, 1, (M, K)) * np.ldexp(1.0, rng.integers(-10, 11, (M, K)))
+    B = rng.uniform(-1, 1, (K, N)) * np.ldexp(1.0, rng.integers(-10, 11, (K, N)))
+    C0 = rng.uniform(-1, 1, (M, N))
+    got = run(cuda, A, B, C0, la, lb, lc, accuracy=AUTO)
+    ref = O.gemm(A, B, C0, la, lb, lc)
+    assert (np.abs(got - ref) <= fp64_tol(A, B, C0)).all()

@@ -167,3 +167,26 @@ def test_server_pool_alloc(cuda):
     for p in (pa, pb, pr):
         srv.free(p)
     srv.close()
+
+
+def test_server_f64_gemm_on_tensor_core_digits(cuda):
+    """float64 GEMMs large enough for the digit scheme (AUTO: guarded, within
+    the FP64 bound; FP64_DIGITS7 explicitly) beside float work: the same
+    bits alone and in the mix."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(7)
+    cases = [ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 1, (600, 520, 400), AUTO),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 0, (384, 700, 256), AUTO),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 1, (300, 200, 500), AUTO),
+             ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F64, 1, (700, 900))]
+    srv = gbblas.Server(streams=4, max_group=16)
+    for c in cases:
+        srv.wait(srv.submit(c.request()))
+    alone = [c.outs[-1] for c in cases]
+    reqs = [c.request() for c in cases]
+    srv.run_trace(reqs, np.zeros(len(reqs)))
+    for c, a in zip(cases, alone):
+        c.check(a)
+        assert torch.equal(a, c.outs[-1]), f"alone != mix for {c.kind} {c.dims}"
+    srv.close()
