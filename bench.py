@@ -633,8 +633,9 @@ def run_precision(args):
 def run_f64(args):
     """Double-precision GEMM, M = N = K = --gemm-n (8192) from float64
     operands on two input sets (U[-1,1) and wide-range s*m*2^e, e in
-    [-10, 10]): the FP64 pipes (FMA kernel) and the Ozaki scheme on the BF16
-    tensor cores with 7 and 8 digits.  TFLOP/s of 2*M*N*K algorithmic flops,
+    [-10, 10]): the library default (AUTO: the guarded 7-digit scheme at
+    this size), the FP64 pipes (FMA kernel) and the unguarded Ozaki scheme on
+    the BF16 tensor cores with 7 and 8 digits.  TFLOP/s of 2*M*N*K algorithmic flops,
     max / mean relative and normwise error against long-double dots on
     sampled entries.  One JSON line per (path, set)."""
     import numpy as np
@@ -667,7 +668,7 @@ def run_f64(args):
             A, B = wide(), wide()
         An, Bn = A.cpu().numpy(), B.cpu().numpy()
         exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
-        for path, acc, products in (("digits7", 6, 28), ("digits8", 7, 36), ("fp64", 5, None)):
+        for path, acc, products in (("auto", 3, 29), ("digits7", 6, 28), ("digits8", 7, 36), ("fp64", 5, None)):
             if path not in args.f64_paths.split(","):
                 continue
             C = torch.zeros(n, n, device="cuda", dtype=torch.float64)
@@ -1315,7 +1316,7 @@ def main():
     ap.add_argument("--paths", default="bf16x3,bf16x6,fp8,fp32",
                     help="precision workload: comma-separated GEMM paths to run")
     ap.add_argument("--sets", default="uniform,wide", help="precision workload: input sets to run")
-    ap.add_argument("--f64-paths", default="digits7,digits8,fp64",
+    ap.add_argument("--f64-paths", default="auto,digits7,digits8,fp64",
                     help="f64 workload: comma-separated double-precision GEMM paths to run")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)

@@ -86,12 +86,16 @@ constexpr int kZeroExp = (int)0x80808080;          // scale of an all-zero row (
 template <int S, int G>
 struct DgCfg {
   static_assert(S >= 4 && S + G <= 8, "4 to 8 digits, and a free TMEM slot for the guard");
-  static constexpr int NP = S + G;              // planes per operand
+  static constexpr int NP = S + G;              // planes per operand in the arena
   static constexpr uint32_t kATile = kBM * 64;  // one plane of A: 128 rows x 64 bytes
   static constexpr uint32_t kBTile = kBN * 64;  // one of B^T: 32 rows x 64 bytes
-  static constexpr uint32_t kAStage = NP * kATile;
-  static constexpr uint32_t kBStage = NP * kBTile;
+  static constexpr uint32_t kAStage = S * kATile;
+  static constexpr uint32_t kBStage = S * kBTile;
   static constexpr uint32_t kStageBytes = kAStage + kBStage;
+  // the guard planes' 32 K at the start of each chunk, in a slot of their own
+  // (a lower bound over part of K is still a lower bound; the digit stages
+  // keep their size, so three of them still fit)
+  static constexpr uint32_t kGuardBytes = G ? kATile + kBTile : 0;
   // stages per TMEM chunk: a group's sum over the chunk stays below 2^24
   // (S * chunk * 2^14 with chunk = 128 K for S <= 7, 64 K for S = 8)
   static constexpr int kChunk = S <= 7 ? 4 : 2;
@@ -99,13 +103,13 @@ struct DgCfg {
   // less than 2^48 to hi and to lo)
   static constexpr int64_t kMaxK = 1 << 20;
   static constexpr size_t kBarBytes = 256;
-  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes) / kStageBytes);
+  static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kGuardBytes) / kStageBytes);
   static constexpr int kStages = kStagesFit > 4 ? 4 : kStagesFit;
-  static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + kBarBytes;
+  static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + kGuardBytes + kBarBytes;
   static_assert(kStages >= 2, "need a double-buffered stage ring");
   static_assert((uint64_t)S * kChunk * kBK * 16384 < (1u << 24), "chunk sums must stay exact in FP32");
   static_assert(kStageBytes % 1024 == 0, "stages stay 1024-byte aligned");
-  static_assert((2 * 4 + 2 * 2 + 1) * 8 + 8 <= kBarBytes, "barrier area too small");
+  static_assert((2 * 4 + 2 * 2 + 2 + 1) * 8 + 8 <= kBarBytes, "barrier area too small");
 };
 
 // One GEMM (device-side view).
@@ -361,21 +365,27 @@ __device__ __forceinline__ void dg_tile(const DgProblem& p, int t, int& m0, int&
 template <int S, int G>
 __global__ void __launch_bounds__(kThreads, 1)
     dgemm_digits_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
+                        const __grid_constant__ CUtensorMap tm_ga, const __grid_constant__ CUtensorMap tm_gb,
                         const DgProblem p, int* __restrict__ err) {
   using CF = DgCfg<S, G>;
   constexpr int ST = CF::kStages;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // stage st: A planes 0..NP-1 (8 KB each), then B's (2 KB each)
+  // stage st: A digit planes 0..S-1 (8 KB each), then B's (2 KB each); after
+  // the stages the guard slot (G: A's guard tile, then B's)
   auto a_tile = [&](int st, int d) { return smem + (size_t)st * CF::kStageBytes + (size_t)d * CF::kATile; };
   auto b_tile = [&](int st) { return smem + (size_t)st * CF::kStageBytes + CF::kAStage; };
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes);
+  unsigned char* guard_a = smem + (size_t)ST * CF::kStageBytes;
+  unsigned char* guard_b = guard_a + CF::kATile;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes + CF::kGuardBytes);
   uint64_t* full = bars;        // [ST]  TMA -> MMA (both producers)
   uint64_t* empty = full + 4;   // [ST]  MMA -> TMA
   uint64_t* tfull = empty + 4;  // [2]   MMA -> epilogue: chunk in TMEM buffer b
   uint64_t* tempty = tfull + 2;  // [2]  epilogue -> MMA: buffer b drained
-  uint64_t* accf = tempty + 2;   // [1]  every MMA of this CTA finished
+  uint64_t* gfull = tempty + 2;  // [1]  TMA -> MMA: the guard slot (both producers)
+  uint64_t* gempty = gfull + 1;  // [1]  MMA -> TMA
+  uint64_t* accf = gempty + 1;   // [1]  every MMA of this CTA finished
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accf + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
@@ -389,11 +399,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], kEpiWarps);
     }
+    mbar_init(gfull, 2);
+    mbar_init(gempty, 1);
     mbar_init(accf, 1);
     *abort_flag = 0;
     fence_mbar_init();
     prefetch_tensormap(&tm_a);
     prefetch_tensormap(&tm_b);
+    if (G) {
+      prefetch_tensormap(&tm_ga);
+      prefetch_tensormap(&tm_gb);
+    }
   }
   if (warp == 1) {
     tmem_alloc(tmem_slot, 512);
@@ -412,12 +428,29 @@ __global__ void __launch_bounds__(kThreads, 1)
   if ((warp == 0 || warp == kBProdWarp) && lane == 0) {
     // producers: warp 0 brings A's digit planes, warp 10 B's, into the same stages
     const bool is_a = warp == 0;
-    int n_issued = 0;
+    int n_issued = 0, g_issued = 0;
     bool stop = false;
     for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
       int m0, n0;
       dg_tile(p, t, m0, n0);
       for (int kt = 0; kt < p.num_kt; ++kt) {
+        if (G && kt % CF::kChunk == 0) {
+          // the guard planes' first 32 K of this chunk, once the MMAs of the
+          // previous chunk's guard product have read the slot
+          if (g_issued > 0 && !mbar_wait_bounded(gempty, (g_issued - 1) & 1, abort_flag, kWaitLimitNs)) {
+            fail();
+            stop = true;
+            break;
+          }
+          if (is_a) {
+            mbar_arrive_expect_tx(gfull, CF::kATile);
+            tma_load_3d(guard_a, &tm_ga, gfull, kt * kBK, m0, 0);
+          } else {
+            mbar_arrive_expect_tx(gfull, CF::kBTile);
+            tma_load_3d(guard_b, &tm_gb, gfull, kt * kBK, n0, 0);
+          }
+          ++g_issued;
+        }
         const int s = n_issued % ST, round = n_issued / ST;
         if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
           fail();
@@ -437,7 +470,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (is_a) issued = n_issued;
   } else if (warp == 1) {
     if (lane == 0) {
-      int consumed = 0, chunk_g = 0;
+      int consumed = 0, chunk_g = 0, g_used = 0;
       bool stop = false;
       for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
         for (int kt = 0; kt < p.num_kt; ++kt) {
@@ -462,6 +495,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           tc_fence_after();
           const uint32_t acc = tmem + (uint32_t)b * kBufCols;
           const uint32_t b0 = smem_u32(b_tile(s));
+          if (G && chunk_first) {
+            // guard plane x guard plane over the chunk's first 32 K -> slot S
+            if (!mbar_wait_bounded(gfull, g_used & 1, abort_flag, kWaitLimitNs)) {
+              fail();
+              stop = true;
+              break;
+            }
+            tc_fence_after();
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk)
+              mma_f16(acc + 32u * S, sw64_kmajor_desc(smem_u32(guard_a) + kk * 32),
+                      sw64_kmajor_desc(smem_u32(guard_b) + kk * 32), idesc_bf16_f32(kBM, kBN), kk == 0 ? 0u : 1u);
+            mma_commit(gempty);
+            ++g_used;
+          }
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
             const uint32_t off = kk * 32;  // 16 BF16 of K inside the swizzled 64-byte row
@@ -472,10 +520,6 @@ __global__ void __launch_bounds__(kThreads, 1)
               mma_f16(acc + 32u * d, sw64_kmajor_desc(smem_u32(a_tile(s, d)) + off), sw64_kmajor_desc(b0 + off),
                       idesc_bf16_f32(kBM, kBN * (S - d)), (chunk_first && kk == 0 && d == 0) ? 0u : 1u);
             }
-            if constexpr (G)  // guard plane x guard plane -> slot S
-              mma_f16(acc + 32u * S, sw64_kmajor_desc(smem_u32(a_tile(s, S)) + off),
-                      sw64_kmajor_desc(b0 + S * CF::kBTile + off), idesc_bf16_f32(kBM, kBN),
-                      (chunk_first && kk == 0) ? 0u : 1u);
           }
           mma_commit(&empty[s]);
           if (chunk_last) mma_commit(&tfull[b]);
@@ -709,8 +753,13 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   GB_TRY(check_launch("digits_kernel"));
 
   CUtensorMap ma, mb;
-  GB_TRY(make_map(&ma, da, (uint64_t)Mp, (uint64_t)Kp, (uint64_t)NP, kBM, false, 64));
-  GB_TRY(make_map(&mb, db, (uint64_t)Np, (uint64_t)Kp, (uint64_t)NP, kBN, false, 64));
+  GB_TRY(make_map(&ma, da, (uint64_t)Mp, (uint64_t)Kp, (uint64_t)S, kBM, false, 64));
+  GB_TRY(make_map(&mb, db, (uint64_t)Np, (uint64_t)Kp, (uint64_t)S, kBN, false, 64));
+  CUtensorMap mga = ma, mgb = mb;  // the guard planes (plane S of each arena)
+  if (G) {
+    GB_TRY(make_map(&mga, da + (size_t)S * a_plane, (uint64_t)Mp, (uint64_t)Kp, 1, kBM, false, 64));
+    GB_TRY(make_map(&mgb, db + (size_t)S * b_plane, (uint64_t)Np, (uint64_t)Kp, 1, kBN, false, 64));
+  }
   DgProblem p;
   p.M = (int)M;
   p.N = (int)N;
@@ -739,7 +788,7 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   dg_setup<S, G>(c);
   int grid = (int)std::min<int64_t>(tiles, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  dgemm_digits_kernel<S, G><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, p, err);
+  dgemm_digits_kernel<S, G><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, mga, mgb, p, err);
   GB_TRY(check_launch("dgemm_digits_kernel"));
   if constexpr (G) {
     // the rejected blocks (usually none: the kernel reads the count and returns)
