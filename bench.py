@@ -325,6 +325,54 @@ def gemm_headline(dev, sp):
     return out
 
 
+def dgemm_headline(dev, sp):
+    """Double-precision GEMM beside the bandwidth line (outside the timed
+    region): C = A*B at M = N = K = 8192 from float64 U[-1,1) (seed 4), the
+    library default (AUTO: exact BF16 digit products on the tensor cores,
+    guarded to the FP64 pipes' error bound) against the FP64 pipes; CUDA
+    events over 3 calls (1 on the pipes) after 1 warm-up; max relative error
+    against long-double dots on 256 sampled entries.  The two-input-set
+    report with the unguarded digit paths is `--workload f64`."""
+    import numpy as np
+    import torch
+
+    import gbblas
+    from oracle import oracle as O
+    n = 8192
+    g = torch.Generator(device=dev).manual_seed(4)
+    A = torch.rand(n, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1
+    B = torch.rand(n, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1
+    C = torch.zeros(n, n, device=dev, dtype=torch.float64)
+    rng = np.random.default_rng(4)
+    rows, cols = rng.integers(0, n, 256), rng.integers(0, n, 256)
+    exact, _ = O.gemm_sample_exact(n, A.cpu().numpy(), n, 1, B.cpu().numpy(), n, 1, rows, cols)
+    out = {"config": "M=N=K=8192 float64 U[-1,1) seed 4, 2*M*N*K flops", "unit": "TFLOP/s"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for path, acc, reps in (("auto_tensor_digits", 3, 3), ("fp64_pipes", 5, 1)):
+        def call():
+            gbblas.call("gbblas_dgemm_ex", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1, acc,
+                        sp)
+        call()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        gbblas.call("gbblas_check_stream", sp)
+        ms = e0.elapsed_time(e1) / reps
+        C.zero_()
+        call()
+        got = C.cpu().numpy()[rows, cols]
+        rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
+        out[path] = {"value": round(2.0 * n ** 3 / (ms / 1e3) / 1e12, 3), "ms": round(ms, 3),
+                     "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean())}
+    out["digits_over_pipes"] = round(out["auto_tensor_digits"]["value"] / out["fp64_pipes"]["value"], 1)
+    del A, B, C
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -477,9 +525,10 @@ def run_gpu(args):
                "sample": f"{len(times)} full steps (all four calls at full size) after 1 warm-up, "
                          f"mean {statistics.mean(times) * 1e3:.1f} ms/step, OpenMP on all host cores"}
 
-    gemm = None
+    gemm = dgemm = None
     if rank == 0 and not args.no_gemm:
         gemm = gemm_headline(dev, sp)
+        dgemm = dgemm_headline(dev, sp)
 
     if rank == 0:
         line = {
@@ -497,6 +546,7 @@ def run_gpu(args):
             "clocks": clocks,
             "results": results,
             "fp32_accurate_gemm": gemm,
+            "fp64_gemm": dgemm,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
