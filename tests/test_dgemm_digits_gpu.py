@@ -302,3 +302,60 @@ def test_auto_layouts_within_fp64_bound(cuda, la, lb, lc):
     got = run(cuda, A, B, C0, la, lb, lc, accuracy=AUTO)
     ref = O.gemm(A, B, C0, la, lb, lc)
     assert (np.abs(got - ref) <= fp64_tol(A, B, C0)).all()
+
+
+# ------------------------------------------------- bit equality with the digit model
+from oracle import ozaki as OZ  # noqa: E402
+
+
+def operands(rng, M, N, K, kind):
+    if kind == "uniform":
+        return rng.uniform(-1, 1, (M, K)), rng.uniform(-1, 1, (K, N))
+    if kind == "wide":
+        def w(shape):
+            return rng.choice([-1.0, 1.0], shape) * rng.uniform(1, 2, shape) * np.ldexp(1.0, rng.integers(-10, 11, shape))
+        return w((M, K)), w((K, N))
+    if kind == "scaled":  # rows / columns 2^-300 .. 2^300 apart, one zero row, one Inf row, one NaN column
+        A = rng.uniform(-1, 1, (M, K)) * np.ldexp(1.0, rng.integers(-300, 301, M))[:, None]
+        B = rng.uniform(-1, 1, (K, N)) * np.ldexp(1.0, rng.integers(-300, 301, N))[None, :]
+        A[M // 2] = 0.0
+        A[1, K // 3] = np.inf
+        B[K // 2, N - 1] = np.nan
+        return A, B
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("kind", ["uniform", "wide", "scaled"])
+def test_bit_exact_against_digit_model(cuda, mode, kind):
+    """Unguarded 7 / 8 digits: the GPU result equals the oracle's integer
+    model of the scheme (oracle/ozaki.py) bit for bit, NaNs included."""
+    rng = np.random.default_rng(31)
+    for (M, N, K), (la, lb, lc) in [((129, 33, 300), (1, 1, 1)), ((200, 70, 513), (0, 1, 0)),
+                                    ((64, 96, 128), (1, 0, 1)), ((5, 7, 33), (0, 0, 1))]:
+        A, B = operands(rng, M, N, K, kind)
+        C0 = rng.uniform(-1, 1, (M, N))
+        got = run(cuda, A, B, C0, la, lb, lc, accuracy=mode)
+        np.testing.assert_array_equal(got, OZ.gemm(A, B, C0, NDIG[mode]), err_msg=f"{M}x{N}x{K} {kind}")
+
+
+@pytest.mark.parametrize("kind", ["uniform", "wide"])
+def test_auto_bit_exact_where_the_guard_keeps_the_digits(cuda, kind):
+    """Guarded AUTO: every 32 x 16 block the model's guard keeps equals the
+    model bit for bit; the blocks it rejects (rows with a 2^40 entry against
+    a zero row of B) are within the FP64 bound."""
+    rng = np.random.default_rng(32)
+    # wide-range operands pass the guard (which samples a quarter of K) from
+    # K of about 4096; below that AUTO sends their blocks to the FP64 pipes
+    M, N, K = 256, 96, (640 if kind == "uniform" else 4096)
+    A, B = operands(rng, M, N, K, kind)
+    A[:40, 0] = 2.0 ** 40
+    B[0, :] = 0.0
+    C0 = rng.uniform(-1, 1, (M, N))
+    got = run_any(cuda, A, B, C0, AUTO)
+    keep = OZ.guard_pass(A, B)
+    assert keep.any() and (~keep).any()
+    want = OZ.gemm(A, B, C0, 7)
+    np.testing.assert_array_equal(got[keep], want[keep])
+    ref = O.gemm(A, B, C0, 1, 1, 1)
+    assert (np.abs(got - ref)[~keep] <= fp64_tol(A, B, C0)[~keep]).all()
