@@ -936,7 +936,8 @@ def run_serving(args):
     pool32 = torch.empty(int(args.pool_gb * (1 << 30)) // 8, device=dev).uniform_(-1, 1, generator=gen)
     pool64 = torch.empty(int(args.pool_gb * (1 << 30)) // 16, dtype=torch.float64, device=dev).uniform_(
         -1, 1, generator=gen)
-    srv = gbblas.Server(budget_bytes=64 << 30, heavy_streams=args.heavy_streams, heavy_us=args.heavy_us)
+    srv = gbblas.Server(streams=args.streams, max_group=args.max_group, budget_bytes=64 << 30,
+                        heavy_streams=args.heavy_streams, heavy_us=args.heavy_us)
     # float64 GEMMs: AUTO (the library default: guarded tensor-core digits
     # where the shape suits) or the FP64 pipes
     f64_acc = 5 if args.f64_accuracy == "fp64" else 3
@@ -1020,8 +1021,9 @@ def run_serving(args):
                                    "dot n log-uniform [1k,64M], 80% f32 (FP32-accurate) / 20% f64, seed 5",
                        "f64_gemm": ("FP64 pipes" if f64_acc == 5 else
                                     "AUTO: guarded 7-digit tensor-core scheme from 2^21 multiply-adds, FP64 pipes below"),
-                       "budget_GiB": 64, "streams": 4, "heavy_streams": args.heavy_streams or 2,
-                       "heavy_us": args.heavy_us or 1000}}
+                       "budget_GiB": 64, "streams": args.streams or 16, "max_group": args.max_group or 256,
+                       "heavy_streams": args.heavy_streams or 2,
+                       "heavy_us": args.heavy_us or 300}}
     print(json.dumps(line), flush=True)
     for p in outs:
         srv.free(p)
@@ -1353,6 +1355,10 @@ def main():
     ap.add_argument("--min-requests", type=int, default=400)
     ap.add_argument("--max-requests", type=int, default=4000)
     ap.add_argument("--lone-requests", type=int, default=200)
+    ap.add_argument("--streams", type=int, default=0,
+                    help="serving: light rounds in flight at once (0: the library default)")
+    ap.add_argument("--max-group", type=int, default=0,
+                    help="serving: requests per light round (0: the library default)")
     ap.add_argument("--heavy-streams", type=int, default=0,
                     help="serving: heavy requests in flight at once (0: the library default)")
     ap.add_argument("--heavy-us", type=int, default=0,

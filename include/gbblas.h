@@ -367,7 +367,7 @@ typedef struct gbblas_request {
 } gbblas_request;
 
 typedef struct gbblas_server_config {
-  int32_t streams;       /* light rounds in flight at once (default 4) */
+  int32_t streams;       /* light rounds in flight at once (default 16) */
   int32_t max_group;     /* requests per light round (default 256) */
   int64_t budget_bytes;  /* admission budget: operands + results + scratch of
                             requests in flight (default 64 GiB) */
@@ -377,7 +377,7 @@ typedef struct gbblas_server_config {
   int64_t heavy_us;      /* estimated GPU time (us) above which a request is
                             heavy: it runs alone on a low-priority stream while
                             light rounds (capped at this much estimated work)
-                            run on high-priority streams (default 1000) */
+                            run on high-priority streams (default 300) */
 } gbblas_server_config;
 
 typedef struct gbblas_server_stats {
