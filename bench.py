@@ -594,8 +594,9 @@ def run_precision(args):
     as split-BF16 (three or six tcgen05 products), FP8-E4M3 with per-128
     K-block scales (tcgen05 kind::f8f6f4) and plain FP32 (FMA pipe), on two
     input sets (U[-1,1) and wide-range s*m*2^e, e in [-10, 10]); TFLOP/s of
-    2*M*N*K algorithmic flops and max / mean relative error against
-    long-double dots on sampled entries.  One JSON line per (path, set)."""
+    2*M*N*K algorithmic flops, max / mean relative error against long-double
+    dots on sampled entries, and the same over the full matrix against the
+    product computed on the FP64 pipes.  One JSON line per (path, set)."""
     import numpy as np
     import torch
 
@@ -626,6 +627,20 @@ def run_precision(args):
             A, B = wide(), wide()
         An, Bn = A.cpu().numpy(), B.cpu().numpy()
         exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
+        # full-matrix FP64 residual on the GPU: C64 = A B on the FP64 pipes
+        # (the FMA kernel, independent of the tensor-core paths checked), and
+        # |A||B| in FP32 for the normwise scale
+        sp0 = torch.cuda.current_stream().cuda_stream or None
+        A64, B64 = A.double(), B.double()
+        C64 = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+        gbblas.call("gbblas_dgemm_ex", n, n, n, A64.data_ptr(), n, 1, B64.data_ptr(), n, 1, C64.data_ptr(), n, 1,
+                    5, sp0)
+        del A64, B64
+        Aa, Ba = A.abs(), B.abs()
+        absAB = torch.zeros(n, n, device="cuda")
+        gbblas.call("gbblas_sgemm", n, n, n, Aa.data_ptr(), n, 1, Ba.data_ptr(), n, 1, absAB.data_ptr(), n, 1, 0, sp0)
+        del Aa, Ba
+        gbblas.call("gbblas_check_stream", sp0)
         for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp8", 2), ("fp32", 0)):
             if path not in args.paths.split(","):
                 continue
@@ -656,12 +671,18 @@ def run_precision(args):
             got = C.cpu().numpy()[rows, cols].astype(np.float64)
             rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
             normwise = np.abs(got - exact) / absx
+            diff = (C.double() - C64).abs_()
+            full = {"max_rel_err": float((diff / C64.abs().clamp_min(1e-300)).max()),
+                    "mean_rel_err": float((diff / C64.abs().clamp_min(1e-300)).mean()),
+                    "max_normwise_err": float((diff / absAB.double().clamp_min(1e-300)).max()),
+                    "reference": "the full M x N product on the FP64 pipes (GPU)"}
+            del diff
             tf = flops / (ms / 1e3) / 1e12
             line = {"metric": "GEMM TFLOP/s (float32 operands)", "path": path, "input_set": set_name,
                     "value": round(tf, 2), "unit": "TFLOP/s", "ms_per_gemm": round(ms, 3), "M": n, "N": n, "K": n,
                     "flops": "2*M*N*K algorithmic", "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
                     "max_normwise_err": float(normwise.max()), "error_sample": f"{sample} entries vs long double",
-                    "clocks": clk.summary()}
+                    "full_matrix_fp64": full, "clocks": clk.summary()}
             products = {"bf16x3": 3, "bf16x6": 6}.get(path)
             if products and peaks.get("bf16_tflops"):
                 line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
@@ -677,7 +698,7 @@ def run_precision(args):
                 line["tensor_peak"] = (f"2 x bf16_tflops {peaks['bf16_tflops']} (measured BF16 burst times the "
                                        "nominal FP8/BF16 ratio; no FP8 peak is measured)")
             print(json.dumps(line), flush=True)
-        del A, B
+        del A, B, C64, absAB
 
 
 def run_f64(args):
