@@ -415,6 +415,9 @@ gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A,
 gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                                 const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
                                 int64_t csc);
+gbblas_status gbblas_dgemm_ex_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                                   const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
+                                   int64_t csc, gbblas_accuracy accuracy);
 gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x,
                                float* y);
 gbblas_status gbblas_dmtv_host(gbblas_layout la, int64_t M, int64_t N, const double* A, const double* x,

@@ -21,8 +21,10 @@
 
 namespace amt {
 
-/// C += A * B.  An optional fifth argument picks the single-precision
-/// arithmetic (amt::gpu::accuracy; default fp32 FMA, the reference's).
+/// C += A * B.  An optional fifth argument picks the arithmetic
+/// (amt::gpu::accuracy): for float the default is fp32 FMA, the
+/// reference's; for double the default is the library's (tensor-core digits
+/// kept within the FP64 error bound where faster), fp64 forces FP64 FMAs.
 template <typename Out, typename E1, typename E2>
 constexpr auto mtm(boost::numeric::ublas::tensor_core<Out>& c, boost::numeric::ublas::tensor_core<E1> const& a,
                    boost::numeric::ublas::tensor_core<E2> const& b, std::optional<std::size_t> num_threads,
@@ -60,9 +62,12 @@ constexpr auto mtm(boost::numeric::ublas::tensor_core<Out>& c, boost::numeric::u
     if constexpr (std::is_same_v<out_value_type, float>)
       s = gbblas_sgemm_host(M, N, K, ap, (int64_t)wa[0], (int64_t)wa[1], bp, (int64_t)wb[0], (int64_t)wb[1], cp,
                             (int64_t)wc[0], (int64_t)wc[1], static_cast<gbblas_accuracy>(acc));
-    else
+    else if (acc == gpu::accuracy::fp32)
       s = gbblas_dgemm_host(M, N, K, ap, (int64_t)wa[0], (int64_t)wa[1], bp, (int64_t)wb[0], (int64_t)wb[1], cp,
                             (int64_t)wc[0], (int64_t)wc[1]);
+    else
+      s = gbblas_dgemm_ex_host(M, N, K, ap, (int64_t)wa[0], (int64_t)wa[1], bp, (int64_t)wb[0], (int64_t)wb[1], cp,
+                               (int64_t)wc[0], (int64_t)wc[1], static_cast<gbblas_accuracy>(acc));
     gpu::check(s, "amt::mtm");
   };
 }

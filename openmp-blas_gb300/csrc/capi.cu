@@ -272,10 +272,24 @@ gbblas_status d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   return GBBLAS_STATUS_SUCCESS;
 }
 
+// The arithmetic choices each element type takes.
+template <typename T>
+gbblas_status check_accuracy(gbblas_accuracy acc) {
+  if constexpr (std::is_same_v<T, float>) {
+    if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+  } else {
+    if (acc != GBBLAS_ACCURACY_FP64 && acc != GBBLAS_ACCURACY_AUTO && !dgemm_digits_count(acc))
+      return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, AUTO, FP64_DIGITS7 or FP64_DIGITS8",
+                 (int)acc);
+  }
+  return GBBLAS_STATUS_SUCCESS;
+}
+
 template <typename T>
 gbblas_status gemm_host(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
                         int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc) {
   GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
+  GB_TRY(check_accuracy<T>(acc));
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
@@ -366,13 +380,7 @@ template <typename T>
 gbblas_status gemm_dev(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa, int64_t csa, const T* B,
                        int64_t rsb, int64_t csb, T* C, int64_t rsc, int64_t csc, gbblas_accuracy acc, void* stream) {
   GB_TRY(check_gemm<T>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc));
-  if constexpr (std::is_same_v<T, float>) {
-    if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
-  } else {
-    if (acc != GBBLAS_ACCURACY_FP64 && acc != GBBLAS_ACCURACY_AUTO && !dgemm_digits_count(acc))
-      return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, AUTO, FP64_DIGITS7 or FP64_DIGITS8",
-                 (int)acc);
-  }
+  GB_TRY(check_accuracy<T>(acc));
   DeviceCtx* c;
   GB_TRY(get_ctx(&c));
   return gemm_any<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, acc, as_stream(stream));
@@ -728,6 +736,11 @@ gbblas_status gbblas_sgemm_host(int64_t M, int64_t N, int64_t K, const float* A,
 gbblas_status gbblas_dgemm_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
                                 const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc) {
   return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, dgemm_default_accuracy());
+}
+gbblas_status gbblas_dgemm_ex_host(int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa, int64_t csa,
+                                   const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc, int64_t csc,
+                                   gbblas_accuracy accuracy) {
+  return gemm_host<double>(M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, accuracy);
 }
 gbblas_status gbblas_smtv_host(gbblas_layout la, int64_t M, int64_t N, const float* A, const float* x, float* y) {
   return gemv_host<float>(la, false, M, N, A, x, la == GBBLAS_FIRST_ORDER, y);

@@ -190,9 +190,9 @@ __global__ void __launch_bounds__(256) row_scale_kernel(const DgOperand oa, cons
         }
       }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+      for (int off = 16; off > 0; off >>= 1) {
+        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, off);
       }
       if (lane == 0) {
         part_max[0][r] = amax;

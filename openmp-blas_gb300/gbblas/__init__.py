@@ -77,6 +77,7 @@ SIGNATURES = {
     "gbblas_server_destroy": (_int, [_vp]),
     "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
     "gbblas_dgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
+    "gbblas_dgemm_ex_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
     "gbblas_smtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
     "gbblas_dmtv_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
     "gbblas_svtm_host": (_int, [_int, _i64, _i64, _vp, _vp, _vp]),
@@ -374,8 +375,11 @@ def gemm_host(M, N, K, a, rsa, csa, b, rsb, csb, c, rsc, csc, accuracy: int = AC
     p = _npfx(a)
     args = [M, N, K, a.ctypes.data, rsa, csa, b.ctypes.data, rsb, csb, c.ctypes.data, rsc, csc]
     if p == "s":
-        args.append(accuracy)
-    call(f"gbblas_{p}gemm_host", *args)
+        call("gbblas_sgemm_host", *args, accuracy)
+    elif accuracy == ACCURACY_FP32:
+        call("gbblas_dgemm_host", *args)
+    else:
+        call("gbblas_dgemm_ex_host", *args, accuracy)
 
 
 def mtv_host(layout, M, N, a, x, y):

@@ -92,6 +92,15 @@ void mtm_case() {
   oracle_gemm<T>(37, 29, 600, A.data(), wa[0], wa[1], B.data(), wb[0], wb[1], lres.data(), wc[0], wc[1]);
   amt::mtm(rres, A, B, std::nullopt)();
   for (std::size_t i = 0; i < rres.size(); ++i) REQUIRE(rres[i] == lres[i]);
+  if constexpr (std::is_same_v<T, double>) {
+    // every double arithmetic is exact on these integers
+    for (auto acc : {amt::gpu::accuracy::fp64, amt::gpu::accuracy::automatic, amt::gpu::accuracy::fp64_digits7,
+                     amt::gpu::accuracy::fp64_digits8}) {
+      auto r2 = amt::make_tensor<T, LC>(37, 29, T(3));
+      amt::mtm(r2, A, B, std::nullopt, acc)();
+      for (std::size_t i = 0; i < r2.size(); ++i) REQUIRE(r2[i] == lres[i]);
+    }
+  }
 }
 
 template <typename T>

@@ -46,6 +46,8 @@ def test_status_strings():
     ("gbblas_sgemm", (2, 2, 2, 16, 1, 2, 16, 1, 2, None, 1, 2, 0, None)),
     ("gbblas_dgemm", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 0, 0, None)),
     ("gbblas_dgemm_ex", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 2, 1, 4, None)),  # BF16X6 is float-only
+    ("gbblas_dgemm_ex_host", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 2, 1, 1)),
+    ("gbblas_sgemm_host", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 2, 1, 5)),  # FP64 is double-only
     ("gbblas_dgemm_ex", (2, 2, 2, 16, 1, 2, 16, 1, 2, 16, 2, 1, 8, None)),
     ("gbblas_dgemm_ex", (2, -2, 2, 16, 1, 2, 16, 1, 2, 16, 2, 1, 6, None)),
     ("gbblas_smtv", (2, 4, 4, 16, 16, 16, None)),
