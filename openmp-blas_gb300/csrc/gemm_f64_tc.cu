@@ -22,8 +22,9 @@
 //      in magnitude and the FP32 accumulation in TMEM is exact.  Every 128 of
 //      K the epilogue converts each group to an integer and adds it, shifted
 //      by its weight, into two 64-bit accumulators per output (exact for K
-//      up to 2^20); at the end of the tile it converts them once to FP64,
-//      scales by the power of two and adds into C.
+//      up to 2^20); at the end of the tile it rounds their 128-bit sum once
+//      to FP64 (integer operations; the power of two goes into the exponent
+//      field) and adds it into C - one FP64 instruction per output.
 //
 // Error: the only roundings are the digit truncation (2^-8S of the scale),
 // the dropped digit products and the final conversion and addition, so
@@ -159,9 +160,18 @@ struct DgOperand {
   int blocks;               // CTAs of this operand
 };
 
+// Magnitudes compare as their bit patterns with the sign cleared (IEEE
+// order), so the scan runs on the integer pipes: GB300's FP64 pipes would
+// bound it (fabs / fmax / isfinite on doubles are FP64 instructions).
+constexpr unsigned long long kAbsMask = 0x7FFFFFFFFFFFFFFFull;
+constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;  // |a| >= this: Inf or NaN
+
+__device__ __forceinline__ unsigned long long abs_bits(const double* p) {
+  return (unsigned long long)__double_as_longlong(__ldg(p)) & kAbsMask;
+}
+
 __global__ void __launch_bounds__(256) row_scale_kernel(const DgOperand oa, const DgOperand ob, int* fix_count) {
-  __shared__ double part_max[8][33];
-  __shared__ int part_bad[8][33];
+  __shared__ unsigned long long part_max[8][33];
   const bool is_a = (int)blockIdx.x < oa.blocks;
   const DgOperand& o = is_a ? oa : ob;
   const int blk = is_a ? (int)blockIdx.x : (int)blockIdx.x - oa.blocks;
@@ -171,75 +181,60 @@ __global__ void __launch_bounds__(256) row_scale_kernel(const DgOperand oa, cons
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x == 0 && tid == 0 && fix_count) *fix_count = 0;
   const int64_t r0 = (int64_t)(blk / o.tiles_k) * 32, k0 = (int64_t)(blk % o.tiles_k) * kScaleTK;
+  unsigned long long amax;  // largest |a| bit pattern; >= kInfBits marks Inf / NaN
   if (cs == 1) {
     // warp w: rows w, w+8, w+16, w+24; lanes along K
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = warp + 8 * i;
-      double amax = 0.0;
-      int bad = 0;
+      unsigned long long m = 0;
       if (r0 + r < rows) {
         const double* p = src + (r0 + r) * rs + k0;
-        double v[kScaleTK / 32];
+        unsigned long long v[kScaleTK / 32];
 #pragma unroll
-        for (int j = 0; j < kScaleTK / 32; ++j) v[j] = (k0 + lane + 32 * j < K) ? __ldg(p + lane + 32 * j) : 0.0;
+        for (int j = 0; j < kScaleTK / 32; ++j) v[j] = (k0 + lane + 32 * j < K) ? abs_bits(p + lane + 32 * j) : 0ull;
 #pragma unroll
-        for (int j = 0; j < kScaleTK / 32; ++j) {
-          bad |= !isfinite(v[j]);
-          amax = fmax(amax, fabs(v[j]));
-        }
+        for (int j = 0; j < kScaleTK / 32; ++j) m = v[j] > m ? v[j] : m;
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
-        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, off));
-        bad |= __shfl_xor_sync(0xffffffffu, bad, off);
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, off);
+        m = x > m ? x : m;
       }
-      if (lane == 0) {
-        part_max[0][r] = amax;
-        part_bad[0][r] = bad;
-      }
+      if (lane == 0) part_max[0][r] = m;
     }
     __syncthreads();
     if (tid >= 32) return;
+    amax = part_max[0][lane];
   } else {
     // thread (slice w, row lane): 32 consecutive K of row lane; a warp reads
     // 32 consecutive rows at each k
-    const int r = lane;
-    double amax = 0.0;
-    int bad = 0;
-    if (r0 + r < rows) {
-      const double* p = src + (r0 + r) * rs;
-      double v[32];
+    unsigned long long m = 0;
+    if (r0 + lane < rows) {
+      const double* p = src + (r0 + lane) * rs;
+      unsigned long long v[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int64_t k = k0 + warp * 32 + j;
-        v[j] = k < K ? __ldg(p + k * cs) : 0.0;
+        v[j] = k < K ? abs_bits(p + k * cs) : 0ull;
       }
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        bad |= !isfinite(v[j]);
-        amax = fmax(amax, fabs(v[j]));
-      }
+      for (int j = 0; j < 32; ++j) m = v[j] > m ? v[j] : m;
     }
-    part_max[warp][r] = amax;
-    part_bad[warp][r] = bad;
+    part_max[warp][lane] = m;
     __syncthreads();
     if (tid >= 32) return;
-    for (int w = 1; w < 8; ++w) {
-      amax = fmax(amax, part_max[w][lane]);
-      bad |= part_bad[w][lane];
-    }
-    part_max[0][lane] = amax;
-    part_bad[0][lane] = bad;
+    for (int w = 1; w < 8; ++w) m = part_max[w][lane] > m ? part_max[w][lane] : m;
+    amax = m;
   }
   // warp 0: one row per lane
-  const double amax = part_max[0][lane];
   if (r0 + lane >= rows) return;
-  if (part_bad[0][lane]) {
+  if (amax >= kInfBits) {
     atomicMax(e_out + r0 + lane, kBadExp);
-  } else if (amax > 0.0) {
-    int e;
-    (void)frexp(amax, &e);  // amax = m 2^e, m in [0.5, 1)
+  } else if (amax != 0) {
+    // the frexp exponent: |a| = f 2^e with f in [0.5, 1)
+    const int ex = (int)(amax >> 52);
+    const int e = ex != 0 ? ex - 1022 : (64 - __clzll((long long)amax)) - 1074;
     atomicMax(e_out + r0 + lane, e);
   }
 }
@@ -348,6 +343,42 @@ __global__ void __launch_bounds__(256) digits_kernel(const DgOperand oa, const D
 }
 
 // ---------------------------------------------------------------- GEMM
+// (hi 2^32 + lo) 2^e2 rounded once to the nearest double (ties to even),
+// with integer operations only: the 128-bit value's top 53 bits and the
+// round bit, the scale added to the exponent field.  A result below the
+// normal range (or above it) goes through ldexp, so it may round twice.
+__device__ __forceinline__ double i128_scaled_to_double(long long hi, long long lo, int e2) {
+  const __int128 v = ((__int128)hi << 32) + (__int128)lo;
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  const unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+  const int n = mh ? 128 - __clzll((long long)mh) : 64 - __clzll((long long)ml);  // bit length, >= 1
+  unsigned long long mant;  // 2^52 <= mant < 2^53
+  int exp2;                 // value = mant 2^exp2
+  if (n <= 53) {
+    mant = ml << (53 - n);
+    exp2 = e2 - (53 - n);
+  } else {
+    const int sh = n - 53;
+    mant = (unsigned long long)(m >> sh);
+    const unsigned __int128 rem = m & ((((unsigned __int128)1) << sh) - 1);
+    const unsigned __int128 half = ((unsigned __int128)1) << (sh - 1);
+    exp2 = e2 + sh;
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) {
+        mant >>= 1;
+        ++exp2;
+      }
+    }
+  }
+  const int be = exp2 + 52 + 1023;  // biased exponent of mant 2^exp2
+  if (be <= 0 || be >= 2047) return ldexp(neg ? -(double)mant : (double)mant, exp2);
+  return __longlong_as_double((neg ? (long long)(1ull << 63) : 0ll) | ((long long)be << 52) |
+                              (long long)(mant & ((1ull << 52) - 1)));
+}
+
 // Output tile t (static round-robin over the CTAs): grouped raster, 8 tile
 // rows per band, so the CTAs running at one time share A's and B's digit
 // tiles in L2.
@@ -612,21 +643,47 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (row < p.M) {
+        // C += r for the thread's 16 outputs: all loads first, then all
+        // stores (the outputs are distinct: a valid C has non-zero strides),
+        // 16-byte accesses where the row segment is contiguous and aligned
         const int ei = p.ea[row] == kBadExp ? kBadExp : used_exp(p.ea[row]);
         double* crow = p.C + (int64_t)row * p.rsc;
         const int cn = n0 + 16 * h;
+        const int nv = min(16, p.N - cn);
+        const bool vec = p.csc == 1 && nv == 16 && (reinterpret_cast<uintptr_t>(crow + cn) & 15) == 0;
+        double cv[16];
+        int ej[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          if (cn + j >= p.N) continue;
-          const int ej = p.eb[cn + j] == kBadExp ? kBadExp : used_exp(p.eb[cn + j]);
+          const int e = j < nv ? p.eb[cn + j] : 0;
+          ej[j] = e == kBadExp ? kBadExp : used_exp(e);
+        }
+        if (vec) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 2) {
+            const double2 t = *reinterpret_cast<const double2*>(crow + cn + j);
+            cv[j] = t.x;
+            cv[j + 1] = t.y;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) cv[j] = j < nv ? crow[(int64_t)(cn + j) * p.csc] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
           // hi 2^32 + lo in units of 2^(e_i + f_j - 14 - 8(S-1))
-          double r;
-          if (ei == kBadExp || ej == kBadExp)
-            r = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+          if (ei == kBadExp || ej[j] == kBadExp)
+            cv[j] += __longlong_as_double(0x7ff8000000000000ll);  // NaN
           else
-            r = ldexp((double)hi[j] * 4294967296.0 + (double)lo[j], ei + ej - 14 - 8 * (S - 1));
-          double* cp = crow + (int64_t)(cn + j) * p.csc;
-          *cp += r;
+            cv[j] += i128_scaled_to_double(hi[j], lo[j], ei + ej[j] - 14 - 8 * (S - 1));
+        }
+        if (vec) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 2) *reinterpret_cast<double2*>(crow + cn + j) = make_double2(cv[j], cv[j + 1]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (j < nv) crow[(int64_t)(cn + j) * p.csc] = cv[j];
         }
       }
     }

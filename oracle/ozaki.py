@@ -16,9 +16,9 @@ demand bit equality between the GPU and this model:
   zero), written in balanced base 256: S digits, the last S-1 in
   [-128, 127], the first in [-128, 128];
 * G_w = sum_k sum_{s+t=w} D_s(a_ik) E_t(b_kj) for w < S (exact integers);
-* hi = sum_{w<S-4} G_w 2^(8(S-5-w)), lo = sum_{w>=S-4} G_w 2^(8(S-1-w)) in
-  64-bit integers, r = ldexp(double(hi) * 2^32 + double(lo),
-  e_i + f_j - 14 - 8(S-1)) with round-to-nearest conversions and addition,
+* r = sum_w G_w 2^(8(S-1-w)) (an exact integer; the kernel holds it as
+  hi 2^32 + lo in two 64-bit integers) rounded once to the nearest double
+  (ties to even) and scaled by 2^(e_i + f_j - 14 - 8(S-1)),
   C_ij = C_ij + r (NaN where the row or column is bad);
 * the guard (7 digits): P = max(|D_0| - 1, 0); L_ij = sum over the first
   32 of K of every 128-K chunk of P(a_ik) P(b_kj); a 32 x 16 output block of
@@ -82,16 +82,14 @@ def groups(DA: np.ndarray, DB: np.ndarray) -> np.ndarray:
 
 
 def combine(G: np.ndarray, e: np.ndarray, f: np.ndarray) -> np.ndarray:
-    """The kernel's epilogue: hi / lo in 64-bit integers, one conversion, the power-of-two scale."""
+    """The kernel's epilogue: the exact integer sum_w G_w 2^(8(S-1-w)) (hi 2^32 + lo)
+    rounded once to the nearest double (ties to even; Python's int -> float),
+    then scaled by the power of two (exact in the normal range)."""
     S = G.shape[0]
-    hi = np.zeros(G.shape[1:], np.int64)
-    lo = np.zeros(G.shape[1:], np.int64)
+    total = np.zeros(G.shape[1:], object)
     for w in range(S):
-        if w < S - 4:
-            hi += G[w] << (8 * (S - 5 - w))
-        else:
-            lo += G[w] << (8 * (S - 1 - w))
-    v = hi.astype(np.float64) * 4294967296.0 + lo.astype(np.float64)
+        total = total + G[w].astype(object) * (1 << (8 * (S - 1 - w)))
+    v = np.vectorize(float, otypes=[np.float64])(total) if total.size else np.zeros(total.shape)
     return np.ldexp(v, (e[:, None] + f[None, :] - 14 - 8 * (S - 1)).astype(np.int32))
 
 
