@@ -797,18 +797,23 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         // dense 16-byte-aligned rows
         const bool add = !pr.overwrite;
         if (vec && cn + kCols <= pr.N) {
+          // 64 bytes at a time: four loads in flight before their stores
 #pragma unroll
-          for (int j = 0; j < kCols; j += 4) {
-            float4* p = reinterpret_cast<float4*>(crow + cn + j);
-            float4 cv = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-            if (add) {
-              const float4 old = *p;
-              cv.x = old.x + cv.x;
-              cv.y = old.y + cv.y;
-              cv.z = old.z + cv.z;
-              cv.w = old.w + cv.w;
+          for (int j0 = 0; j0 < kCols; j0 += 16) {
+            float4* p = reinterpret_cast<float4*>(crow + cn + j0);
+            float4 cv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) cv[u] = add ? p[u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int j = j0 + 4 * u;
+              cv[u].x += acc[j];
+              cv[u].y += acc[j + 1];
+              cv[u].z += acc[j + 2];
+              cv[u].w += acc[j + 3];
             }
-            *p = cv;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) p[u] = cv[u];
           }
         } else {
 #pragma unroll
