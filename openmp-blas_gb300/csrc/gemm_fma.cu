@@ -276,18 +276,23 @@ __global__ void __launch_bounds__(Cfg<T, BM, BN, BK, TM, TN>::NT, 2)
     __syncthreads();
   }
 
-  // ---- C += acc (the reference's copy_from_buff, include/simd_loop.hpp:160-190)
+  // ---- C += acc (the reference's copy_from_buff, include/simd_loop.hpp:160-190);
+  // a row's loads are issued before its stores (the compiler cannot see
+  // that runtime strides keep the outputs apart)
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     const int64_t gm = m0 + (i / 4) * (BM / CF::TM4) + ty * 4 + (i % 4);
     if (gm >= M) continue;
+    T old[TN];
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       const int64_t gn = n0 + (j / 4) * (BN / CF::TN4) + tx * 4 + (j % 4);
-      if (gn < N) {
-        T* p = C + gm * rsc + gn * csc;
-        *p += acc[i][j];
-      }
+      old[j] = gn < N ? C[gm * rsc + gn * csc] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int64_t gn = n0 + (j / 4) * (BN / CF::TN4) + tx * 4 + (j % 4);
+      if (gn < N) C[gm * rsc + gn * csc] = old[j] + acc[i][j];
     }
   }
   }  // tile loop

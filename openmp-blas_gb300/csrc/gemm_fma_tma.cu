@@ -24,9 +24,10 @@
 // Persistent: grid = min(tiles, SMs or the caller's cap), tiles in grouped
 // raster order (8 tile rows per band) for L2 reuse; the ring carries over
 // from tile to tile.  Split-K (parts > 1, for shapes whose tiles leave SMs
-// idle): each unit = (tile, K part) adds its K range into a zeroed partial,
-// then the partials are added into C in part order - within the same bound,
-// not the same bits as the unsplit kernels.  Roofline: the FMA pipes,
+// idle): each unit = (tile, K part) stores its K range's sum into that
+// part's partial (no other unit writes those elements), then the partials
+// are added into C in part order - within the same bound, not the same bits
+// as the unsplit kernels.  Roofline: the FMA pipes,
 // 2*M*N*K flops.
 #include <cuda.h>
 
@@ -238,40 +239,73 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&empty[s]);
       }
       if (!ok) break;
-      // C += acc (rows / columns outside the matrix dropped); split-K: into
-      // this part's dense partial
-      float* Ct = parts > 1 ? part_buf + (int64_t)pp * M * N : C;
-      const int64_t rs = parts > 1 ? (int64_t)N : rsc, cs = parts > 1 ? 1 : csc;
+      // C += acc (rows / columns outside the matrix dropped).  Split-K: this
+      // part's dense partial, which no other unit writes - stored, not added.
+      // Loads of C for four rows are issued before their stores (the
+      // compiler cannot see that runtime strides keep the rows apart).
+      const bool partial = parts > 1;
+      float* Ct = partial ? part_buf + (int64_t)pp * M * N : C;
+      const int64_t rs = partial ? (int64_t)N : rsc, cs = partial ? 1 : csc;
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int m = m0 + owned<A_KMAJ>(ty, i);
-        if (m >= M) continue;
-        float* crow = Ct + (int64_t)m * rs;
+      for (int i0 = 0; i0 < 8; i0 += 4) {
         if constexpr (!B_KMAJ) {
           // columns tx*4 + {0..3} and 64 + tx*4 + {0..3}: two float4 when C rows are contiguous
           const bool vec = cs == 1 && ((rs & 3) == 0) && ((reinterpret_cast<uintptr_t>(Ct) & 15) == 0);
+          float4 cv[4][2];
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int n = n0 + tx * 4 + 64 * h;
-            if (vec && n + 4 <= N) {
-              float4* p = reinterpret_cast<float4*>(crow + n);
-              float4 cv = *p;
-              cv.x += acc[i][4 * h];
-              cv.y += acc[i][4 * h + 1];
-              cv.z += acc[i][4 * h + 2];
-              cv.w += acc[i][4 * h + 3];
-              *p = cv;
-            } else {
+          for (int i = 0; i < 4; ++i) {
+            const int m = m0 + owned<A_KMAJ>(ty, i0 + i);
 #pragma unroll
-              for (int q = 0; q < 4; ++q)
-                if (n + q < N) crow[(int64_t)(n + q) * cs] += acc[i][4 * h + q];
+            for (int h = 0; h < 2; ++h) {
+              const int n = n0 + tx * 4 + 64 * h;
+              cv[i][h] = (!partial && vec && m < M && n + 4 <= N)
+                             ? *reinterpret_cast<const float4*>(Ct + (int64_t)m * rs + n)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int m = m0 + owned<A_KMAJ>(ty, i0 + i);
+            if (m >= M) continue;
+            float* crow = Ct + (int64_t)m * rs;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int n = n0 + tx * 4 + 64 * h;
+              const float* a4 = &acc[i0 + i][4 * h];
+              if (vec && n + 4 <= N) {
+                float4 v = cv[i][h];
+                v.x += a4[0];
+                v.y += a4[1];
+                v.z += a4[2];
+                v.w += a4[3];
+                *reinterpret_cast<float4*>(crow + n) = v;
+              } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  if (n + q < N) {
+                    float* cq = crow + (int64_t)(n + q) * cs;
+                    *cq = partial ? a4[q] : *cq + a4[q];
+                  }
+              }
             }
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int n = n0 + owned<true>(tx, j);
-            if (n < N) crow[(int64_t)n * cs] += acc[i][j];
+          for (int i = 0; i < 4; ++i) {
+            const int m = m0 + owned<A_KMAJ>(ty, i0 + i);
+            if (m >= M) continue;
+            float* crow = Ct + (int64_t)m * rs;
+            float old[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int n = n0 + owned<true>(tx, j);
+              old[j] = (!partial && n < N) ? crow[(int64_t)n * cs] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int n = n0 + owned<true>(tx, j);
+              if (n < N) crow[(int64_t)n * cs] = old[j] + acc[i0 + i][j];
+            }
           }
         }
       }
@@ -368,7 +402,7 @@ gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, co
   GB_TRY(get_scratch(c, stream, kScratchZeroBytes + part_bytes, &s));
   int* err = reinterpret_cast<int*>(static_cast<char*>(s) + kErrWordOffset);
   float* part_buf = parts > 1 ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
-  if (parts > 1) GB_CUDA_TRY(cudaMemsetAsync(part_buf, 0, part_bytes, stream));
+  // (every element of every part is written by exactly one (tile, part) unit: no clearing)
   gbblas_status st;
   if (ak && bk)
     st = launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
