@@ -237,8 +237,13 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
     // preparation, the FP64 pipes elsewhere.
     if (const int digits = dgemm_digits_count(acc))
       return launch_dgemm_digits(c, digits, false, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
-    if (acc == GBBLAS_ACCURACY_AUTO && dgemm_auto_digits(M, N, K, c->num_sms))
-      return launch_dgemm_digits(c, 7, true, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+    if (acc == GBBLAS_ACCURACY_AUTO && dgemm_auto_digits(M, N, K, c->num_sms)) {
+      // a shape beyond the digit kernels' grid, or digit planes that do not
+      // fit in device memory, fall back to the FP64 pipes
+      const gbblas_status st = launch_dgemm_digits(c, 7, true, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+      if (st != GBBLAS_STATUS_ALLOC_FAILED && st != GBBLAS_STATUS_NOT_SUPPORTED) return st;
+      cudaGetLastError();  // a failed allocation leaves no sticky error; clear the last one
+    }
   }
   if constexpr (std::is_same_v<T, float>) {
     // BF16X3 / BF16X6 / FP8 always take the tensor cores.  AUTO: whichever
