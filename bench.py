@@ -1351,7 +1351,7 @@ def run_sweep(args):
         else:
             cpu.update(0.0)
     gbblas.call("gbblas_check_stream", None)
-    csv_path = args.sweep_csv or os.path.join(ROOT, "gpurun_out", f"sweep_{op}.csv")
+    csv_path = args.sweep_csv or os.path.join(ROOT, "openmp-blas_gb300", "_build", f"sweep_{op}.csv")
     os.makedirs(os.path.dirname(csv_path), exist_ok=True)
     m.csv(csv_path)
     print(m.str("tensor"), file=sys.stderr)

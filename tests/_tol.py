@@ -2,8 +2,8 @@
 
 GEMM / GEMV / plain dot: |gpu - oracle| <= 2 * K * eps_T * (|A||B| + |C0|)
 elementwise, K = reduction length (both sides round at most K times; the
-reference's own error against FP64 stays below 0.33 K eps on the survey's
-shapes).  Kahan FP32 dot against the exact sum: 4 * eps_f32 * sum|a_i b_i|
+reference's own error against FP64 stays below 0.33 K eps on the shapes of
+its own tests).  Kahan FP32 dot against the exact sum: 4 * eps_f32 * sum|a_i b_i|
 plus half an ulp of the result.
 """
 import numpy as np
@@ -39,7 +39,7 @@ def assert_vec_close(got, ref, scale, K, dtype, c=C_GEMM, what=""):
 
 # The reference's f32 division under its -ffast-math x86 build is a
 # reciprocal estimate refined by one Newton step, up to 3 ulp from the IEEE
-# quotient (measured on 10^5 random quotients); this build divides exactly.
+# quotient (measured on 10^5 random quotients); this library divides exactly.
 REF_F32_DIV_ULP = 4
 
 
