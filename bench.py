@@ -958,7 +958,8 @@ def run_serving(args):
     pool64 = torch.empty(int(args.pool_gb * (1 << 30)) // 16, dtype=torch.float64, device=dev).uniform_(
         -1, 1, generator=gen)
     srv = gbblas.Server(streams=args.streams, max_group=args.max_group, budget_bytes=64 << 30,
-                        heavy_streams=args.heavy_streams, heavy_us=args.heavy_us)
+                        heavy_streams=args.heavy_streams, heavy_us=args.heavy_us,
+                        heavy_sm_percent=args.heavy_sm_percent)
     # float64 GEMMs: AUTO (the library default: guarded tensor-core digits
     # where the shape suits) or the FP64 pipes
     f64_acc = 5 if args.f64_accuracy == "fp64" else 3
@@ -1043,7 +1044,7 @@ def run_serving(args):
                        "f64_gemm": ("FP64 pipes" if f64_acc == 5 else
                                     "AUTO: guarded 7-digit tensor-core scheme from 2^21 multiply-adds, FP64 pipes below"),
                        "budget_GiB": 64, "streams": args.streams or 16, "max_group": args.max_group or 256,
-                       "heavy_streams": args.heavy_streams or 2,
+                       "heavy_streams": args.heavy_streams or 2, "heavy_sm_percent": args.heavy_sm_percent or 75,
                        "heavy_us": args.heavy_us or 300}}
     print(json.dumps(line), flush=True)
     for p in outs:
@@ -1380,6 +1381,8 @@ def main():
                     help="serving: light rounds in flight at once (0: the library default)")
     ap.add_argument("--max-group", type=int, default=0,
                     help="serving: requests per light round (0: the library default)")
+    ap.add_argument("--heavy-sm-percent", type=int, default=0,
+                    help="serving: share of the SMs a heavy request may take (0: the library default)")
     ap.add_argument("--heavy-streams", type=int, default=0,
                     help="serving: heavy requests in flight at once (0: the library default)")
     ap.add_argument("--heavy-us", type=int, default=0,

@@ -373,7 +373,8 @@ typedef struct gbblas_server_config {
                             requests in flight (default 64 GiB) */
   int64_t scratch_bytes; /* per-stream scratch reserved at start (default 1 GiB) */
   int32_t heavy_streams; /* heavy requests in flight at once (default 2) */
-  int32_t reserved;
+  int32_t heavy_sm_percent; /* share of the SMs a heavy request's grid may take
+                               (1..100; default 75): light rounds keep the rest */
   int64_t heavy_us;      /* estimated GPU time (us) above which a request is
                             heavy: it runs alone on a low-priority stream while
                             light rounds (capped at this much estimated work)

@@ -342,7 +342,7 @@ void scheduler_main(gbblas_server_s* s) {
         // of the GPU.  (Capping only while light work was already queued let
         // later arrivals wait behind whole heavy kernels: p99 2.3x the lone
         // p99 at 1 k req/s against 1.1x with the permanent cap.)
-        if (heavy) rd->max_ctas = std::max(1, s->ctx->num_sms * 3 / 4);
+        if (heavy) rd->max_ctas = std::max(1, s->ctx->num_sms * s->cfg.heavy_sm_percent / 100);
         cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
         lk.unlock();
         gbblas_status e = launch_round(s, rd, st);
@@ -381,8 +381,10 @@ gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_serve
   s->cfg.scratch_bytes = int64_t(1) << 30;
   s->cfg.heavy_streams = 2;
   s->cfg.heavy_us = 300;
+  s->cfg.heavy_sm_percent = 75;
   if (cfg) {
     if (cfg->heavy_streams > 0) s->cfg.heavy_streams = cfg->heavy_streams;
+    if (cfg->heavy_sm_percent > 0) s->cfg.heavy_sm_percent = std::min(cfg->heavy_sm_percent, 100);
     if (cfg->heavy_us > 0) s->cfg.heavy_us = cfg->heavy_us;
     if (cfg->streams > 0) s->cfg.streams = cfg->streams;
     if (cfg->max_group > 0) s->cfg.max_group = cfg->max_group;

@@ -178,6 +178,8 @@ def test_server_f64_gemm_on_tensor_core_digits(cuda):
     rng = np.random.default_rng(7)
     cases = [ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 1, (600, 520, 400), AUTO),
              ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 0, (384, 700, 256), AUTO),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 1, (256, 300, 500), gbblas.ACCURACY_FP64_DIGITS7),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 0, (200, 100, 300), gbblas.ACCURACY_FP64),
              ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 1, (300, 200, 500), AUTO),
              ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F64, 1, (700, 900))]
     srv = gbblas.Server(streams=4, max_group=16)
