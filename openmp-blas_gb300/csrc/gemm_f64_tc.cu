@@ -32,7 +32,18 @@
 // about 4 K 2^-53 max_k|a_ik| max_k|b_kj|.  The FP64 pipe's own bound is
 // K 2^-53 sum_k |a_ik| |b_kj|: the two agree where each row's and column's
 // magnitudes are comparable; rows mixing very large and very small values
-// lose relative accuracy in their small entries (use the FP64 pipes there).
+// lose relative accuracy in their small entries.
+//
+// The guard (7 digits, G = 1; what AUTO runs): one more plane per operand,
+// P = max(|D_0| - 1, 0) <= |x| 2^7, whose products summed over the first
+// 32 of K of every 128-K chunk bound sum_k |a_ik||b_kj| from below.  An
+// epilogue warp keeps its 32 x 16 block only where that bound makes the
+// digit error smaller than the FP64 pipes' bound; other blocks leave C
+// alone and are recomputed on the FP64 pipes by dgemm_fixup_kernel.
+//
+// The method is the published Ozaki scheme (error-free splitting of
+// floating-point matrix products into exactly computable ones, by Ozaki,
+// Ogita, Oishi and Rump), here with balanced base-256 integer digits.
 //
 // Kernel (persistent, one CTA per SM, tiles of 128 x 32 in static
 // round-robin order): per 32-K stage one 3-D TMA copy per operand brings all
@@ -49,8 +60,9 @@
 // and returns.
 //
 // Replaces the double-precision mtm of the reference (include/mtm.hpp:
-// 208-267 with include/simd_loop.hpp:132-158) when the caller asks for
-// GBBLAS_ACCURACY_FP64_DIGITS.  Roofline: the tensor pipe and shared-memory
+// 208-267 with include/simd_loop.hpp:132-158): guarded under AUTO (the
+// library's default for double where it is faster than the FP64 pipes),
+// unguarded for GBBLAS_ACCURACY_FP64_DIGITS7 / 8.  Roofline: the tensor pipe and shared-memory
 // bandwidth; 2*M*N*K algorithmic flops (the tensor cores execute
 // S(S+1)/2 times that in BF16 products).
 #include <cuda.h>
