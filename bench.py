@@ -641,7 +641,7 @@ def run_precision(args):
         gbblas.call("gbblas_sgemm", n, n, n, Aa.data_ptr(), n, 1, Ba.data_ptr(), n, 1, absAB.data_ptr(), n, 1, 0, sp0)
         del Aa, Ba
         gbblas.call("gbblas_check_stream", sp0)
-        for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp8", 2), ("fp32", 0)):
+        for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp16x3", 8), ("fp8", 2), ("fp32", 0)):
             if path not in args.paths.split(","):
                 continue
             C = torch.zeros(n, n, device="cuda")
@@ -683,7 +683,7 @@ def run_precision(args):
                     "flops": "2*M*N*K algorithmic", "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
                     "max_normwise_err": float(normwise.max()), "error_sample": f"{sample} entries vs long double",
                     "full_matrix_fp64": full, "clocks": clk.summary()}
-            products = {"bf16x3": 3, "bf16x6": 6}.get(path)
+            products = {"bf16x3": 3, "bf16x6": 6, "fp16x3": 3}.get(path)
             if products and peaks.get("bf16_tflops"):
                 line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
                 line["tensor_peak"] = (f"{products} BF16 products per algorithmic flop vs bf16_tflops "
@@ -1393,7 +1393,7 @@ def main():
     ap.add_argument("--batch-accuracy", default="bf16x3", choices=["bf16x3", "bf16x6"])
     ap.add_argument("--gemm-n", type=int, default=8192)
     ap.add_argument("--gemm-iters", type=int, default=5)
-    ap.add_argument("--paths", default="bf16x3,bf16x6,fp8,fp32",
+    ap.add_argument("--paths", default="bf16x3,bf16x6,fp16x3,fp8,fp32",
                     help="precision workload: comma-separated GEMM paths to run")
     ap.add_argument("--sets", default="uniform,wide", help="precision workload: input sets to run")
     ap.add_argument("--f64-paths", default="auto,digits7,digits8,fp64",

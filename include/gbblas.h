@@ -81,8 +81,13 @@ typedef enum gbblas_accuracy {
                                        products of weight < 7 summed exactly; error at most
                                        about 4 K 2^-53 max_k|a_ik| max_k|b_kj| (the FP64
                                        bound has sum_k |a_ik||b_kj| there); K <= 2^20 */
-  GBBLAS_ACCURACY_FP64_DIGITS8 = 7  /* the same with 8 digits (36 products): 2^-8 of that
+  GBBLAS_ACCURACY_FP64_DIGITS8 = 7, /* the same with 8 digits (36 products): 2^-8 of that
                                        error; K <= 2^20 */
+  /* Single-precision GEMM: */
+  GBBLAS_ACCURACY_FP16X3 = 8        /* FP32-accurate, three tcgen05 products: every row of A
+                                       and column of B scaled by a power of two into FP16's
+                                       range and split a = h + l in FP16 (22 significand
+                                       bits), h*h + h*l + l*h with FP32 accumulation */
 } gbblas_accuracy;
 
 /* ---------------------------------------------------------------- library */

@@ -334,7 +334,7 @@ gbblas_status gbblas_batch_create(const gbblas_gemm_desc* gemms, int64_t ngemm, 
     set_error("gbblas_batch_create: bad arguments");
     return GBBLAS_STATUS_INVALID_VALUE;
   }
-  if ((int)accuracy < 0 || (int)accuracy > 4) {
+  if (((int)accuracy < 0 || (int)accuracy > 4) && accuracy != GBBLAS_ACCURACY_FP16X3) {
     set_error("gbblas_batch_create: unknown accuracy %d", (int)accuracy);
     return GBBLAS_STATUS_INVALID_VALUE;
   }

@@ -281,7 +281,8 @@ gbblas_status d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
 template <typename T>
 gbblas_status check_accuracy(gbblas_accuracy acc) {
   if constexpr (std::is_same_v<T, float>) {
-    if ((int)acc < 0 || (int)acc > 4) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
+    if (((int)acc < 0 || (int)acc > 4) && acc != GBBLAS_ACCURACY_FP16X3)
+      return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm: unknown accuracy %d", (int)acc);
   } else {
     if (acc != GBBLAS_ACCURACY_FP64 && acc != GBBLAS_ACCURACY_AUTO && !dgemm_digits_count(acc))
       return bad(GBBLAS_STATUS_INVALID_VALUE, "dgemm: accuracy %d is not FP64, AUTO, FP64_DIGITS7 or FP64_DIGITS8",
@@ -704,7 +705,7 @@ gbblas_status gbblas_ddot_tuning(int64_t n, const double* a, const double* b, in
 gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count, gbblas_accuracy accuracy,
                                    void* stream) {
   if (count < 0 || (count > 0 && !descs)) return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: bad arguments");
-  if ((int)accuracy < 0 || (int)accuracy > 4)
+  if (((int)accuracy < 0 || (int)accuracy > 4) && accuracy != GBBLAS_ACCURACY_FP16X3)
     return bad(GBBLAS_STATUS_INVALID_VALUE, "gemm_grouped: unknown accuracy %d", (int)accuracy);
   for (int64_t i = 0; i < count; ++i) {
     const gbblas_gemm_desc& g = descs[i];

@@ -62,6 +62,7 @@
 // per problem (split-BF16 issues 3 or 6 times that in BF16 products).
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
@@ -97,13 +98,17 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
 
 // Kernel modes: 2 / 3 = FP32 split into that many BF16 pieces; kModeFp8 =
-// E4M3 operands with one power-of-two scale per 128 elements along K.
+// E4M3 operands with one power-of-two scale per 128 elements along K;
+// kModeF16 = FP32 scaled by a power of two per row of A / column of B and
+// split into two FP16 pieces (11 significand bits each), three products.
 constexpr int kModeFp8 = 8;
+constexpr int kModeF16 = 12;
 
 template <int MODE>
 struct ModeTraits {
   static constexpr bool fp8 = MODE == kModeFp8;
-  static constexpr int P = fp8 ? 1 : MODE;     // operand planes per operand
+  static constexpr bool f16 = MODE == kModeF16;
+  static constexpr int P = fp8 ? 1 : (f16 ? 2 : MODE);  // operand planes per operand
   // Bytes of K per operand row in one K sub-tile (128-byte swizzle).  The
   // six-product split measured slower with 64-byte rows (32-K stages, 4 in
   // shared memory instead of 2): 245 vs 269 TFLOP/s at 8192^3.
@@ -114,7 +119,9 @@ struct ModeTraits {
   // bounds the four-MMA FP8 stage).
   static constexpr int kSub = fp8 ? 2 : 1;
   static constexpr int kBKe = fp8 ? 128 * kSub : kRowBytes / 2;  // K elements per stage
-  static constexpr int kChunk = fp8 ? kChunkTilesFp8 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);  // slices per TMEM chunk
+  // slices per TMEM chunk (the FP16 split folds every 128 of K, as the
+  // six-product split does: its pieces carry 22 of the 24 bits)
+  static constexpr int kChunk = fp8 ? kChunkTilesFp8 : (MODE == 2 ? kChunkTiles3 : kChunkTiles6);
   // Epilogue warps: 8 for the split, each 32 tile rows x 64 columns (with
   // 128 FP32 accumulators per thread the kernel ran out of registers and
   // spilled); 4 for FP8, each 32 rows x 128 columns (no spills).
@@ -231,6 +238,63 @@ struct PrepTile {
 // One CTA per tile.  Interior tiles of 16-byte-aligned sources are read with
 // 128-bit loads along whichever dimension is contiguous; edge tiles and other
 // strides element by element (still coalesced along the contiguous side).
+// FP16 split: e[R] for every arena row R = the frexp exponent of the row's
+// largest magnitude (so the row, scaled by 2^(15 - e), lies below 2^15 and
+// inside FP16's range).  Same tiles as the preparation; magnitudes compared
+// as bit patterns; the rows' maxima of a tile combined in shared memory and
+// then atomicMax-ed into e (which starts filled with the byte 0x80: a row no
+// tile wrote, all zero or padding, reads as 0).
+constexpr int kF16ScaleTop = 15;
+__global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restrict__ jobs, int njobs,
+                                                        int* __restrict__ e_out) {
+  constexpr int TK = 64, TR = 64;
+  __shared__ unsigned int rmax[TR];
+  __shared__ int sjob;
+  const int t = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].tile_start <= t)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    sjob = lo;
+  }
+  if (tid < TR) rmax[tid] = 0u;
+  __syncthreads();
+  const SplitJob& j = jobs[sjob];
+  const int local = t - j.tile_start;
+  const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
+  unsigned int m[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int idx = tid + 256 * i;
+    const int r = j.cs == 1 ? idx / TK : idx % TR, k = j.cs == 1 ? idx % TK : idx / TR;
+    m[i] = (r0 + r < j.rows && k0 + k < j.K)
+               ? (__float_as_uint(__ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs)) & 0x7FFFFFFFu)
+               : 0u;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int idx = tid + 256 * i;
+    const int r = j.cs == 1 ? idx / TK : idx % TR;
+    if (m[i]) atomicMax(&rmax[r], m[i]);
+  }
+  __syncthreads();
+  if (tid < TR && r0 + tid < j.rows && rmax[tid] != 0u) {
+    int e;
+    (void)frexpf(__uint_as_float(rmax[tid] >= 0x7F800000u ? 0x7F7FFFFFu : rmax[tid]), &e);  // Inf / NaN: the top exponent
+    atomicMax(e_out + j.dst_row + r0 + tid, e);
+  }
+}
+
+__device__ __forceinline__ int f16_row_exp(const int* e, int64_t row) {
+  const int v = e[row];
+  return v == (int)0x80808080 ? 0 : v;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                          void* __restrict__ out, int64_t piece_stride, int64_t pitch,
@@ -318,6 +382,34 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
       if (lane == 0)
         scales[(row >> 7) * scale_stride + k0 + 4 * (row & 31) + ((row >> 5) & 3)] =
             (uint32_t)(127 + e) * 0x01010101u;
+    }
+  } else if constexpr (MODE == kModeF16) {
+    // half-warp per row as below; the row scaled by 2^(15 - e) (exact), then
+    // h = fp16_rn(v), l = fp16_rn(v - h) (v - h exact in FP32)
+    __half* ph = static_cast<__half*>(out);
+    const int* erow = reinterpret_cast<const int*>(scales);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = warp * 8 + 2 * i + (lane >> 4), kk = (lane & 15) * 4;
+      const int64_t arow = j.dst_row + r0 + r;
+      const int sh = kF16ScaleTop - f16_row_exp(erow, arow);
+      float4 v = *reinterpret_cast<const float4*>(&tile[r * LD + kk]);
+      v = make_float4(ldexpf(v.x, sh), ldexpf(v.y, sh), ldexpf(v.z, sh), ldexpf(v.w, sh));
+      const int64_t base = arow * pitch + k0 + kk;
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const __half2 h01 = __floats2half2_rn(v.x, v.y);
+        const __half2 h23 = __floats2half2_rn(v.z, v.w);
+        uint2 w;
+        w.x = *reinterpret_cast<const uint32_t*>(&h01);
+        w.y = *reinterpret_cast<const uint32_t*>(&h23);
+        *reinterpret_cast<uint2*>(ph + p * piece_stride + base) = w;
+        const float2 f01 = __half22float2(h01), f23 = __half22float2(h23);
+        v.x -= f01.x;
+        v.y -= f01.y;
+        v.z -= f23.x;
+        v.w -= f23.y;
+      }
     }
   } else {
     // half-warp per row: rows 8w + 2i + (lane / 16), lane % 16: 4 consecutive K of 64
@@ -580,11 +672,12 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         if (t < 0) break;
       }
     } else if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(BMT, kBN);  // split-BF16; M = 256 for a pair
+      // split-BF16 (FP16 pieces for kModeF16); M = 256 for a pair
+      constexpr uint32_t idesc = MT::f16 ? idesc_f16_f32(BMT, kBN) : idesc_bf16_f32(BMT, kBN);
       // single CTAs: p0*[q0; q1] as one N = 256 MMA - the q0 and q1 tiles of
       // B^T lie back to back in the stage and the main and correction
       // accumulators side by side in TMEM, so A's p0 is read once for both
-      constexpr uint32_t idesc_n256 = idesc_bf16_f32(kBM, 2 * kBN);
+      constexpr uint32_t idesc_n256 = MT::f16 ? idesc_f16_f32(kBM, 2 * kBN) : idesc_bf16_f32(kBM, 2 * kBN);
       int consumed = 0;  // K slices consumed (all tiles)
       int chunk_g = 0;   // chunks started (all tiles)
       bool stop = false;
@@ -763,6 +856,14 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       if (!ok) break;
       const int aborted = __shfl_sync(0xffffffffu, *abort_flag, 0);
       if (aborted) break;
+      if constexpr (MT::f16) {
+        // undo the row and column scales: acc * 2^(e_i + f_j - 30)
+        const int* ea = reinterpret_cast<const int*>(sa);
+        const int* eb = reinterpret_cast<const int*>(sb);
+        const int ei = f16_row_exp(ea, (int64_t)pr.a_row + m0 + q * 32 + lane) - 2 * kF16ScaleTop;
+#pragma unroll
+        for (int c = 0; c < kCols; ++c) acc[c] = ldexpf(acc[c], ei + f16_row_exp(eb, (int64_t)pr.b_row + n0 + col0 + c));
+      }
       if constexpr (MT::fp8) {
         if (pr.c_tma) {
           // C += the warp's 32 rows, 32 columns at a time, by TMA reduce-add
@@ -978,7 +1079,8 @@ struct TcGroupPlan {
   CUtensorMap map_a, map_b;
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool fp8() const { return mode == kModeFp8; }
-  int planes() const { return fp8() ? 1 : mode; }
+  bool f16() const { return mode == kModeF16; }
+  int planes() const { return fp8() ? 1 : (f16() ? 2 : mode); }
   int slice_k() const {  // K elements per stage
     return fp8() ? ModeTraits<kModeFp8>::kBKe : (mode == 3 ? ModeTraits<3>::kBKe : ModeTraits<2>::kBKe);
   }
@@ -997,7 +1099,7 @@ namespace {
 // GBBLAS_TC_PAIR setting).
 gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl,
                          const TcLaunchOpts& opt = TcLaunchOpts()) {
-  if (mode != 2 && mode != 3 && mode != kModeFp8) {
+  if (mode != 2 && mode != 3 && mode != kModeFp8 && mode != kModeF16) {
     set_error("tensor-core gemm: unknown mode %d", mode);
     return GBBLAS_STATUS_INVALID_VALUE;
   }
@@ -1022,7 +1124,7 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   bool want_pair = opt.pair == 1;
   if (opt.pair < 0)
     if (const char* e = std::getenv("GBBLAS_TC_PAIR"); e && e[0] == '1') want_pair = true;
-  if (want_pair && mode != kModeFp8) {
+  if (want_pair && mode != kModeFp8 && mode != kModeF16) {
     double w1 = 0, w2 = 0;
     for (int64_t i : order) {
       const double nk = (double)round_up(d[i].N, kBN) * (double)round_up(d[i].K, pk);
@@ -1097,7 +1199,9 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   pl.off_arena = pl.off_red + align256(sizeof(SplitReduce) * pl.reds.size());
   const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
   pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
-  const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : 0;  // one 4-byte scale word per row and K-block
+  // FP8: one 4-byte scale word per row and K-block; FP16 split: one
+  // 4-byte power-of-two exponent per row
+  const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : (pl.f16() ? 1 : 0);
   pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
   pl.off_ws = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
   pl.bytes = pl.off_ws + align256((size_t)ws);
@@ -1220,6 +1324,15 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+  if constexpr (MODE == kModeF16) {
+    // per-row exponents of A's and B^T's arena rows, then the pieces
+    GB_CUDA_TRY(cudaMemsetAsync(scales_a(pl), 0x80, sizeof(int) * (size_t)pl.a_rows, stream));
+    GB_CUDA_TRY(cudaMemsetAsync(scales_b(pl), 0x80, sizeof(int) * (size_t)pl.b_rows, stream));
+    f16_scale_kernel<<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, reinterpret_cast<int*>(scales_a(pl)));
+    GB_TRY(check_launch("f16_scale_kernel(A)"));
+    f16_scale_kernel<<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, reinterpret_cast<int*>(scales_b(pl)));
+    GB_TRY(check_launch("f16_scale_kernel(B)"));
+  }
   // FP8 scale words: 128 per K-block of each 128-row block, i.e. `kpad` per row block
   prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, arena_a(pl),
                                                           (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
@@ -1230,7 +1343,7 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                                                           pl.kpad);
   GB_TRY(check_launch("prep_group_kernel(B)"));
   gbblas_status st;
-  if constexpr (MODE != kModeFp8) {
+  if constexpr (MODE != kModeFp8 && MODE != kModeF16) {
     st = pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
                  : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
   } else {
@@ -1256,15 +1369,17 @@ int tc_mode(gbblas_accuracy acc) {
     case GBBLAS_ACCURACY_BF16X3: return 2;
     case GBBLAS_ACCURACY_BF16X6: return 3;
     case GBBLAS_ACCURACY_FP8: return kModeFp8;
+    case GBBLAS_ACCURACY_FP16X3: return kModeF16;
     default: return 0;
   }
 }
 
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
   const bool fp8 = mode == kModeFp8;
-  const int64_t planes = fp8 ? 1 : mode, sk = fp8 ? ModeTraits<kModeFp8>::kBKe : kBK;
+  const int64_t planes = fp8 ? 1 : (mode == kModeF16 ? 2 : mode), sk = fp8 ? ModeTraits<kModeFp8>::kBKe : kBK;
   const int64_t rows = round_up(M, 2 * kBM) + round_up(N, kBN), Kp = round_up(K, sk);
-  return (size_t)(rows * (Kp * (fp8 ? 1 : 2) + kPitchPadBytes) * planes + (fp8 ? rows * (Kp / 128) * 4 : 0));
+  return (size_t)(rows * (Kp * (fp8 ? 1 : 2) + kPitchPadBytes) * planes + (fp8 ? rows * (Kp / 128) * 4 : 0) +
+                  (mode == kModeF16 ? rows * 4 : 0));
 }
 
 void tc_prepare(DeviceCtx* c) {
@@ -1273,6 +1388,7 @@ void tc_prepare(DeviceCtx* c) {
   kernel_setup<2, false>(c);
   kernel_setup<3, false>(c);
   kernel_setup<kModeFp8, false>(c);
+  kernel_setup<kModeF16, false>(c);
   kernel_setup<2, true>(c);
   kernel_setup<3, true>(c);
 }
@@ -1281,6 +1397,7 @@ gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t 
   switch (pl->mode) {
     case 3: return launch_bound<3>(c, *pl, stream, max_ctas);
     case kModeFp8: return launch_bound<kModeFp8>(c, *pl, stream, max_ctas);
+    case kModeF16: return launch_bound<kModeF16>(c, *pl, stream, max_ctas);
     default: return launch_bound<2>(c, *pl, stream, max_ctas);
   }
 }

@@ -450,7 +450,7 @@ gbblas_status gbblas_server_submit(gbblas_server s, const gbblas_request* r, uin
   }
   if (r->op < GBBLAS_OP_MTM || r->op > GBBLAS_OP_DOT || (r->dtype != GBBLAS_F32 && r->dtype != GBBLAS_F64) ||
       (r->layout != GBBLAS_FIRST_ORDER && r->layout != GBBLAS_LAST_ORDER) || r->accuracy < 0 ||
-      r->accuracy > (r->dtype == GBBLAS_F64 ? 7 : 4)) {
+      (r->dtype == GBBLAS_F64 ? r->accuracy > 7 : (r->accuracy > 4 && r->accuracy != GBBLAS_ACCURACY_FP16X3))) {
     set_error("gbblas_server_submit: bad op, dtype, layout or accuracy");
     return GBBLAS_STATUS_INVALID_VALUE;
   }

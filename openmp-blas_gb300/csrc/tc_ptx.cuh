@@ -244,6 +244,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
+// The same with F16 A/B (format 0 in bits 7-9 and 10-12).
+__host__ __device__ constexpr uint32_t idesc_f16_f32(uint32_t M, uint32_t N) {
+  return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
 // Instruction descriptor for kind::mxf8f6f4 with E4M3 A/B (format 0 in bits
 // 7-9 and 10-12), F32 D, both K-major, UE8M0 scales (bit 23): bits 4-5 pick
 // the byte of B's scale word, 29-30 that of A's; same N / M fields.

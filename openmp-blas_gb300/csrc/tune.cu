@@ -331,7 +331,8 @@ TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t
   const char* pe = std::getenv("GBBLAS_TC_PAIR");
   const bool pair_env = pe && pe[0];
   const int single = pair_env ? -1 : 0;
-  const bool pairs = !pair_env && mode != tc_mode(GBBLAS_ACCURACY_FP8) && M >= 256 &&
+  const bool pairs = !pair_env && mode != tc_mode(GBBLAS_ACCURACY_FP8) && mode != tc_mode(GBBLAS_ACCURACY_FP16X3) &&
+                     M >= 256 &&
                      (double)((M + 255) / 256 * 256) <= 1.1 * (double)((M + 127) / 128 * 128);
   // without measurements: the largest listed split (the tiles alone leave
   // most SMs idle) and the GBBLAS_TC_PAIR setting

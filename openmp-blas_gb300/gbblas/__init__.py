@@ -26,6 +26,7 @@ ACCURACY_BF16X6 = 4
 ACCURACY_FP64 = 5          # double GEMM on the FP64 pipes
 ACCURACY_FP64_DIGITS7 = 6  # double GEMM, Ozaki scheme on the BF16 tensor cores, 7 digits
 ACCURACY_FP64_DIGITS8 = 7  # the same with 8 digits
+ACCURACY_FP16X3 = 8        # float GEMM: scaled FP16 hi + lo, three tcgen05 products
 
 STATUS = {
     0: "SUCCESS", 1: "INVALID_VALUE", 2: "SHAPE_MISMATCH", 3: "ALLOC_FAILED",

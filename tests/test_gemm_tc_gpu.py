@@ -19,13 +19,23 @@ pytestmark = pytest.mark.gpu
 
 BF16X3 = 1
 BF16X6 = 4
-MODES = [BF16X3, BF16X6]
+FP16X3 = 8
+MODES = [BF16X3, BF16X6, FP16X3]
 
 # Per-product error of hi*hi + hi*lo + lo*hi: the dropped lo*lo and the split
 # residuals are each <= 2^-16 of |a||b| (BF16 keeps 8 significant bits, so
 # |a - hi| <= 2^-9 |a| and |a - hi - lo| <= 2^-17 |a|); FP32 accumulation adds
 # K * eps32 at most.  Tolerance: 2^-14 + 2 K eps32 times (|A||B|)_ij.
 def split_tol(absA, absB, K, mode=BF16X3):
+    if mode == FP16X3:
+        # rows / columns scaled by 2^(15 - e) into FP16's range; h + l keeps 22
+        # bits of a normal element (|a - h - l| <= 2^-22 |a|), and an element's
+        # lo in FP16's subnormal range is off by at most 2^-25 of 2^(e - 15);
+        # the dropped l*l is below 2^-22 |a||b|
+        sa = np.ldexp(1.0, np.frexp(absA.max(axis=1) if absA.shape[1] else np.zeros(absA.shape[0]))[1])
+        sb = np.ldexp(1.0, np.frexp(absB.max(axis=0) if absB.shape[0] else np.zeros(absB.shape[1]))[1])
+        return ((2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB) +
+                2.0 ** -38 * max(K, 1) * np.outer(sa, sb))
     if mode == BF16X6:  # all 24 bits kept; dropped products below 2^-23 of |a||b|
         return (2.0 ** -21 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
     return (2.0 ** -14 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
@@ -148,10 +158,12 @@ def test_auto_accuracy_small_uses_fp32_path(cuda):
     np.testing.assert_array_equal(run(cuda, A, B, Z, 1, 1, 1, accuracy=3), run(cuda, A, B, Z, 1, 1, 1, accuracy=0))
 
 
+@pytest.mark.parametrize("mode", [BF16X6, FP16X3])
 @pytest.mark.parametrize("dataset", ["uniform", "wide"])
-def test_six_products_at_most_fp32_max_relative_error(cuda, dataset):
-    """M = N = K = 1024 (seed 12): the six-product split's largest
-    elementwise relative error against FP64 is no larger than plain FP32's,
+def test_six_products_at_most_fp32_max_relative_error(cuda, dataset, mode):
+    """M = N = K = 1024 (seed 12): the six-product BF16 split's and the
+    three-product FP16 split's largest elementwise relative error against
+    FP64 is no larger than plain FP32's,
     on U[-1,1) and on s * m * 2^e (e in [-10, 10]) operands."""
     rng = np.random.default_rng(12)
     n = 1024
@@ -166,7 +178,7 @@ def test_six_products_at_most_fp32_max_relative_error(cuda, dataset):
     Z = np.zeros((n, n), np.float32)
     exact = A.astype(np.float64) @ B.astype(np.float64)
     denom = np.maximum(np.abs(exact), 1e-300)
-    r6 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=BF16X6) - exact) / denom)
+    r6 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=mode) - exact) / denom)
     r32 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=0) - exact) / denom)
-    print(f"{dataset}: max relative error bf16x6 {r6:.3e}  fp32 {r32:.3e}")
+    print(f"{dataset}: max relative error mode {mode} {r6:.3e}  fp32 {r32:.3e}")
     assert r6 <= r32
