@@ -272,8 +272,9 @@ def fma_peak_tflops(clocks=None):
 def gemm_headline(dev, sp):
     """The first part of the headline metric beside the bandwidth line
     (outside the timed region): C = A*B at M = N = K = 8192 from float32
-    U[-1,1) (seed 2), split-BF16 with six products (FP32-accurate) and three
-    products against plain FP32 FMA; 2*M*N*K algorithmic flops, CUDA events
+    U[-1,1) (seed 2), split-BF16 with six products (FP32-accurate), split-FP16
+    with three (FP32-accurate on these operands) and split-BF16 with three
+    against plain FP32 FMA; 2*M*N*K algorithmic flops, CUDA events
     over 3 calls after 1 warm-up; max / mean relative error against
     long-double dots on 1024 sampled entries.  The full two-input-set report
     is `--workload precision`."""
@@ -293,7 +294,7 @@ def gemm_headline(dev, sp):
     exact, _ = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
     out = {"config": "M=N=K=8192 float32 U[-1,1) seed 2, 2*M*N*K flops", "unit": "TFLOP/s"}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for path, acc in (("bf16x6", 4), ("bf16x3", 1), ("fp32", 0)):
+    for path, acc in (("bf16x6", 4), ("fp16x3", 8), ("bf16x3", 1), ("fp32", 0)):
         def call():
             gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1, acc, sp)
         call()
@@ -318,8 +319,10 @@ def gemm_headline(dev, sp):
         if bf16:  # BF16 products per algorithmic flop against the measured BF16 burst
             out["bf16x6"]["tensor_frac"] = round(6 * out["bf16x6"]["value"] / bf16, 4)
             out["bf16x3"]["tensor_frac"] = round(3 * out["bf16x3"]["value"] / bf16, 4)
+            out["fp16x3"]["tensor_frac"] = round(3 * out["fp16x3"]["value"] / bf16, 4)
     out["bf16x6_over_fp32"] = round(out["bf16x6"]["value"] / out["fp32"]["value"], 2)
     out["bf16x3_over_fp32"] = round(out["bf16x3"]["value"] / out["fp32"]["value"], 2)
+    out["fp16x3_over_fp32"] = round(out["fp16x3"]["value"] / out["fp32"]["value"], 2)
     del A, B, C
     torch.cuda.empty_cache()
     return out
