@@ -81,7 +81,7 @@ void pack(ValueType* out, SizeType const wo, ValueType const* in, SizeType const
 namespace gpu {
 
 /// GEMM arithmetic (see gbblas_accuracy in gbblas.h).  float: fp32 (the
-/// default), bf16x3, fp8, automatic, bf16x6.  double: fp32 (the default:
+/// default), bf16x3, fp8, automatic, bf16x6, fp16x3.  double: fp32 (the default:
 /// gbblas_dgemm's - automatic unless GBBLAS_DGEMM_FP64=1), automatic (the
 /// guarded tensor-core digits where faster), fp64 (the FP64 pipes),
 /// fp64_digits7 / fp64_digits8 (unguarded tensor-core digits).
@@ -94,6 +94,7 @@ enum class accuracy : int {
   fp64 = GBBLAS_ACCURACY_FP64,
   fp64_digits7 = GBBLAS_ACCURACY_FP64_DIGITS7,
   fp64_digits8 = GBBLAS_ACCURACY_FP64_DIGITS8,
+  fp16x3 = GBBLAS_ACCURACY_FP16X3,
 };
 
 /// Throw std::runtime_error for a failed C-ABI call (the reference reports
