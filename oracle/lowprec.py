@@ -15,6 +15,11 @@ wrong kernel (a mismatch against this model):
 * C = sum over blocks of s_a * s_b * (q_a . q_b), the dot products exact
   (E4M3 products are exact in FP32), only the final FP32 sums round.
 
+It also restates the split-FP16 path's operand preparation
+(GBBLAS_ACCURACY_FP16X3): a power-of-two scale per row into FP16's range and
+the split into FP16 hi + lo pieces, with the truncation bound its GPU tests
+use.
+
 Only tests/ and bench.py's precision report import this module.
 """
 from __future__ import annotations
@@ -88,3 +93,30 @@ def gemm_fp8_abs_model(A: np.ndarray, B: np.ndarray) -> np.ndarray:
         sl = slice(b * BLOCK, (b + 1) * BLOCK)
         out += (np.abs(qa[:, sl]) @ np.abs(qb[:, sl]).T) * sa[:, b:b + 1] * sb[:, b][None, :]
     return out
+
+
+# ---------------------------------------------------------------- split-FP16
+F16_SCALE_TOP = 15  # a row scaled by 2^(15 - e) lies below 2^15, inside FP16's range
+
+
+def f16_split_rows(X: np.ndarray):
+    """The split-FP16 path's operand preparation for rows of X (float32,
+    rows x K): e = the frexp exponent of each row's largest magnitude (0 for
+    an all-zero row), v = x 2^(15 - e) (exact), h = fp16_rn(v),
+    l = fp16_rn(v - h).  Returns (h, l, e) with h, l in the scaled units."""
+    X = np.asarray(X, np.float32)
+    amax = np.abs(X).max(axis=1) if X.shape[1] else np.zeros(X.shape[0], np.float32)
+    e = np.frexp(amax.astype(np.float64))[1]
+    e[amax == 0] = 0
+    v = np.ldexp(X.astype(np.float32), (F16_SCALE_TOP - e)[:, None].astype(np.int32)).astype(np.float32)
+    h = v.astype(np.float16).astype(np.float32)
+    l = (v - h).astype(np.float16).astype(np.float32)
+    return h, l, e
+
+
+def f16_split_error_bound(X: np.ndarray) -> np.ndarray:
+    """|x - (h + l) 2^(e - 15)| <= 2^-22 |x| + 2^-25 2^(e - 15) elementwise:
+    22 bits of a normal element, and an l in FP16's subnormal range off by
+    half its 2^-24 spacing."""
+    _, _, e = f16_split_rows(X)
+    return 2.0 ** -22 * np.abs(np.asarray(X, np.float64)) + np.ldexp(2.0 ** -25, (e - F16_SCALE_TOP)[:, None])

@@ -1,6 +1,7 @@
-"""The FP8 arithmetic model (oracle/lowprec.py) pinned on the CPU: E4M3
+"""The low-precision models (oracle/lowprec.py) pinned on the CPU: E4M3
 rounding against PyTorch's own float8_e4m3fn cast and hand-checked values,
-block scales against their definition."""
+block scales against their definition, and the split-FP16 preparation
+against its truncation bound."""
 import numpy as np
 import pytest
 
@@ -44,3 +45,24 @@ def test_model_exact_on_small_integers():
     A = rng.integers(-8, 9, (40, 300)).astype(np.float32)
     B = rng.integers(-8, 9, (300, 24)).astype(np.float32)
     np.testing.assert_array_equal(L.gemm_fp8_model(A, B), A.astype(np.float64) @ B)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "wide", "tiny"])
+def test_f16_split_within_its_bound(kind):
+    """The split-FP16 preparation: scaled rows stay inside FP16's range and
+    h + l reproduces every element within the bound the GPU tests assume."""
+    rng = np.random.default_rng(9)
+    shape = (64, 512)
+    if kind == "uniform":
+        X = rng.uniform(-1, 1, shape)
+    elif kind == "wide":
+        X = rng.choice([-1.0, 1.0], shape) * rng.uniform(1, 2, shape) * np.ldexp(1.0, rng.integers(-10, 11, shape))
+    else:  # magnitudes spread over 2^-40 .. 2^0 within each row
+        X = rng.uniform(-1, 1, shape) * np.ldexp(1.0, rng.integers(-40, 1, shape))
+    X = X.astype(np.float32)
+    X[5] = 0.0
+    h, l, e = L.f16_split_rows(X)
+    assert np.isfinite(h).all() and np.abs(h).max() <= 2.0 ** 15
+    rec = (h.astype(np.float64) + l.astype(np.float64)) * np.ldexp(1.0, (e - L.F16_SCALE_TOP)[:, None])
+    assert (np.abs(rec - X.astype(np.float64)) <= L.f16_split_error_bound(X)).all()
+    assert (h[5] == 0).all() and (l[5] == 0).all()
