@@ -1,5 +1,6 @@
 // gemm_tc.cu - GEMM on the 5th-generation tensor cores, single and grouped:
-// FP32-accurate (split-BF16) and low-accuracy (FP8-E4M3, block-scaled).
+// FP32-accurate (split-BF16; split-FP16 on scaled operands) and low-accuracy
+// (FP8-E4M3, block-scaled).
 // C += A * B for float A, B, C of any layout; a group is any number of
 // independent problems of any shapes.
 //
@@ -10,6 +11,10 @@
 //      prep_group_kernel, split-BF16: every FP32 element a becomes P BF16 pieces
 //        p0 = bf16_rn(a), p1 = bf16_rn(a - p0), p2 = bf16_rn(a - p0 - p1),
 //        piece planes one after another.
+//      prep_group_kernel, split-FP16: every row of A / column of B is scaled
+//        by 2^(15 - e) (e from f16_scale_kernel: the frexp exponent of its
+//        largest magnitude) and split h = fp16_rn(v), l = fp16_rn(v - h);
+//        the epilogue multiplies by 2^(e_i + f_j - 30) again.
 //      prep_group_kernel, FP8: every 128-element K-block of a row becomes
 //        128 E4M3 values and one power-of-two scale, kept as its UE8M0
 //        exponent byte in 512-byte atoms (128 rows of one K-block) beside
