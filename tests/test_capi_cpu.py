@@ -108,3 +108,14 @@ def test_descriptor_structs_match_the_c_layout(tmp_path):
     want += [getattr(gbblas.GemmDesc, f).offset for f in fields_g]
     want += [getattr(gbblas.GemvDesc, f).offset for f in fields_v]
     assert out == want
+
+
+def test_accuracy_constants_match_the_header():
+    """The binding's ACCURACY_* values are the header's gbblas_accuracy values."""
+    import re
+    text = open(os.path.join(ROOT, "include", "gbblas.h")).read()
+    enum = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"GBBLAS_ACCURACY_(\w+)\s*=\s*(\d+)", text))
+    assert {"FP32", "BF16X3", "FP8", "AUTO", "BF16X6", "FP64", "FP64_DIGITS7", "FP64_DIGITS8", "FP16X3"} <= set(enum)
+    for name, value in enum.items():
+        assert getattr(gbblas, "ACCURACY_" + name) == value, name
+    assert len(set(enum.values())) == len(enum)
