@@ -80,6 +80,8 @@ def step_bytes() -> int:
 def config(extra=None):
     c = {"workload": WORKLOAD, "M": M, "N": N, "dot_n": NDOT, "layout": "row-major",
          "dtypes": ["f32", "f64"], "bytes_per_step": step_bytes(),
+         "inputs": "std::mt19937_64(1) draws A, x, a, b in order; U[-1,1) = (draw >> 11) 2^-52 - 1 "
+                   "(double), (draw >> 40) 2^-23 - 1 (float)",
          "l2": "inputs larger than L2 (no flush needed)"}
     if extra:
         c.update(extra)
@@ -204,12 +206,67 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU side
 
-def cpu_step_oracle(bufs) -> None:
+def cpu_step_oracle(bufs):
+    """One step on the host cores through the oracle's restatement of the
+    reference's OpenMP code (oracle/oracle.c; its entry points work on the
+    caller's buffers, where the compiled reference's test wrappers copy each
+    operand into a tensor first).  Returns the two dot values."""
     from oracle import oracle as O
     O.mtv_raw(1, M, N, bufs["A32"], bufs["x32"], bufs["y32"])
-    O.dot(bufs["a32"], bufs["b32"])
+    r32 = O.dot(bufs["a32"], bufs["b32"])
     O.mtv_raw(1, M, N, bufs["A64"], bufs["x64"], bufs["y64"])
-    O.dot(bufs["a64"], bufs["b64"])
+    r64 = O.dot(bufs["a64"], bufs["b64"])
+    return r32, r64
+
+
+def oracle_errors(host, y32, y64, results):
+    """Every output of the GPU step against the oracle's restatement of the
+    reference on the same inputs: max |gpu - oracle| / (2 K eps (|A||x|)_i)
+    for mtv (the parity tolerance is 1) and the same ratio for the dots,
+    plus the dots against the exact sum (long double)."""
+    import numpy as np
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    out = {}
+    for tag, y in (("32", y32), ("64", y64)):
+        A, x = host["A" + tag].numpy(), host["x" + tag].numpy()
+        dt = A.dtype
+        eps = float(np.finfo(dt).eps)
+        ref = np.zeros(M, dt)
+        O.mtv_raw(1, M, N, A, x, ref)
+        absA = np.abs(A)
+        absx = np.abs(x)
+        scale = np.zeros(M, dt)
+        O.mtv_raw(1, M, N, absA, absx, scale)
+        del absA
+        tol = 2 * N * eps * scale.astype(np.float64) + np.finfo(np.float64).tiny
+        err = np.abs(np.asarray(y, np.float64) - ref.astype(np.float64))
+        out["mtv_f" + tag] = {"max_err_over_tol": float((err / tol).max()), "max_abs_err": float(err.max()),
+                              "oracle_sum": float(ref.astype(np.float64).sum())}
+        a, b = host["a" + tag].numpy(), host["b" + tag].numpy()
+        rd = float(O.dot(a, b))
+        exact, absdot = O.dot_exact(a, b)
+        got = results["dot_f" + tag]
+        out["dot_f" + tag] = {"oracle": rd, "exact": exact,
+                              "err_over_tol": abs(got - rd) / (2 * NDOT * eps * absdot),
+                              "rel_err_vs_exact": abs(got - exact) / abs(exact)}
+    out["tolerance"] = "|gpu - oracle| <= 2 K eps (|A||x|) elementwise (K = reduction length); ratio <= 1 passes"
+    return out
+
+
+def link_rate(buf, dev) -> float:
+    """Host-to-device copy rate (GB/s) of a pinned host tensor, best of 5."""
+    import torch
+    d = torch.empty_like(buf, device=dev)
+    best = 0.0
+    for _ in range(5):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.copy_(buf, non_blocking=True)
+        torch.cuda.synchronize()
+        best = max(best, buf.numel() * buf.element_size() / (time.perf_counter() - t0) / 1e9)
+    del d
+    return best
 
 
 def cpu_buffers_from(host):
@@ -218,17 +275,36 @@ def cpu_buffers_from(host):
         "y32": np.zeros(M, np.float32), "y64": np.zeros(M, np.float64)}
 
 
+INPUT_KEYS = ("A", "x", "a", "b")
+
+
+def input_counts():
+    """Segment lengths of the bandwidth configuration's seeded inputs, drawn
+    in this order from one std::mt19937_64(SEED): A (M*N), x (N), a, b (NDOT)."""
+    return [M * N, N, NDOT, NDOT]
+
+
 def make_cpu_inputs():
-    """Seeded U[-1,1) inputs generated on the CPU (reference arm)."""
-    import numpy as np
-    rng = np.random.default_rng(SEED)
+    """The seeded inputs as numpy arrays, drawn by the oracle's own
+    restatement of the generator (reference arm: no GPU library loaded)."""
+    from oracle import oracle as O
+    f32, f64 = O.seeded_fill(SEED, input_counts())
     out = {}
-    for tag, dt in (("32", np.float32), ("64", np.float64)):
-        out["A" + tag] = rng.uniform(-1, 1, M * N).astype(dt)
-        out["x" + tag] = rng.uniform(-1, 1, N).astype(dt)
-        out["a" + tag] = rng.uniform(-1, 1, NDOT).astype(dt)
-        out["b" + tag] = rng.uniform(-1, 1, NDOT).astype(dt)
+    for k, a, b in zip(INPUT_KEYS, f32, f64):
+        out[k + "32"], out[k + "64"] = a, b
     return out
+
+
+def step_results(y32, y64, r32, r64):
+    """The numbers both arms print for one step's outputs: dot values and
+    checksums of y (sum, sum of squares, first and last entry, in float64),
+    so results on the shared seeded inputs can be compared across arms."""
+    import numpy as np
+
+    def summary(y):
+        y = np.asarray(y, np.float64)
+        return {"sum": float(y.sum()), "sumsq": float((y * y).sum()), "first": float(y[0]), "last": float(y[-1])}
+    return {"mtv_f32": summary(y32), "mtv_f64": summary(y64), "dot_f32": float(r32), "dot_f64": float(r64)}
 
 
 def time_cpu(bufs, min_seconds=10.0, max_steps=50):
@@ -246,8 +322,8 @@ def time_cpu(bufs, min_seconds=10.0, max_steps=50):
 
 
 def cpu_kind():
-    from oracle import oracle as O
-    return "reference" if O.ref_available() else "port"
+    """The bandwidth step on the CPU always runs the oracle port."""
+    return "port"
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -269,63 +345,143 @@ def fma_peak_tflops(clocks=None):
     return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
 
 
-def gemm_headline(dev, sp):
-    """The first part of the headline metric beside the bandwidth line
-    (outside the timed region): C = A*B at M = N = K = 8192 from float32
-    U[-1,1) (seed 2), split-BF16 with six products (FP32-accurate), split-FP16
-    with three (FP32-accurate on these operands) and split-BF16 with three
-    against plain FP32 FMA; 2*M*N*K algorithmic flops, CUDA events
-    over 3 calls after 1 warm-up; max / mean relative error against
-    long-double dots on 1024 sampled entries.  The full two-input-set report
-    is `--workload precision`."""
+PRECISION_PATHS = (("bf16x6", 4, 6), ("fp16x3", 8, 3), ("bf16x3", 1, 3), ("fp8", 2, None), ("fp32", 0, None))
+
+
+def precision_inputs(n, set_name):
+    """The precision configuration's float32 operands on the host: one
+    std::mt19937_64(2) draws A then B, as U[-1,1) ("uniform") or as the
+    wide-range set s*m*2^e, m in [1, 2), e in [-10, 10] ("wide")."""
+    import numpy as np
+
+    import gbblas
+    A, B = np.empty((n, n), np.float32), np.empty((n, n), np.float32)
+    kind = gbblas.FILL_UNIFORM if set_name == "uniform" else gbblas.FILL_WIDE
+    gbblas.seeded_fill(2, [A.reshape(-1), B.reshape(-1)], None, kind=kind)
+    return A, B
+
+
+def precision_report(n=8192, sets=("uniform", "wide"), paths=None, warmup=1, iters=3, sample=1024,
+                     full_matrix=True):
+    """C = A*B, M = N = K = n from float32 operands (the precision
+    configuration), per input set and arithmetic path: split-BF16 with six
+    or three tcgen05 products, split-FP16 with three, FP8-E4M3 with per-128
+    K-block scales and plain FP32 on the FMA pipes.  TFLOP/s of 2*M*N*K
+    algorithmic flops (CUDA events over `iters` calls after `warmup`), the
+    pipe's roofline fraction, max / mean relative error against long-double
+    dots on `sample` sampled entries (outside the timed region), and with
+    `full_matrix` the same over all M*N entries against the product on the
+    FP64 pipes.  Returns {set: {path: record}}."""
     import numpy as np
     import torch
 
     import gbblas
     from oracle import oracle as O
-    n = 8192
-    g = torch.Generator(device=dev).manual_seed(2)
-    A = torch.rand(n, n, generator=g, device=dev) * 2 - 1
-    B = torch.rand(n, n, generator=g, device=dev) * 2 - 1
-    C = torch.zeros(n, n, device=dev)
+    paths = paths or [p for p, _, _ in PRECISION_PATHS]
+    flops = 2.0 * n ** 3
     rng = np.random.default_rng(2)
-    rows, cols = rng.integers(0, n, 1024), rng.integers(0, n, 1024)
-    An, Bn = A.cpu().numpy(), B.cpu().numpy()
-    exact, _ = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
-    out = {"config": "M=N=K=8192 float32 U[-1,1) seed 2, 2*M*N*K flops", "unit": "TFLOP/s"}
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for path, acc in (("bf16x6", 4), ("fp16x3", 8), ("bf16x3", 1), ("fp32", 0)):
-        def call():
-            gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1, acc, sp)
-        call()
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(3):
+    rows, cols = rng.integers(0, n, sample), rng.integers(0, n, sample)
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(pp)) if os.path.exists(pp) else {}
+    sp = torch.cuda.current_stream().cuda_stream or None
+    report = {}
+    for set_name in sets:
+        An, Bn = precision_inputs(n, set_name)
+        exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
+        A, B = torch.from_numpy(An).cuda(), torch.from_numpy(Bn).cuda()
+        C64 = absAB = None
+        if full_matrix:
+            # C64 = A B on the FP64 pipes (the FMA kernel, independent of the
+            # tensor-core paths checked); |A||B| in FP32 for the normwise scale
+            A64, B64 = A.double(), B.double()
+            C64 = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+            gbblas.call("gbblas_dgemm_ex", n, n, n, A64.data_ptr(), n, 1, B64.data_ptr(), n, 1, C64.data_ptr(), n,
+                        1, gbblas.ACCURACY_FP64, sp)
+            del A64, B64
+            Aa, Ba = A.abs(), B.abs()
+            absAB = torch.zeros(n, n, device="cuda")
+            gbblas.call("gbblas_sgemm", n, n, n, Aa.data_ptr(), n, 1, Ba.data_ptr(), n, 1, absAB.data_ptr(), n, 1,
+                        gbblas.ACCURACY_FP32, sp)
+            del Aa, Ba
+            gbblas.call("gbblas_check_stream", sp)
+        report[set_name] = {}
+        C = torch.zeros(n, n, device="cuda")
+        for path, acc, products in PRECISION_PATHS:
+            if path not in paths:
+                continue
+
+            def call():
+                gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1,
+                            acc, sp)
+            for _ in range(warmup):
+                call()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(0) as clk:
+                t0 = time.time()
+                e0.record()
+                for _ in range(iters):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                clk.mark(t0, time.time())
+            gbblas.call("gbblas_check_stream", sp)
+            ms = e0.elapsed_time(e1) / iters
+            C.zero_()  # one clean product for the error checks
             call()
-        e1.record()
-        torch.cuda.synchronize()
-        gbblas.call("gbblas_check_stream", sp)
-        ms = e0.elapsed_time(e1) / 3
-        C.zero_()
-        call()
-        got = C.cpu().numpy()[rows, cols].astype(np.float64)
-        rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
-        out[path] = {"value": round(2.0 * n ** 3 / (ms / 1e3) / 1e12, 2), "ms": round(ms, 3),
-                     "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean())}
-    out["fp32"]["fma_frac"] = round(out["fp32"]["value"] / fma_peak_tflops(), 4)
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        bf16 = json.load(open(peaks_path)).get("bf16_tflops")
-        if bf16:  # BF16 products per algorithmic flop against the measured BF16 burst
-            out["bf16x6"]["tensor_frac"] = round(6 * out["bf16x6"]["value"] / bf16, 4)
-            out["bf16x3"]["tensor_frac"] = round(3 * out["bf16x3"]["value"] / bf16, 4)
-            out["fp16x3"]["tensor_frac"] = round(3 * out["fp16x3"]["value"] / bf16, 4)
-    out["bf16x6_over_fp32"] = round(out["bf16x6"]["value"] / out["fp32"]["value"], 2)
-    out["bf16x3_over_fp32"] = round(out["bf16x3"]["value"] / out["fp32"]["value"], 2)
-    out["fp16x3_over_fp32"] = round(out["fp16x3"]["value"] / out["fp32"]["value"], 2)
-    del A, B, C
-    torch.cuda.empty_cache()
-    return out
+            got = C.cpu().numpy()[rows, cols].astype(np.float64)
+            rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
+            tf = flops / (ms / 1e3) / 1e12
+            rec = {"value": round(tf, 2), "unit": "TFLOP/s", "ms": round(ms, 3),
+                   "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
+                   "max_normwise_err": float((np.abs(got - exact) / absx).max()), "clocks": clk.summary()}
+            if full_matrix:
+                diff = (C.double() - C64).abs_()
+                mag = C64.abs().clamp_min(1e-300)
+                rec["full_matrix_vs_fp64"] = {"max_rel_err": float((diff / mag).max()),
+                                              "mean_rel_err": float((diff / mag).mean()),
+                                              "max_normwise_err": float((diff / absAB.double().clamp_min(1e-300)).max())}
+                del diff, mag
+            if products and peaks.get("bf16_tflops"):
+                rec["roofline"] = {"bound": "tensor", "achieved": round(products * tf, 1),
+                                   "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                                   "frac": round(products * tf / peaks["bf16_tflops"], 4),
+                                   "peak_source": f"{products} BF16/FP16 products per algorithmic flop against "
+                                                  "MEASURED_PEAKS.json bf16_tflops (measured, burst)"}
+            elif path == "fp8" and peaks.get("bf16_tflops"):
+                rec["roofline"] = {"bound": "tensor", "achieved": round(tf, 1), "peak": 2 * peaks["bf16_tflops"],
+                                   "unit": "TFLOP/s", "frac": round(tf / (2 * peaks["bf16_tflops"]), 4),
+                                   "peak_source": "2 x MEASURED_PEAKS.json bf16_tflops (measured BF16 burst times "
+                                                  "the nominal FP8/BF16 ratio; no FP8 peak is measured)"}
+            elif path == "fp32":
+                fp = fma_peak_tflops(rec["clocks"])
+                rec["roofline"] = {"bound": "fma", "achieved": round(tf, 2), "peak": round(fp, 1),
+                                   "unit": "TFLOP/s", "frac": round(tf / fp, 4),
+                                   "peak_source": "SMs x 128 FP32 FMA lanes x 2 flop x max SM clock (nominal)"}
+            report[set_name][path] = rec
+        del A, B, C, C64, absAB
+        torch.cuda.empty_cache()
+    return report
+
+
+def precision_keys(report, n):
+    """The default line's two precision keys from a precision report: the
+    FP32-accurate paths against plain FP32 per set, and FP8 per set."""
+    cfg = (f"C = A*B, M = N = K = {n} from float32; std::mt19937_64(2) draws A then B: U[-1,1) "
+           "(uniform) or s*m*2^e, m in [1,2), e in [-10,10] (wide); 2*M*N*K algorithmic flops; errors vs "
+           "long-double dots on sampled entries and vs the full product on the FP64 pipes")
+    acc = {"config": cfg}
+    fp8 = {"config": cfg}
+    for set_name, rec in report.items():
+        acc[set_name] = {p: r for p, r in rec.items() if p != "fp8"}
+        if "fp32" in rec:
+            for p in ("bf16x6", "fp16x3", "bf16x3"):
+                if p in rec:
+                    acc[set_name][f"{p}_over_fp32"] = round(rec[p]["value"] / rec["fp32"]["value"], 2)
+                    acc[set_name][f"{p}_max_rel_err_below_fp32"] = rec[p]["max_rel_err"] <= rec["fp32"]["max_rel_err"]
+        if "fp8" in rec:
+            fp8[set_name] = rec["fp8"]
+    return acc, fp8
 
 
 def dgemm_headline(dev, sp):
@@ -376,6 +532,51 @@ def dgemm_headline(dev, sp):
     return out
 
 
+def default_extras(args, dev, sp):
+    """The rest of the headline metric, measured after the bandwidth step
+    (outside its timed region) so that one default run carries all of it:
+    the precision configuration (FP32-accurate paths and FP8 on both input
+    sets), double-precision GEMM, the plain 1024^3 mtm, the batching
+    configuration and the served latencies.  Each entry carries its own
+    roofline and clock record; one that fails records its error and the
+    others still run."""
+    import copy
+
+    import torch
+    out = {}
+
+    def guarded(key, fn):
+        t0 = time.perf_counter()
+        try:
+            out.update(fn()) if key is None else out.__setitem__(key, fn())
+        except Exception as e:  # keep the rest of the line
+            out[key or "precision"] = {"error": f"{type(e).__name__}: {e}"}
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return time.perf_counter() - t0
+
+    def precision():
+        rep = precision_report(8192, iters=3, sample=1024)
+        acc, fp8 = precision_keys(rep, 8192)
+        return {"fp32_accurate_gemm": acc, "fp8": fp8}
+
+    secs = {}
+    secs["precision"] = guarded(None, precision)
+    secs["fp64_gemm"] = guarded("fp64_gemm", lambda: dgemm_headline(dev, sp))
+    a = copy.copy(args)
+    a.warmup = max(3, args.warmup)
+    secs["mtm_1024"] = guarded("mtm_1024", lambda: mtm_report(a))
+    b = copy.copy(args)
+    b.steps, b.warmup, b.pool_gb, b.batch_accuracy = 5, 2, 48.0, "bf16x3"
+    secs["batching"] = guarded("batching", lambda: batching_report(b))
+    c = copy.copy(args)
+    c.rates, c.min_requests, c.max_requests, c.lone_requests, c.seconds = [5000, 10000, 20000], 4000, 4000, 4000, 0.0
+    c.pool_gb, c.f64_accuracy = 16.0, "auto"
+    secs["served"] = guarded("served", lambda: serving_report(c))
+    out["extras_seconds"] = {k: round(v, 1) for k, v in secs.items()}
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -388,19 +589,19 @@ def run_gpu(args):
     gbblas.lib()
     gbblas.call("gbblas_init")
 
-    g = torch.Generator(device=dev).manual_seed(SEED + rank)
-
-    def U(n, dt):
-        return torch.rand(n, generator=g, device=dev, dtype=dt).mul_(2).sub_(1)
-
-    t = {}
+    # The seeded inputs, drawn on the host into pinned buffers (the same values
+    # the reference arm draws; every rank the same), then uploaded once.  The
+    # pinned buffers are also the e2e step's host inputs.
+    host = {}
+    for k, n in zip(INPUT_KEYS, input_counts()):
+        host[k + "32"] = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        host[k + "64"] = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    gbblas.seeded_fill(SEED, [host[k + "32"] for k in INPUT_KEYS], [host[k + "64"] for k in INPUT_KEYS])
+    t = {k: v.to(dev) for k, v in host.items()}
     for tag, dt in (("32", torch.float32), ("64", torch.float64)):
-        t["A" + tag] = U(M * N, dt)
-        t["x" + tag] = U(N, dt)
         t["y" + tag] = torch.zeros(M, dtype=dt, device=dev)
-        t["a" + tag] = U(NDOT, dt)
-        t["b" + tag] = U(NDOT, dt)
         t["r" + tag] = torch.zeros(1, dtype=dt, device=dev)
+    torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream or None
     L = gbblas.lib()
@@ -476,8 +677,9 @@ def run_gpu(args):
     if os.path.exists(tfile):
         traffic = json.load(open(tfile)).get(dom)
 
-    # ---- results against device-side checks (cheap sanity, not the parity tests)
-    results = {"dot_f32": t["r32"].item(), "dot_f64": t["r64"].item()}
+    # ---- results on the shared seeded inputs (the reference arm prints the same keys)
+    y32, y64 = t["y32"].cpu().numpy(), t["y64"].cpu().numpy()
+    results = step_results(y32, y64, t["r32"].item(), t["r64"].item())
 
     if args.small:
         if rank == 0:
@@ -485,16 +687,10 @@ def run_gpu(args):
         return
 
     # ---- e2e: the same step through the host-buffer C ABI from pinned memory
-    host = {}
-    for k in ("A32", "x32", "a32", "b32", "A64", "x64", "a64", "b64"):
-        host[k] = torch.empty(t[k].shape, dtype=t[k].dtype, pin_memory=True)
-        host[k].copy_(t[k])
     hy32 = torch.zeros(M, dtype=torch.float32, pin_memory=True)
     hy64 = torch.zeros(M, dtype=torch.float64, pin_memory=True)
     hr32 = np.zeros(1, np.float32)
     hr64 = np.zeros(1, np.float64)
-    for k in host:
-        host[k] = host[k]
     p = {k: v.data_ptr() for k, v in host.items()}
 
     def e2e_step():
@@ -514,31 +710,45 @@ def run_gpu(args):
     barrier()
     h2d = sum(host[k].numel() * host[k].element_size() for k in host)
     d2h = M * 4 + 4 + M * 8 + 8
-    e2e = {"value": round(aggregate(sb * e2e_steps, ws, e2e_s) / 1e9, 2), "unit": UNIT,
+    e2e_val = aggregate(sb * e2e_steps, ws, e2e_s) / 1e9
+    link = link_rate(host["A64"], dev)
+    e2e = {"value": round(e2e_val, 2), "unit": UNIT,
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
-           "api": "gbblas_smtv_host/gbblas_sdot_host/gbblas_dmtv_host/gbblas_ddot_host (pinned host buffers)"}
+           "api": "gbblas_smtv_host/gbblas_sdot_host/gbblas_dmtv_host/gbblas_ddot_host (pinned host buffers)",
+           "link_gbs": round(link, 1), "frac_of_link": round(e2e_val / ws / link, 4),
+           "link": "host-to-device copy of one pinned 2 GiB buffer (cudaMemcpyAsync), best of 5, this run"}
+    # the host path must give the device path's bits on the same inputs
+    e2e_results = step_results(hy32.numpy(), hy64.numpy(), hr32[0], hr64[0])
+    e2e["same_results_as_device"] = e2e_results == results
+
+    # ---- errors against the oracle on the same inputs (outside every timed region)
+    if rank == 0 and not args.no_cpu:
+        results["vs_oracle"] = oracle_errors(host, y32, y64, results)
 
     # ---- CPU baseline (rank 0 only): the oracle on the host cores
     cpu = None
     if rank == 0 and not args.no_cpu:
-        bufs = cpu_buffers_from({k: host[k] for k in ("A32", "x32", "a32", "b32", "A64", "x64", "a64", "b64")})
+        bufs = cpu_buffers_from(host)
         times = time_cpu(bufs, min_seconds=args.cpu_seconds)
         cpu = {"value": round(sb / statistics.mean(times) / 1e9, 3), "unit": UNIT,
                "cores": os.cpu_count(), "kind": cpu_kind(),
                "sample": f"{len(times)} full steps (all four calls at full size) after 1 warm-up, "
                          f"mean {statistics.mean(times) * 1e3:.1f} ms/step, OpenMP on all host cores"}
 
-    gemm = dgemm = None
+    extras = {}
     if rank == 0 and not args.no_gemm:
-        gemm = gemm_headline(dev, sp)
-        dgemm = dgemm_headline(dev, sp)
+        t.clear()  # the step's device buffers; the pinned host inputs stay for nothing else
+        host.clear()
+        torch.cuda.empty_cache()
+        extras = default_extras(args, dev, sp)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "config": config(),
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
@@ -548,9 +758,8 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "clocks": clocks,
             "results": results,
-            "fp32_accurate_gemm": gemm,
-            "fp64_gemm": dgemm,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -577,131 +786,41 @@ def run_reference(args):
         cpu_step_oracle(bufs)
     dt = time.perf_counter() - t0
     value = step_bytes() * args.steps / dt / 1e9
+    r32, r64 = cpu_step_oracle(bufs)  # the outputs of one more step, for the results key
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic", "config": config({"parallelism": "host CPU (OpenMP)"}),
+        "data": "synthetic", "config": config(), "parallelism": "host CPU (OpenMP)",
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
                          "sample": f"{args.steps} full steps after {args.warmup} warm-up, all host cores; "
-                                   + ("reference headers compiled unmodified" if kind == "reference" else
-                                      "oracle/oracle.c restatement of the reference's OpenMP code "
-                                      "(the reference sources are not on this machine)")},
+                                   "oracle/oracle.c restatement of the reference's OpenMP code, pinned "
+                                   "against the compiled reference where its sources exist"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "results": step_results(bufs["y32"], bufs["y64"], r32, r64),
     }
     print(json.dumps(line), flush=True)
 
 
 def run_precision(args):
     """The precision configuration: C = A*B, M = N = K = 8192 from float32,
-    as split-BF16 (three or six tcgen05 products), FP8-E4M3 with per-128
-    K-block scales (tcgen05 kind::f8f6f4) and plain FP32 (FMA pipe), on two
-    input sets (U[-1,1) and wide-range s*m*2^e, e in [-10, 10]); TFLOP/s of
-    2*M*N*K algorithmic flops, max / mean relative error against long-double
-    dots on sampled entries, and the same over the full matrix against the
-    product computed on the FP64 pipes.  One JSON line per (path, set)."""
-    import numpy as np
+    as split-BF16 (three or six tcgen05 products), split-FP16 (three), FP8-E4M3
+    with per-128 K-block scales and plain FP32 (FMA pipe), on two input sets
+    (U[-1,1) and wide-range s*m*2^e, e in [-10, 10]); TFLOP/s of 2*M*N*K
+    algorithmic flops, max / mean relative error against long-double dots on
+    sampled entries, and the same over the full matrix against the product
+    computed on the FP64 pipes.  One JSON line per (path, set)."""
     import torch
-
-    import gbblas
-    from oracle import oracle as O
     torch.cuda.set_device(0)
     n = args.gemm_n
-    flops = 2.0 * n ** 3
-    g = torch.Generator(device="cuda").manual_seed(2)
-    rng = np.random.default_rng(2)
-    sample = 4096
-    rows = rng.integers(0, n, sample)
-    cols = rng.integers(0, n, sample)
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    for set_name in ("uniform", "wide"):
-        if set_name not in args.sets.split(","):
-            continue
-        if set_name == "uniform":
-            A = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
-            B = torch.rand(n, n, generator=g, device="cuda") * 2 - 1
-        else:
-            def wide():
-                s = torch.where(torch.rand(n, n, generator=g, device="cuda") < 0.5, -1.0, 1.0)
-                m = torch.rand(n, n, generator=g, device="cuda") + 1.0
-                e = torch.randint(-10, 11, (n, n), generator=g, device="cuda").float()
-                return s * m * torch.exp2(e)
-            A, B = wide(), wide()
-        An, Bn = A.cpu().numpy(), B.cpu().numpy()
-        exact, absx = O.gemm_sample_exact(n, An, n, 1, Bn, n, 1, rows, cols)
-        # full-matrix FP64 residual on the GPU: C64 = A B on the FP64 pipes
-        # (the FMA kernel, independent of the tensor-core paths checked), and
-        # |A||B| in FP32 for the normwise scale
-        sp0 = torch.cuda.current_stream().cuda_stream or None
-        A64, B64 = A.double(), B.double()
-        C64 = torch.zeros(n, n, device="cuda", dtype=torch.float64)
-        gbblas.call("gbblas_dgemm_ex", n, n, n, A64.data_ptr(), n, 1, B64.data_ptr(), n, 1, C64.data_ptr(), n, 1,
-                    5, sp0)
-        del A64, B64
-        Aa, Ba = A.abs(), B.abs()
-        absAB = torch.zeros(n, n, device="cuda")
-        gbblas.call("gbblas_sgemm", n, n, n, Aa.data_ptr(), n, 1, Ba.data_ptr(), n, 1, absAB.data_ptr(), n, 1, 0, sp0)
-        del Aa, Ba
-        gbblas.call("gbblas_check_stream", sp0)
-        for path, acc in (("bf16x3", 1), ("bf16x6", 4), ("fp16x3", 8), ("fp8", 2), ("fp32", 0)):
-            if path not in args.paths.split(","):
-                continue
-            C = torch.zeros(n, n, device="cuda")
-            sp = torch.cuda.current_stream().cuda_stream or None
-
-            def call():
-                gbblas.call("gbblas_sgemm", n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, 1, C.data_ptr(), n, 1,
-                            acc, sp)
-            for _ in range(args.warmup):
-                call()
-            torch.cuda.synchronize()
-            iters = args.gemm_iters
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with ClockSampler(0) as clk:
-                t0 = time.time()
-                e0.record()
-                for _ in range(iters):
-                    call()
-                e1.record()
-                torch.cuda.synchronize()
-                clk.mark(t0, time.time())
-            gbblas.call("gbblas_check_stream", sp)
-            ms = e0.elapsed_time(e1) / iters
-            # one clean product for the error check
-            C.zero_()
-            call()
-            got = C.cpu().numpy()[rows, cols].astype(np.float64)
-            rel = np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300)
-            normwise = np.abs(got - exact) / absx
-            diff = (C.double() - C64).abs_()
-            full = {"max_rel_err": float((diff / C64.abs().clamp_min(1e-300)).max()),
-                    "mean_rel_err": float((diff / C64.abs().clamp_min(1e-300)).mean()),
-                    "max_normwise_err": float((diff / absAB.double().clamp_min(1e-300)).max()),
-                    "reference": "the full M x N product on the FP64 pipes (GPU)"}
-            del diff
-            tf = flops / (ms / 1e3) / 1e12
-            line = {"metric": "GEMM TFLOP/s (float32 operands)", "path": path, "input_set": set_name,
-                    "value": round(tf, 2), "unit": "TFLOP/s", "ms_per_gemm": round(ms, 3), "M": n, "N": n, "K": n,
-                    "flops": "2*M*N*K algorithmic", "max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()),
-                    "max_normwise_err": float(normwise.max()), "error_sample": f"{sample} entries vs long double",
-                    "full_matrix_fp64": full, "clocks": clk.summary()}
-            products = {"bf16x3": 3, "bf16x6": 6, "fp16x3": 3}.get(path)
-            if products and peaks.get("bf16_tflops"):
-                line["tensor_frac"] = round(products * tf / peaks["bf16_tflops"], 4)
-                line["tensor_peak"] = (f"{products} BF16 products per algorithmic flop vs bf16_tflops "
-                                       f"{peaks['bf16_tflops']} (measured, burst)")
-            if path == "fp32":
-                fma_peak = fma_peak_tflops(line["clocks"])
-                line["fma_frac"] = round(tf / fma_peak, 4)
-                line["fma_peak"] = (f"{fma_peak:.1f} TFLOP/s: SMs x 128 FP32 FMA lanes x 2 flop x max SM clock "
-                                    "(nominal; no FMA peak is measured)")
-            if path == "fp8" and peaks.get("bf16_tflops"):
-                line["tensor_frac"] = round(tf / (2 * peaks["bf16_tflops"]), 4)
-                line["tensor_peak"] = (f"2 x bf16_tflops {peaks['bf16_tflops']} (measured BF16 burst times the "
-                                       "nominal FP8/BF16 ratio; no FP8 peak is measured)")
+    rep = precision_report(n, sets=args.sets.split(","), paths=args.paths.split(","), warmup=args.warmup,
+                           iters=args.gemm_iters, sample=4096)
+    for set_name, paths in rep.items():
+        for path, rec in paths.items():
+            line = {"metric": "GEMM TFLOP/s (float32 operands)", "path": path, "input_set": set_name, "M": n,
+                    "N": n, "K": n, "flops": "2*M*N*K algorithmic", "error_sample": "4096 entries vs long double"}
+            line.update(rec)
             print(json.dumps(line), flush=True)
-        del A, B, C64, absAB
 
 
 def run_f64(args):
@@ -801,6 +920,10 @@ def batching_shapes(seed=3):
 
 
 def run_batching(args):
+    print(json.dumps(batching_report(args)), flush=True)
+
+
+def batching_report(args):
     """The batching configuration: one graph-captured batch of 512 GEMMs
     (float32 in, split-BF16 on the tensor cores) and 4096 row-major GEMVs,
     U[-1,1) from seed 3.  The GEMV matrices (243.5 GB in total) are windows
@@ -936,12 +1059,18 @@ def run_batching(args):
             "gpu_launches_incl_graphs": int(launches), "clocks": clk.summary(),
             "config": {"workload": "512 GEMM log-uniform [32,2048] + 4096 GEMV log-uniform [256,16384], seed 3",
                        "gemv_pool_GiB": args.pool_gb}}
-    print(json.dumps(line), flush=True)
     for b in (b_all, b_gemm, b_gemv):
         b.close()
+    del gemm_t, gemv_t, pool
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_serving(args):
+    print(json.dumps(serving_report(args)), flush=True)
+
+
+def serving_report(args):
     """The serving configuration: Poisson arrivals at each rate of --rates of
     60 % mtm, 30 % mtv, 10 % dot; GEMM and GEMV dims log-uniform in
     [64, 4096], dot lengths log-uniform in [1k, 64M]; 80 % float32 at FP32
@@ -1049,10 +1178,12 @@ def run_serving(args):
                        "budget_GiB": 64, "streams": args.streams or 16, "max_group": args.max_group or 256,
                        "heavy_streams": args.heavy_streams or 2, "heavy_sm_percent": args.heavy_sm_percent or 75,
                        "heavy_us": args.heavy_us or 300}}
-    print(json.dumps(line), flush=True)
     for p in outs:
         srv.free(p)
     srv.close()
+    del pool32, pool64
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_stream_ops(args):
@@ -1163,6 +1294,10 @@ def run_stream_ops(args):
 
 
 def run_mtm(args):
+    print(json.dumps(mtm_report(args)), flush=True)
+
+
+def mtm_report(args):
     """The plain single-precision mtm configuration: C = A*B, M = N = K = 1024,
     row-major float32, A then B U[-1,1) from seed 0, C zeroed; FP32 on the FMA
     pipes (the default accuracy).  TFLOP/s with 2*M*N*K flops (and the
@@ -1179,9 +1314,8 @@ def run_mtm(args):
     from oracle import oracle as O
     torch.cuda.set_device(0)
     n = 1024
-    rng = np.random.default_rng(0)
-    A = rng.uniform(-1, 1, (n, n)).astype(np.float32)
-    B = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    A, B = np.empty((n, n), np.float32), np.empty((n, n), np.float32)
+    gbblas.seeded_fill(0, [A.reshape(-1), B.reshape(-1)], None)
     tA, tB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
     tC = torch.zeros(n, n, device="cuda")
     sp = torch.cuda.current_stream().cuda_stream or None
@@ -1227,7 +1361,8 @@ def run_mtm(args):
     line = {"metric": "plain mtm TFLOP/s (float32, FMA pipes)", "value": round(tf, 3), "unit": "TFLOP/s",
             "n_gpus": 1, "steps": iters, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "mtm C = A*B, M = N = K = 1024, row-major float32, U[-1,1) seed 0 (A then B)",
+            "config": {"workload": "mtm C = A*B, M = N = K = 1024, row-major float32, U[-1,1) from "
+                                   "std::mt19937_64(0), A then B",
                        "flops": "2*M*N*K", "l2": "operands fit in L2 (12 MB); repeated calls"},
             "reference_gflops_count": round(n * n * (2 * n - 1) / (ms / 1e3) / 1e9, 1),
             "roofline": {"bound": "fma", "achieved": round(tf, 3), "peak": round(peak, 1), "unit": "TFLOP/s",
@@ -1254,7 +1389,7 @@ def run_mtm(args):
         line["cpu_baseline"] = {"value": round(2.0 * n ** 3 / cpu_s / 1e12, 4), "unit": "TFLOP/s",
                                 "cores": os.cpu_count(), "kind": ref_kind,
                                 "sample": f"the full 1024^3 mtm, mean of 10 after 2 warm-ups ({cpu_s * 1e3:.1f} ms)"}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_sweep(args):
@@ -1407,7 +1542,8 @@ def main():
     ap.add_argument("--impl", default="gbblas", choices=["gbblas", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-gemm", action="store_true",
-                    help="default workload: skip the FP32-accurate GEMM figures added beside the line")
+                    help="default workload: skip the measurements added beside the bandwidth line "
+                         "(precision, FP8, double GEMM, 1024^3 mtm, batching, serving)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--small", action="store_true",
                     help="profiling case: mtv 8192^2 and dot 2^26 (still larger than L2), "

@@ -127,6 +127,30 @@ gbblas_status gbblas_selftest_bounded_wait(int64_t limit_us, void* stream);
  * current device.  Safe to call at any time no call is in flight. */
 gbblas_status gbblas_release_cache(void);
 
+/* --------------------------------------------------------- seeded inputs
+ * No counterpart in the reference (its drivers fill operands with ones,
+ * src/mtm.cpp:204-205, and its tests with rand() % 100, test/test_utils.hpp:4-8).
+ * This is the input recipe of this library's benchmark configurations and
+ * parity tests, exported so that any caller can regenerate exactly the
+ * operands a published figure was measured on.  Host code only: it needs no
+ * GPU and touches no device memory. */
+
+typedef enum gbblas_fill_kind {
+  GBBLAS_FILL_UNIFORM = 0, /* U[-1,1): one draw x per value; double (x >> 11) * 2^-52 - 1,
+                              float (x >> 40) * 2^-23 - 1 (both exact) */
+  GBBLAS_FILL_WIDE = 1     /* s * m * 2^e from two draws d1, d2 per value: s = -1 if bit 63
+                              of d1 is set, m = 1 + (d1 bits 11..62) * 2^-52 (double) or
+                              1 + (d1 bits 40..62) * 2^-23 (float), e = ((d2 >> 32) mod 21) - 10 */
+} gbblas_fill_kind;
+
+/* One std::mt19937_64 seeded with `seed` draws nseg segments one after the
+ * other, counts[s] values each; value i of segment s goes to out_f32[s][i]
+ * and/or out_f64[s][i] (either array, or any entry of it, may be NULL: the
+ * values are drawn and skipped).  The float and the double of one value
+ * come from the same draws.  HOST pointers. */
+gbblas_status gbblas_seeded_fill(uint64_t seed, int32_t kind, int64_t nseg, const int64_t* counts,
+                                 float* const* out_f32, double* const* out_f64);
+
 /* ------------------------------------------------------------------ mtm */
 
 /* C += A * B (single precision).                      replaces amt::mtm,
@@ -211,6 +235,13 @@ gbblas_status gbblas_ddot(int64_t n, const double* a, const double* b, double* r
  * pointer are the caller's, as for gbblas_sdot.
  *   - The first call on each device looks up that array's device address
  *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     Under CUDA's default lazy module loading, that first call may also be
+ *     what loads the library's device code onto the device, and the CUDA
+ *     driver allocates the array then.  So the promise "allocates nothing"
+ *     holds from the second call on each device: make the first one during
+ *     set-up, where allocation is still allowed.
+ *   - The address is cached per device for the life of the process; after a
+ *     cudaDeviceReset on a device this library must not be used on it again.
  *   - All calls share the one array and it keeps the last call's contents;
  *     the call clears the part that must start at zero.  Calls whose work
  *     overlaps on the GPU (different streams, or different host threads

@@ -33,7 +33,10 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // ----------------------------------------------------------------- context
 namespace {
 std::mutex g_ctx_mu;
-DeviceCtx* g_ctx[64] = {nullptr};
+// Published once per device with a release store after construction; the
+// fast path reads it with an acquire load, so two host threads making their
+// first call at the same time never see a half-built context.
+std::atomic<DeviceCtx*> g_ctx[64] = {};
 }  // namespace
 
 gbblas_status get_ctx(DeviceCtx** out) {
@@ -43,13 +46,13 @@ gbblas_status get_ctx(DeviceCtx** out) {
     set_error("no CUDA device: %s", cudaGetErrorString(e));
     return GBBLAS_STATUS_NO_DEVICE;
   }
-  DeviceCtx* c = g_ctx[dev];
+  DeviceCtx* c = g_ctx[dev].load(std::memory_order_acquire);
   if (c) {
     *out = c;
     return GBBLAS_STATUS_SUCCESS;
   }
   std::lock_guard<std::mutex> lk(g_ctx_mu);
-  if (!g_ctx[dev]) {
+  if (!g_ctx[dev].load(std::memory_order_relaxed)) {
     cudaDeviceProp p;
     GB_CUDA_TRY(cudaGetDeviceProperties(&p, dev));
     if (!(p.major == 10 && p.minor == 3)) {
@@ -62,9 +65,9 @@ gbblas_status get_ctx(DeviceCtx** out) {
     n->cc_major = p.major;
     n->cc_minor = p.minor;
     n->smem_optin = p.sharedMemPerBlockOptin;
-    g_ctx[dev] = n;
+    g_ctx[dev].store(n, std::memory_order_release);
   }
-  *out = g_ctx[dev];
+  *out = g_ctx[dev].load(std::memory_order_relaxed);
   return GBBLAS_STATUS_SUCCESS;
 }
 
@@ -80,7 +83,13 @@ gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void*
       return GBBLAS_STATUS_ALLOC_FAILED;
     }
     GB_CUDA_TRY(cudaMemsetAsync(p, 0, kScratchZeroBytes, stream));
-    if (s.ptr) GB_CUDA_TRY(cudaFreeAsync(s.ptr, stream));
+    if (s.ptr) {
+      // carry a device error status still unread in the old buffer over to
+      // the new one, so gbblas_check_stream reports it after the growth
+      GB_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(p) + kErrWordOffset, static_cast<char*>(s.ptr) + kErrWordOffset,
+                                  sizeof(int), cudaMemcpyDeviceToDevice, stream));
+      GB_CUDA_TRY(cudaFreeAsync(s.ptr, stream));
+    }
     s.ptr = p;
     s.bytes = want;
   }

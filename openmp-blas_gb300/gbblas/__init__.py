@@ -101,7 +101,11 @@ SIGNATURES = {
     "gbblas_dtranspose_inplace_host": (_int, [_i64, _vp]),
     "gbblas_sew_host": (_int, [_int, _i64, _vp, _vp, _vp]),
     "gbblas_dew_host": (_int, [_int, _i64, _vp, _vp, _vp]),
+    "gbblas_seeded_fill": (_int, [ctypes.c_uint64, ctypes.c_int32, _i64, _vp, _vp, _vp]),
 }
+
+FILL_UNIFORM = 0  # U[-1, 1)
+FILL_WIDE = 1     # s * m * 2^e, m in [1, 2), e in [-10, 10]
 
 EW_ADD, EW_SUB, EW_MUL, EW_DIV = 0, 1, 2, 3
 
@@ -397,3 +401,50 @@ def dot_host(a, b):
     out = np.zeros(1, a.dtype)
     call(f"gbblas_{_npfx(a)}dot_host", a.size, a.ctypes.data, b.ctypes.data, out.ctypes.data)
     return out[0]
+
+
+# ---------------------------------------------------------------- seeded inputs
+
+def _host_ptr(buf) -> int:
+    """Address of a host buffer: a numpy array or a (pinned) CPU torch tensor."""
+    if hasattr(buf, "ctypes"):
+        return buf.ctypes.data
+    if getattr(buf, "is_cuda", False):
+        raise ValueError("seeded_fill writes host memory; got a CUDA tensor")
+    return buf.data_ptr()
+
+
+def _numel(buf) -> int:
+    return int(buf.size if hasattr(buf, "ctypes") else buf.numel())
+
+
+def seeded_fill(seed: int, f32=None, f64=None, kind: int = FILL_UNIFORM) -> None:
+    """Fill host buffers with the benchmark configurations' seeded inputs
+    (gbblas_seeded_fill): one std::mt19937_64(seed) draws the segments in
+    order.  `f32` / `f64` are equally long lists of host buffers (numpy arrays
+    or CPU torch tensors, contiguous) or None; entry i of either list may be
+    None, and segment i's length comes from whichever buffer is given.  An
+    int in place of a buffer is a segment of that many values drawn and
+    skipped."""
+    f32 = list(f32) if f32 is not None else None
+    f64 = list(f64) if f64 is not None else None
+    nseg = len(f32 if f32 is not None else (f64 or []))
+    counts = (ctypes.c_int64 * max(nseg, 1))()
+    p32 = (ctypes.c_void_p * max(nseg, 1))()
+    p64 = (ctypes.c_void_p * max(nseg, 1))()
+    for i in range(nseg):
+        a = f32[i] if f32 is not None else None
+        b = f64[i] if f64 is not None else None
+        if isinstance(a, int) or isinstance(b, int):
+            counts[i] = int(a if isinstance(a, int) else b)
+            p32[i] = p64[i] = None
+            continue
+        if a is None and b is None:
+            raise ValueError(f"segment {i} has no buffer")
+        n = _numel(a) if a is not None else _numel(b)
+        if a is not None and b is not None and _numel(b) != n:
+            raise ValueError(f"segment {i}: float and double buffers differ in length")
+        counts[i] = n
+        p32[i] = _host_ptr(a) if a is not None else None
+        p64[i] = _host_ptr(b) if b is not None else None
+    call("gbblas_seeded_fill", seed, kind, nseg, counts, p32, p64)

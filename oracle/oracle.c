@@ -341,3 +341,90 @@ void orc_sgemm_sample_exact(size_t K, const float* A, ptrdiff_t rsa, ptrdiff_t c
     absout[s] = (double)aacc;
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Seeded inputs: MT19937-64 (Matsumoto & Nishimura, "Tables of 64-bit      */
+/* Mersenne Twisters", 2000; the engine std::mt19937_64 names) and the      */
+/* value mappings of the benchmark configurations.  The GPU library draws   */
+/* the same values through the C++ standard library's engine; this is an    */
+/* independent restatement from the published algorithm, so the two        */
+/* checking each other pins both.                                           */
+/* ------------------------------------------------------------------------ */
+
+#define MT64_N 312
+#define MT64_M 156
+
+typedef struct {
+  uint64_t mt[MT64_N];
+  int i;
+} orc_mt64_t;
+
+static void mt64_seed(orc_mt64_t* g, uint64_t seed) {
+  g->mt[0] = seed;
+  for (int i = 1; i < MT64_N; ++i)
+    g->mt[i] = 6364136223846793005ULL * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + (uint64_t)i;
+  g->i = MT64_N;
+}
+
+static inline uint64_t mt64_twist(uint64_t upper_from, uint64_t lower_from, uint64_t far) {
+  const uint64_t x = (upper_from & 0xFFFFFFFF80000000ULL) | (lower_from & 0x7FFFFFFFULL);
+  return far ^ (x >> 1) ^ ((x & 1ULL) ? 0xB5026F5AA96619E9ULL : 0ULL);
+}
+
+static uint64_t mt64_next(orc_mt64_t* g) {
+  if (g->i >= MT64_N) {
+    int k = 0;
+    for (; k < MT64_N - MT64_M; ++k) g->mt[k] = mt64_twist(g->mt[k], g->mt[k + 1], g->mt[k + MT64_M]);
+    for (; k < MT64_N - 1; ++k) g->mt[k] = mt64_twist(g->mt[k], g->mt[k + 1], g->mt[k + MT64_M - MT64_N]);
+    g->mt[MT64_N - 1] = mt64_twist(g->mt[MT64_N - 1], g->mt[0], g->mt[MT64_M - 1]);
+    g->i = 0;
+  }
+  uint64_t x = g->mt[g->i++];
+  x ^= (x >> 29) & 0x5555555555555555ULL;
+  x ^= (x << 17) & 0x71D67FFFEDA60000ULL;
+  x ^= (x << 37) & 0xFFF7EEE000000000ULL;
+  x ^= x >> 43;
+  return x;
+}
+
+/* The first n raw 64-bit outputs of the engine seeded with `seed`. */
+void orc_mt64_raw(uint64_t seed, int64_t n, uint64_t* out) {
+  orc_mt64_t g;
+  mt64_seed(&g, seed);
+  for (int64_t i = 0; i < n; ++i) out[i] = mt64_next(&g);
+}
+
+/* kind 0: U[-1,1) - double (x >> 11) 2^-52 - 1, float (x >> 40) 2^-23 - 1.
+ * kind 1: wide range s m 2^e from two draws d1, d2 - s from bit 63 of d1,
+ * m = 1 + (d1 bits 11..62) 2^-52 (double) or 1 + (d1 bits 40..62) 2^-23
+ * (float), e = ((d2 >> 32) mod 21) - 10.  Segments are drawn one after the
+ * other from one engine; NULL outputs are drawn and skipped. */
+int orc_seeded_fill(uint64_t seed, int kind, int64_t nseg, const int64_t* counts, float* const* f32,
+                    double* const* f64) {
+  if (kind != 0 && kind != 1) return 1;
+  orc_mt64_t g;
+  mt64_seed(&g, seed);
+  for (int64_t s = 0; s < nseg; ++s) {
+    float* f = f32 ? f32[s] : NULL;
+    double* d = f64 ? f64[s] : NULL;
+    for (int64_t i = 0; i < counts[s]; ++i) {
+      const uint64_t x = mt64_next(&g);
+      if (kind == 0) {
+        if (f) f[i] = (float)(x >> 40) * 0x1.0p-23f - 1.0f;
+        if (d) d[i] = (double)(x >> 11) * 0x1.0p-52 - 1.0;
+      } else {
+        const uint64_t x2 = mt64_next(&g);
+        const int e = (int)((x2 >> 32) % 21u) - 10;
+        if (f) {
+          const float v = ldexpf(1.0f + (float)((x >> 40) & ((1u << 23) - 1)) * 0x1.0p-23f, e);
+          f[i] = (x >> 63) ? -v : v;
+        }
+        if (d) {
+          const double v = ldexp(1.0 + (double)((x >> 11) & ((1ULL << 52) - 1)) * 0x1.0p-52, e);
+          d[i] = (x >> 63) ? -v : v;
+        }
+      }
+    }
+  }
+  return 0;
+}

@@ -6,7 +6,7 @@ Two libraries are wrapped:
   (oracle/oracle.c, which cites the reference file:line it follows).  It is
   built on every machine (``make -C oracle``).
 * ``oracle/_ref/libamt_ref.so`` - the reference's own headers compiled
-  unmodified (``make -C oracle ref``), present only where the reference
+  unmodified (``make -C oracle ref REF_ROOT=<checkout>``), present only where the reference
   sources are.  ``ref_available()`` says whether it loaded.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg and
@@ -43,8 +43,9 @@ _ref_tried = False
 def build(with_ref: bool = False) -> None:
     """Compile liboracle.so (and, if asked and possible, the reference lib)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=False)
+    root = os.environ.get("AMT_REFERENCE_ROOT", "")
+    if with_ref and root:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={root}"], check=False)
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -98,6 +99,10 @@ def lib():
         L.orc_partition.argtypes = [_c_size, ctypes.c_int, _vp]
         L.orc_max_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_mt64_raw.argtypes = [ctypes.c_uint64, ctypes.c_int64, _vp]
+        L.orc_mt64_raw.restype = None
+        L.orc_seeded_fill.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int64, _vp, _vp, _vp]
+        L.orc_seeded_fill.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -432,3 +437,29 @@ def ref_ew(op, a, b):
     if getattr(ref(), f"ref_{_sfx(aa.dtype)}ew")(op, aa.size, _ptr(aa), _ptr(bb), _ptr(c)) != 0:
         raise RuntimeError("reference element-wise op threw")
     return c
+
+
+# ---------------------------------------------------------------- seeded inputs
+
+def mt64_raw(seed: int, n: int) -> np.ndarray:
+    """The first n outputs of MT19937-64 seeded with `seed` (the oracle's own
+    restatement of the engine)."""
+    out = np.empty(n, np.uint64)
+    lib().orc_mt64_raw(ctypes.c_uint64(seed), n, _ptr(out))
+    return out
+
+
+def seeded_fill(seed: int, counts, f32: bool = True, f64: bool = True, kind: int = 0):
+    """Segments of the seeded inputs drawn in order from one MT19937-64(seed):
+    returns (list of float32 arrays or None, list of float64 arrays or None)."""
+    counts = [int(c) for c in counts]
+    n = len(counts)
+    a32 = [np.empty(c, np.float32) for c in counts] if f32 else None
+    a64 = [np.empty(c, np.float64) for c in counts] if f64 else None
+    cc = (ctypes.c_int64 * max(n, 1))(*counts)
+    p32 = (ctypes.c_void_p * max(n, 1))(*([a.ctypes.data for a in a32] if f32 else []))
+    p64 = (ctypes.c_void_p * max(n, 1))(*([a.ctypes.data for a in a64] if f64 else []))
+    rc = lib().orc_seeded_fill(ctypes.c_uint64(seed), kind, n, cc, p32 if f32 else None, p64 if f64 else None)
+    if rc != 0:
+        raise ValueError(f"orc_seeded_fill: bad kind {kind}")
+    return a32, a64

@@ -2,7 +2,7 @@
 
 Run here, where the reference sources exist:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref REF_ROOT=<reference checkout> && python tests/golden/make_golden.py
 
 The outputs come from oracle/_ref/libamt_ref.so, i.e. the reference's
 include/{mtm,mtv,dot,outer,trans,el_wise_op}.hpp compiled unmodified.  The inputs follow the
@@ -50,7 +50,7 @@ OUT = os.path.join(HERE, "golden.npz")
 
 def main() -> None:
     if not O.ref_available():
-        raise SystemExit("oracle/_ref/libamt_ref.so missing: run `make -C oracle ref` where the reference is")
+        raise SystemExit("oracle/_ref/libamt_ref.so missing: run `make -C oracle ref REF_ROOT=<reference checkout>` where the reference is")
     rng = np.random.default_rng(20240601)
     g: dict[str, np.ndarray] = {}
     names = []

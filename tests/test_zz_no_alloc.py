@@ -29,11 +29,37 @@ def test_sdot_noalloc_matches_sdot_twice(cuda, n):
     _sdot(gbblas, "gbblas_sdot", a, b, ref)
     eps = float(np.finfo(np.float32).eps)
     tol = 4 * eps * float((a.double() * b.double()).abs().sum()) + eps * abs(ref.item())
+    # the exact sum (long double) from the CPU oracle, with the Kahan dot's bound
+    from oracle import oracle as O
+    exact, absdot = O.dot_exact(a.cpu().numpy(), b.cpu().numpy())
+    tol_exact = 4 * eps * absdot + 0.5 * eps * abs(exact)
     for _ in range(2):
         out = torch.full((1,), float("nan"), device="cuda")
         _sdot(gbblas, "gbblas_sdot_noalloc", a, b, out)
         torch.cuda.synchronize()
         assert abs(out.item() - ref.item()) <= tol, (n, out.item(), ref.item())
+        assert abs(out.item() - exact) <= tol_exact, (n, out.item(), exact)
+
+
+def test_sdot_noalloc_device_memory_unchanged(cuda):
+    """After the first call on the device (set-up), further calls take no
+    device memory: the free device memory the driver reports does not move
+    over many calls of several sizes."""
+    torch = cuda
+    import gbblas
+    g = torch.Generator(device="cuda").manual_seed(11)
+    a = torch.rand(1 << 23, device="cuda", generator=g) - 0.5
+    b = torch.rand(1 << 23, device="cuda", generator=g) - 0.5
+    out = torch.zeros(1, device="cuda")
+    _sdot(gbblas, "gbblas_sdot_noalloc", a, b, out)  # set-up call
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for k in range(60):
+        n = [7, 4099, 1 << 20, 1 << 23][k % 4]
+        gbblas.call("gbblas_sdot_noalloc", n, a.data_ptr(), b.data_ptr(), out.data_ptr(), None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_sdot_noalloc_alternating_sizes(cuda):
