@@ -65,6 +65,9 @@ gbblas_status get_ctx(DeviceCtx** out) {
     n->cc_major = p.major;
     n->cc_minor = p.minor;
     n->smem_optin = p.sharedMemPerBlockOptin;
+    int pma = 0;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pma = 0;
+    n->pageable_access = pma;
     g_ctx[dev].store(n, std::memory_order_release);
   }
   *out = g_ctx[dev].load(std::memory_order_relaxed);
@@ -145,6 +148,25 @@ gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out) {
   }
   *out = c->stage;
   return GBBLAS_STATUS_SUCCESS;
+}
+
+const void* host_read_view(DeviceCtx* c, const void* p) {
+  const char* e = std::getenv("GBBLAS_HOST_DIRECT");
+  if (!p || (e && e[0] == '0')) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // not a pointer the runtime knows: stage it
+    return nullptr;
+  }
+  switch (at.type) {
+    case cudaMemoryTypeHost:
+      return at.devicePointer;  // page-locked: its mapped address (null if not mapped)
+    case cudaMemoryTypeDevice:
+    case cudaMemoryTypeManaged:
+      return at.device == c->device ? p : nullptr;
+    default:
+      return c->pageable_access ? p : nullptr;
+  }
 }
 
 namespace {
@@ -326,6 +348,13 @@ gbblas_status gemm_host(int64_t M, int64_t N, int64_t K, const T* A, int64_t rsa
   return GBBLAS_STATUS_SUCCESS;
 }
 
+// The streaming *_host calls read the large operand (the matrix of a GEMV,
+// both vectors of a dot) straight from host memory where the device can
+// (host_read_view): the kernel's own loads then move the bytes over the host
+// link while it computes, with no staging copy and no copy-then-compute
+// serialisation; the result is the same bits, since the kernel, grid and
+// reduction order are those of the device call.  Small operands (x, y, the
+// dot's result) are staged: the kernels read x many times over.
 template <typename T>
 gbblas_status gemv_host(gbblas_layout la, bool transpose, int64_t M, int64_t N, const T* A, const T* x,
                         bool accumulate, T* y) {
@@ -336,13 +365,16 @@ gbblas_status gemv_host(gbblas_layout la, bool transpose, int64_t M, int64_t N, 
   GB_TRY(get_ctx(&c));
   HostGuard g(c);
   const size_t na = (size_t)(M * N), nx = (size_t)in_len, ny = (size_t)out_len;
+  const T* vA = na ? static_cast<const T*>(host_read_view(c, A)) : nullptr;
+  if (vA && !aligned16(vA)) vA = nullptr;  // the staged copy keeps the kernel's 128-bit loads
+  const size_t stage_a = vA ? 0 : round256(na * sizeof(T));
   void* base;
-  GB_TRY(get_stage(c, round256(na * sizeof(T)) + round256(nx * sizeof(T)) + round256(ny * sizeof(T)), &base));
-  T* dA = static_cast<T*>(base);
-  T* dx = reinterpret_cast<T*>(static_cast<char*>(base) + round256(na * sizeof(T)));
+  GB_TRY(get_stage(c, stage_a + round256(nx * sizeof(T)) + round256(ny * sizeof(T)), &base));
+  T* dA = vA ? const_cast<T*>(vA) : static_cast<T*>(base);
+  T* dx = reinterpret_cast<T*>(static_cast<char*>(base) + stage_a);
   T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(dx) + round256(nx * sizeof(T)));
   cudaStream_t s = c->host_stream;
-  GB_TRY(h2d(dA, A, na * sizeof(T), s));
+  if (!vA) GB_TRY(h2d(dA, A, na * sizeof(T), s));
   GB_TRY(h2d(dx, x, nx * sizeof(T), s));
   if (accumulate) GB_TRY(h2d(dy, y, ny * sizeof(T), s));
   GB_TRY(gemv_any<T>(c, la, transpose, M, N, dA, dx, accumulate, dy, s));
@@ -359,14 +391,18 @@ gbblas_status dot_host(int64_t n, const T* a, const T* b, T* result) {
   GB_TRY(get_ctx(&c));
   HostGuard g(c);
   const size_t bytes = (size_t)n * sizeof(T);
+  const T* va = n ? static_cast<const T*>(host_read_view(c, a)) : nullptr;
+  const T* vb = n ? static_cast<const T*>(host_read_view(c, b)) : nullptr;
+  if (!va || !vb || !aligned16(va) || !aligned16(vb)) va = vb = nullptr;  // both direct, 128-bit loads, or neither
+  const size_t stage_a = va ? 0 : round256(bytes), stage_b = vb ? 0 : round256(bytes);
   void* base;
-  GB_TRY(get_stage(c, 2 * round256(bytes) + 256, &base));
-  T* da = static_cast<T*>(base);
-  T* db = reinterpret_cast<T*>(static_cast<char*>(base) + round256(bytes));
-  T* dr = reinterpret_cast<T*>(static_cast<char*>(base) + 2 * round256(bytes));
+  GB_TRY(get_stage(c, stage_a + stage_b + 256, &base));
+  T* da = va ? const_cast<T*>(va) : static_cast<T*>(base);
+  T* db = vb ? const_cast<T*>(vb) : reinterpret_cast<T*>(static_cast<char*>(base) + stage_a);
+  T* dr = reinterpret_cast<T*>(static_cast<char*>(base) + stage_a + stage_b);
   cudaStream_t s = c->host_stream;
-  GB_TRY(h2d(da, a, bytes, s));
-  GB_TRY(h2d(db, b, bytes, s));
+  if (!va) GB_TRY(h2d(da, a, bytes, s));
+  if (!vb) GB_TRY(h2d(db, b, bytes, s));
   GB_TRY(launch_dot<T>(c, n, da, db, dr, s));
   GB_TRY(d2h(result, dr, sizeof(T), s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));

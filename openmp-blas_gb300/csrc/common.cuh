@@ -63,6 +63,9 @@ struct DeviceCtx {
   int num_sms = 0;
   int cc_major = 0, cc_minor = 0;
   size_t smem_optin = 0;
+  // cudaDevAttrPageableMemoryAccess: the device reads pageable host memory
+  // coherently (through the host's page tables on a Grace-coupled GPU)
+  int pageable_access = 0;
   std::mutex mu;
   struct Scratch {
     void* ptr = nullptr;
@@ -96,6 +99,14 @@ void release_scratch(DeviceCtx* c, cudaStream_t stream);
 
 // Staging arena of at least `bytes` for the *_host paths (caller holds host_mu).
 gbblas_status get_stage(DeviceCtx* c, size_t bytes, void** out);
+
+// Address at which this library's kernels may read the host buffer `p`
+// directly (over the host link, no staging copy), or nullptr when it must be
+// staged: page-locked memory (cudaHostAlloc / cudaHostRegister) through its
+// mapped device address, device or managed memory as it is, pageable memory
+// only on a device that reads it coherently.  GBBLAS_HOST_DIRECT=0 turns
+// direct reads off (every host operand is then staged).
+const void* host_read_view(DeviceCtx* c, const void* p);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

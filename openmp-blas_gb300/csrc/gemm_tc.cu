@@ -250,6 +250,27 @@ struct PrepTile {
 // then atomicMax-ed into e (which starts filled with the byte 0x80: a row no
 // tile wrote, all zero or padding, reads as 0).
 constexpr int kF16ScaleTop = 15;
+
+// Edge / strided tiles of f16_scale_kernel: value i of a thread (element
+// tid + 256 i of the 64 x 64 tile) into the rows' maxima.  K contiguous: it
+// lies in row tid / 64 + 4 i and a warp's 32 lanes hold 32 K of that row (one
+// shared atomic per warp and row); otherwise all 16 lie in row tid % 64.
+__device__ __forceinline__ void f16_scale_tile_rows(const unsigned (&m)[16], int tid, bool k_contig,
+                                                    unsigned* rmax) {
+  if (k_contig) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const unsigned w = __reduce_max_sync(0xffffffffu, m[i]);
+      if ((tid & 31) == 0 && w) atomicMax(&rmax[tid / 64 + 4 * i], w);
+    }
+  } else {
+    unsigned w = 0u;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) w = max(w, m[i]);
+    if (w) atomicMax(&rmax[tid % 64], w);
+  }
+}
+
 __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                         int* __restrict__ e_out) {
   constexpr int TK = 64, TR = 64;
@@ -272,20 +293,57 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restri
   const SplitJob& j = jobs[sjob];
   const int local = t - j.tile_start;
   const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
-  unsigned int m[16];
+  const bool full = r0 + TR <= j.rows && k0 + TK <= j.K;
+  const bool al16 = (reinterpret_cast<uintptr_t>(j.src) & 15) == 0;
+  auto mag4 = [](float4 v) {
+    return max(max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu),
+               max(__float_as_uint(v.z) & 0x7FFFFFFFu, __float_as_uint(v.w) & 0x7FFFFFFFu));
+  };
+  if (full && al16 && j.cs == 1 && (j.rs & 3) == 0) {
+    // interior tile, K contiguous: 128-bit loads, float4 i of a thread in row
+    // tid / 16 + 16 i; the 16 lanes of a half-warp share that row
+    unsigned w[4];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int idx = tid + 256 * i;
-    const int r = j.cs == 1 ? idx / TK : idx % TR, k = j.cs == 1 ? idx % TK : idx / TR;
-    m[i] = (r0 + r < j.rows && k0 + k < j.K)
-               ? (__float_as_uint(__ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs)) & 0x7FFFFFFFu)
-               : 0u;
-  }
+    for (int i = 0; i < 4; ++i) {
+      const int idx = tid + 256 * i;
+      w[i] = mag4(dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + idx / 16) * j.rs + k0 + 4 * (idx % 16))));
+    }
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const int idx = tid + 256 * i;
-    const int r = j.cs == 1 ? idx / TK : idx % TR;
-    if (m[i]) atomicMax(&rmax[r], m[i]);
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) w[i] = max(w[i], __shfl_xor_sync(0xffffffffu, w[i], o));
+      if ((tid & 15) == 0 && w[i]) atomicMax(&rmax[tid / 16 + 16 * i], w[i]);
+    }
+  } else if (full && al16 && j.rs == 1 && (j.cs & 3) == 0) {
+    // interior tile, rows contiguous: 128-bit loads of rows 4 (tid % 16) .. + 3,
+    // the same four rows for all of a thread's loads; lanes l and l ^ 16 too
+    unsigned w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = tid + 256 * i;
+      const float4 v =
+          dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + idx / 16) * j.cs + r0 + 4 * (idx % 16)));
+      w[0] = max(w[0], __float_as_uint(v.x) & 0x7FFFFFFFu);
+      w[1] = max(w[1], __float_as_uint(v.y) & 0x7FFFFFFFu);
+      w[2] = max(w[2], __float_as_uint(v.z) & 0x7FFFFFFFu);
+      w[3] = max(w[3], __float_as_uint(v.w) & 0x7FFFFFFFu);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      w[q] = max(w[q], __shfl_xor_sync(0xffffffffu, w[q], 16));
+      if ((tid & 31) < 16 && w[q]) atomicMax(&rmax[4 * (tid % 16) + q], w[q]);
+    }
+  } else {
+    unsigned int m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int idx = tid + 256 * i;
+      const int r = j.cs == 1 ? idx / TK : idx % TR, k = j.cs == 1 ? idx % TK : idx / TR;
+      m[i] = (r0 + r < j.rows && k0 + k < j.K)
+                 ? (__float_as_uint(__ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs)) & 0x7FFFFFFFu)
+                 : 0u;
+    }
+    f16_scale_tile_rows(m, tid, j.cs == 1, rmax);
   }
   __syncthreads();
   if (tid < TR && r0 + tid < j.rows && rmax[tid] != 0u) {
@@ -293,6 +351,13 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restri
     (void)frexpf(__uint_as_float(rmax[tid] >= 0x7F800000u ? 0x7F7FFFFFu : rmax[tid]), &e);  // Inf / NaN: the top exponent
     atomicMax(e_out + j.dst_row + r0 + tid, e);
   }
+}
+
+// x * 2^n, correctly rounded (what ldexpf gives), by one multiply with a
+// normal power of two where n allows it (the common case: one integer add,
+// a shift and a multiply) and ldexpf otherwise.
+__device__ __forceinline__ float scale_pow2(float x, int n) {
+  return (n >= -126 && n <= 127) ? x * __int_as_float((n + 127) << 23) : ldexpf(x, n);
 }
 
 __device__ __forceinline__ int f16_row_exp(const int* e, int64_t row) {
@@ -399,7 +464,7 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
       const int64_t arow = j.dst_row + r0 + r;
       const int sh = kF16ScaleTop - f16_row_exp(erow, arow);
       float4 v = *reinterpret_cast<const float4*>(&tile[r * LD + kk]);
-      v = make_float4(ldexpf(v.x, sh), ldexpf(v.y, sh), ldexpf(v.z, sh), ldexpf(v.w, sh));
+      v = make_float4(scale_pow2(v.x, sh), scale_pow2(v.y, sh), scale_pow2(v.z, sh), scale_pow2(v.w, sh));
       const int64_t base = arow * pitch + k0 + kk;
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
@@ -833,20 +898,35 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         }
         tc_fence_after();
         const uint32_t tb = trow + (uint32_t)b * MT::kBufCols;
+        // the fold: FP8 has one accumulator per buffer, the splits two (main,
+        // corrections), added with packed round-to-nearest FP32 adds
+        if constexpr (MT::fp8) {
 #pragma unroll
-        for (int c0 = 0; c0 < kCols; c0 += 16) {
-          float v0[16];
-          tmem_ld16(tb + c0, v0);
-          if constexpr (MT::fp8) {
+          for (int c0 = 0; c0 < kCols; c0 += 16) {
+            float v0[16];
+            tmem_ld16(tb + c0, v0);
             tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[c0 + j] += v0[j];
-          } else {
-            float v1[16];
+            for (int j = 0; j < 16; j += 2) {
+              const float2 r = __fadd2_rn(make_float2(acc[c0 + j], acc[c0 + j + 1]), make_float2(v0[j], v0[j + 1]));
+              acc[c0 + j] = r.x;
+              acc[c0 + j + 1] = r.y;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int c0 = 0; c0 < kCols; c0 += 16) {
+            float v0[16], v1[16];
+            tmem_ld16(tb + c0, v0);
             tmem_ld16(tb + kBN + c0, v1);
             tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[c0 + j] += v0[j] + v1[j];
+            for (int j = 0; j < 16; j += 2) {
+              const float2 r = __fadd2_rn(make_float2(v0[j], v0[j + 1]), make_float2(v1[j], v1[j + 1]));
+              const float2 q = __fadd2_rn(make_float2(acc[c0 + j], acc[c0 + j + 1]), r);
+              acc[c0 + j] = q.x;
+              acc[c0 + j + 1] = q.y;
+            }
           }
         }
         tc_fence_before();
@@ -867,7 +947,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         const int* eb = reinterpret_cast<const int*>(sb);
         const int ei = f16_row_exp(ea, (int64_t)pr.a_row + m0 + q * 32 + lane) - 2 * kF16ScaleTop;
 #pragma unroll
-        for (int c = 0; c < kCols; ++c) acc[c] = ldexpf(acc[c], ei + f16_row_exp(eb, (int64_t)pr.b_row + n0 + col0 + c));
+        for (int c = 0; c < kCols; ++c)
+          acc[c] = scale_pow2(acc[c], ei + f16_row_exp(eb, (int64_t)pr.b_row + n0 + col0 + c));
       }
       if constexpr (MT::fp8) {
         if (pr.c_tma) {
