@@ -131,7 +131,7 @@ gbblas_status launch_dot(DeviceCtx* c, int64_t n, const T* a, const T* b, T* res
 
 // max_ctas > 0 caps the grid (the kernel loops over tiles), leaving SMs to
 // other streams.
-// tile (FP32 only): 3 = TMA-fed with split-K where the tiles leave SMs idle,
+// tile (FP32 only): 3 = TMA-fed, stream-K (K blocks shared out equally among the SMs),
 // 2 = TMA-fed 128 x 128 kernel (gemm_fma_tma.cu; where
 // sgemm_tma_eligible), 1 = 128 x 128 CTA tiles, 0 = 64 x 64, -1 = by the
 // tile count (TMA-fed for a row-major B once the 128 x 128 tiles fill the
@@ -147,12 +147,13 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
 bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa, const float* B,
                         int64_t rsb, int64_t csb);
 void sgemm_tma_prepare(DeviceCtx* c);  // kernel attributes, before any stream capture
-// parts > 1: split-K into that many K ranges (sgemm_tma_split_parts gives
-// the count that fills one wave of SMs, 1 when none does).
+// streamk != 0: the tiles' K blocks shared out equally among the CTAs
+// (stream-K; sgemm_tma_streamk_useful says where whole tiles fill the SMs
+// badly enough for it to be worth trying).
 gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                                int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
-                               int64_t csc, cudaStream_t stream, int max_ctas = 0, int parts = 1);
-int sgemm_tma_split_parts(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
+                               int64_t csc, cudaStream_t stream, int max_ctas = 0, int streamk = 0);
+bool sgemm_tma_streamk_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 
 // C += A*B on the tcgen05 tensor cores (gemm_tc.cu).  mode = tc_mode(acc):
 // 2 / 3 = FP32 operands split into that many BF16 pieces, 8 = FP8-E4M3 with

@@ -23,12 +23,16 @@
 //
 // Persistent: grid = min(tiles, SMs or the caller's cap), tiles in grouped
 // raster order (8 tile rows per band) for L2 reuse; the ring carries over
-// from tile to tile.  Split-K (parts > 1, for shapes whose tiles leave SMs
-// idle): each unit = (tile, K part) stores its K range's sum into that
-// part's partial (no other unit writes those elements), then the partials
-// are added into C in part order - within the same bound, not the same bits
-// as the unsplit kernels.  Roofline: the FMA pipes,
-// 2*M*N*K flops.
+// from tile to tile.  Stream-K (for shapes whose tiles fill the SMs badly,
+// e.g. 64 tiles of a 1024^3 product on 152 SMs): the tiles' K blocks, laid
+// end to end, are cut into one equal range per CTA, so every SM does the
+// same number of FMAs.  A CTA whose range covers a whole tile adds it into C
+// as above; a range that covers part of a tile ("segment") stores its sum
+// into the segment's slot, and the tile's last segment to finish (an atomic
+// count per tile) adds the slots in K order and then that sum into C - a
+// fixed order for a given grid, so the bits repeat run to run, within the
+// same bound as the unsplit kernels but not their bits.  No second kernel
+// and no waiting on other CTAs.  Roofline: the FMA pipes, 2*M*N*K flops.
 #include <cuda.h>
 
 #include <mutex>
@@ -53,7 +57,7 @@ constexpr int kThreads = 32 * (kComputeWarps + 1);
 constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + 256 /*barriers*/;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 static_assert(kSmem <= 232448, "exceeds 227 KB of shared memory");
-static_assert((2 * kStages) * 8 + 4 <= 256, "barrier area too small");
+static_assert((2 * kStages + 2) * 8 + 4 <= 256, "barrier area too small");
 
 // The 8 values (one per owned row or column i) of 4 consecutive k (kq*4..+3)
 // from a tile: v[i][kk].
@@ -111,13 +115,16 @@ template <bool A_KMAJ, bool B_KMAJ>
 __global__ void __launch_bounds__(kThreads, 1)
     sgemm_tma_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b, int M, int N,
                      int K, float* __restrict__ C, int64_t rsc, int64_t csc, int tiles_m, int tiles_n,
-                     int parts, float* __restrict__ part_buf, int* __restrict__ err) {
+                     int streamk, int max_seg, float* __restrict__ slots, int* __restrict__ tile_cnt,
+                     int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)kStages * kStageBytes);
   uint64_t* empty = full + kStages;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(empty + kStages);
+  uint64_t* seg_stored = empty + kStages;   // stream-K: every compute warp stored its part of a segment
+  uint64_t* seg_decided = seg_stored + 1;  // stream-K: the tile count was taken
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(seg_decided + 1);
   auto a_tile = [&](int s) { return smem + (size_t)s * kStageBytes; };
   auto b_tile = [&](int s) { return smem + (size_t)s * kStageBytes + kTileBytes; };
 
@@ -127,6 +134,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kComputeWarps);  // one arrival per compute warp
     }
+    mbar_init(seg_stored, kComputeWarps);
+    mbar_init(seg_decided, 1);
     *abort_flag = 0;
     fence_mbar_init();
     prefetch_tensormap(&tm_a);
@@ -138,20 +147,42 @@ __global__ void __launch_bounds__(kThreads, 1)
     *abort_flag = 1;
     atomicExch(err, (int)GBBLAS_STATUS_TIMEOUT);
   };
-  // work unit u = (tile u / parts, K part u % parts); parts > 1 (split-K):
-  // each unit adds its K range into its own zeroed M x N partial
-  const int nunits = tiles_m * tiles_n * parts;
+  const int ntiles = tiles_m * tiles_n;
   const int nk = (K + kBK - 1) / kBK;
+  // The CTA's segments (tile t, K blocks kb..ke-1), in order: whole tiles
+  // t = blockIdx.x, + gridDim.x, ... or, stream-K, its range of the tiles'
+  // K blocks laid end to end.  seg(i, t, kb, ke) gives segment i; false when
+  // there is none.
+  const int64_t kt_total = (int64_t)ntiles * nk;
+  const int64_t range_b = streamk ? kt_total * blockIdx.x / gridDim.x : 0;
+  const int64_t range_e = streamk ? kt_total * (blockIdx.x + 1) / gridDim.x : 0;
+  auto seg = [&](int64_t& pos, int& t, int& kb, int& ke) -> bool {
+    if (!streamk) {
+      t = (int)pos;
+      if (t >= ntiles) return false;
+      kb = 0;
+      ke = nk;
+      pos += gridDim.x;
+      return true;
+    }
+    if (pos >= range_e) return false;
+    t = (int)(pos / nk);
+    kb = (int)(pos % nk);
+    const int64_t left = range_e - pos;
+    ke = left < (int64_t)(nk - kb) ? kb + (int)left : nk;
+    pos += ke - kb;
+    return true;
+  };
+  const int64_t pos0 = streamk ? range_b : blockIdx.x;
   int issued = 0;
 
   if (warp == kComputeWarps) {
     if (lane == 0) {
       bool stop = false;
-      for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x) {
-        const int t = u / parts, pp = u % parts;
+      int t, kb, ke;
+      for (int64_t pos = pos0; !stop && seg(pos, t, kb, ke);) {
         int m0, n0;
         tile_origin(t, tiles_m, tiles_n, m0, n0);
-        const int kb = (int)((int64_t)nk * pp / parts), ke = (int)((int64_t)nk * (pp + 1) / parts);
         for (int kt = kb; kt < ke; ++kt) {
           const int s = issued % kStages, round = issued / kStages;
           if (round > 0 && !mbar_wait_bounded(&empty[s], (round - 1) & 1, abort_flag, kWaitLimitNs)) {
@@ -176,11 +207,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
     int consumed = 0;
     bool ok = true;
-    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
-      const int t = u / parts, pp = u % parts;
+    int t, kb, ke;
+    int nparts = 0;              // stream-K segments this CTA finished (phases of the two barriers)
+    __shared__ int seg_last;     // stream-K: 1 if this segment is its tile's last to finish
+    for (int64_t pos = pos0; ok && seg(pos, t, kb, ke);) {
       int m0, n0;
       tile_origin(t, tiles_m, tiles_n, m0, n0);
-      const int kb = (int)((int64_t)nk * pp / parts), ke = (int)((int64_t)nk * (pp + 1) / parts);
       float acc[8][8];
 #pragma unroll
       for (int i = 0; i < 8; ++i)
@@ -239,13 +271,60 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&empty[s]);
       }
       if (!ok) break;
-      // C += acc (rows / columns outside the matrix dropped).  Split-K: this
-      // part's dense partial, which no other unit writes - stored, not added.
-      // Loads of C for four rows are issued before their stores (the
-      // compiler cannot see that runtime strides keep the rows apart).
-      const bool partial = parts > 1;
-      float* Ct = partial ? part_buf + (int64_t)pp * M * N : C;
-      const int64_t rs = partial ? (int64_t)N : rsc, cs = partial ? 1 : csc;
+      if (kb != 0 || ke != nk) {
+        // stream-K segment of tile t: segments are numbered in K order by
+        // the CTA that holds their first K block (the largest c with
+        // range_b(c) <= x is ((x + 1) G - 1) / T)
+        const int64_t G = gridDim.x;
+        const int64_t c0 = ((int64_t)t * nk + 1) * G - 1;
+        const int first = (int)(c0 / kt_total), last = (int)((((int64_t)t * nk + nk) * G - 1) / kt_total);
+        const int sidx = (int)blockIdx.x - first, nseg = last - first + 1;
+        float* slot = slots + ((int64_t)t * max_seg + sidx) * (kBM * kBN);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            __stcg(slot + owned<A_KMAJ>(ty, i) * kBN + owned<B_KMAJ>(tx, j), acc[i][j]);
+        // every compute warp's slot stores, then one count per segment
+        // (bounded waits on two barriers: an aborted warp never leaves the
+        // others waiting)
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(seg_stored);
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(seg_stored, nparts & 1, abort_flag, kWaitLimitNs))) {
+          if (lane == 0) fail();
+          break;
+        }
+        if (threadIdx.x == 0) {
+          seg_last = atomicAdd(tile_cnt + t, 1) == nseg - 1;
+          __threadfence();
+          mbar_arrive(seg_decided);
+        }
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(seg_decided, nparts & 1, abort_flag, kWaitLimitNs))) {
+          if (lane == 0) fail();
+          break;
+        }
+        ++nparts;
+        if (!seg_last) continue;  // another segment of the tile finishes it
+        __threadfence();
+        // the last segment: the tile's sum over its slots in K order (this
+        // segment's own slot included), then into C below
+        for (int q = 0; q < nseg; ++q) {
+          const float* sq = slots + ((int64_t)t * max_seg + q) * (kBM * kBN);
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const float v = __ldcg(sq + owned<A_KMAJ>(ty, i) * kBN + owned<B_KMAJ>(tx, j));
+              acc[i][j] = q == 0 ? v : acc[i][j] + v;
+            }
+        }
+      }
+      // C += acc (rows / columns outside the matrix dropped).  Loads of C for
+      // four rows are issued before their stores (the compiler cannot see
+      // that runtime strides keep the rows apart).
+      float* Ct = C;
+      const int64_t rs = rsc, cs = csc;
 #pragma unroll
       for (int i0 = 0; i0 < 8; i0 += 4) {
         if constexpr (!B_KMAJ) {
@@ -258,7 +337,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
               const int n = n0 + tx * 4 + 64 * h;
-              cv[i][h] = (!partial && vec && m < M && n + 4 <= N)
+              cv[i][h] = (vec && m < M && n + 4 <= N)
                              ? *reinterpret_cast<const float4*>(Ct + (int64_t)m * rs + n)
                              : make_float4(0.f, 0.f, 0.f, 0.f);
             }
@@ -284,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int q = 0; q < 4; ++q)
                   if (n + q < N) {
                     float* cq = crow + (int64_t)(n + q) * cs;
-                    *cq = partial ? a4[q] : *cq + a4[q];
+                    *cq += a4[q];
                   }
               }
             }
@@ -299,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
               const int n = n0 + owned<true>(tx, j);
-              old[j] = (!partial && n < N) ? crow[(int64_t)n * cs] : 0.f;
+              old[j] = n < N ? crow[(int64_t)n * cs] : 0.f;
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -321,19 +400,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Split-K: C += part[0] + part[1] + ... (parts in order), grid-stride.
-__global__ void __launch_bounds__(256) sgemm_parts_reduce_kernel(float* __restrict__ C, int64_t rsc, int64_t csc,
-                                                                 const float* __restrict__ part, int M, int N,
-                                                                 int parts) {
-  const int64_t total = (int64_t)M * N;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    float s = part[e];
-    for (int p = 1; p < parts; ++p) s += part[(int64_t)p * total + e];
-    const int64_t r = e / N, c = e % N;
-    C[r * rsc + c * csc] += s;
-  }
-}
-
 // The four kernels' shared-memory attribute, once per device (before any
 // stream capture: tc_prepare calls this too).
 void set_attributes(DeviceCtx* c) {
@@ -350,14 +416,12 @@ void set_attributes(DeviceCtx* c) {
 
 template <bool AK, bool BK>
 gbblas_status launch_cfg(DeviceCtx* c, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t N,
-                         int64_t K, float* C, int64_t rsc, int64_t csc, int* err, cudaStream_t stream, int max_ctas,
-                         int parts, float* part_buf) {
+                         int64_t K, float* C, int64_t rsc, int64_t csc, int* err, cudaStream_t stream, int grid,
+                         int streamk, int max_seg, float* slots, int* tile_cnt) {
   set_attributes(c);
   const int tiles_m = (int)((M + kBM - 1) / kBM), tiles_n = (int)((N + kBN - 1) / kBN);
-  int64_t grid = std::min<int64_t>((int64_t)tiles_m * tiles_n * parts, c->num_sms);
-  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  sgemm_tma_kernel<AK, BK><<<(unsigned)grid, kThreads, kSmem, stream>>>(ma, mb, (int)M, (int)N, (int)K, C, rsc, csc,
-                                                                      tiles_m, tiles_n, parts, part_buf, err);
+  sgemm_tma_kernel<AK, BK><<<(unsigned)grid, kThreads, kSmem, stream>>>(
+      ma, mb, (int)M, (int)N, (int)K, C, rsc, csc, tiles_m, tiles_n, streamk, max_seg, slots, tile_cnt, err);
   return check_launch("sgemm_tma_kernel");
 }
 
@@ -377,7 +441,7 @@ bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t
 
 gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                                int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
-                               int64_t csc, cudaStream_t stream, int max_ctas, int parts) {
+                               int64_t csc, cudaStream_t stream, int max_ctas, int streamk) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if (!sgemm_tma_eligible(M, N, K, A, rsa, csa, B, rsb, csb)) {
     set_error("TMA-fed sgemm: operands not 16-byte aligned with 16-byte-multiple strides");
@@ -394,36 +458,37 @@ gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, co
     GB_TRY(make_map_f32_2d(&mb, B, (uint64_t)K, (uint64_t)N, (uint64_t)csb, kBK, kBN, true));
   else
     GB_TRY(make_map_f32_2d(&mb, B, (uint64_t)N, (uint64_t)K, (uint64_t)rsb, kBN, kBK, false));
-  const int nk = (int)((K + kBK - 1) / kBK);
-  if (parts < 1) parts = 1;
-  if (parts > nk) parts = nk;
-  const size_t part_bytes = parts > 1 ? sizeof(float) * (size_t)parts * (size_t)M * (size_t)N : 0;
-  void* s = nullptr;
-  GB_TRY(get_scratch(c, stream, kScratchZeroBytes + part_bytes, &s));
-  int* err = reinterpret_cast<int*>(static_cast<char*>(s) + kErrWordOffset);
-  float* part_buf = parts > 1 ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
-  // (every element of every part is written by exactly one (tile, part) unit: no clearing)
-  gbblas_status st;
-  if (ak && bk)
-    st = launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
-  else if (ak)
-    st = launch_cfg<true, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
-  else if (bk)
-    st = launch_cfg<false, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
-  else
-    st = launch_cfg<false, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, max_ctas, parts, part_buf);
-  if (st != GBBLAS_STATUS_SUCCESS || parts == 1) return st;
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((M * N + 255) / 256, 4 * (int64_t)c->num_sms));
-  sgemm_parts_reduce_kernel<<<blocks, 256, 0, stream>>>(C, rsc, csc, part_buf, (int)M, (int)N, parts);
-  return check_launch("sgemm_parts_reduce_kernel");
-}
-
-int sgemm_tma_split_parts(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
   const int64_t tiles = ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN);
   const int64_t nk = (K + kBK - 1) / kBK;
-  for (int p = 4; p >= 2; --p)
-    if (tiles * p <= (int64_t)c->num_sms && nk >= 8 * p) return p;
-  return 1;
+  int64_t grid = c->num_sms;
+  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+  if (!streamk) grid = std::min<int64_t>(grid, tiles);
+  grid = std::min<int64_t>(grid, tiles * nk);  // stream-K: every CTA gets at least one K block
+  // stream-K: a tile meets at most (nk - 1) / L + 2 CTA ranges, L the shortest range
+  const int64_t shortest = tiles * nk / grid;
+  const int max_seg = streamk ? (int)((nk - 1) / shortest + 2) : 0;
+  const size_t slot_bytes = streamk ? sizeof(float) * (size_t)kBM * kBN * (size_t)(tiles * max_seg) : 0;
+  const size_t cnt_bytes = streamk ? sizeof(int) * (size_t)tiles : 0;
+  void* s = nullptr;
+  GB_TRY(get_scratch(c, stream, kScratchZeroBytes + slot_bytes + cnt_bytes, &s));
+  int* err = reinterpret_cast<int*>(static_cast<char*>(s) + kErrWordOffset);
+  float* slots = streamk ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
+  int* tile_cnt = streamk ? reinterpret_cast<int*>(static_cast<char*>(s) + kScratchZeroBytes + slot_bytes) : nullptr;
+  // the per-tile counts start at zero (the scratch is shared with other kernels on this stream)
+  if (streamk) GB_CUDA_TRY(cudaMemsetAsync(tile_cnt, 0, cnt_bytes, stream));
+  const int g = (int)grid, sk = streamk ? 1 : 0;
+  if (ak && bk) return launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
+  if (ak) return launch_cfg<true, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
+  if (bk) return launch_cfg<false, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
+  return launch_cfg<false, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
+}
+
+bool sgemm_tma_streamk_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN);
+  const int64_t nk = (K + kBK - 1) / kBK;
+  const int64_t sms = c->num_sms;
+  // whole tiles leave part of the last wave idle, and there is K to share
+  return nk >= 8 && tiles < 4 * sms && tiles % sms != 0 && tiles % sms < sms * 9 / 10;
 }
 
 }  // namespace gbblas

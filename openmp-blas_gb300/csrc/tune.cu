@@ -384,9 +384,9 @@ int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t s
   if (!b.ok()) return -1;
   const gbblas_gemm_desc d = b.desc();
   // 0 = 64 x 64, 1 = 128 x 128 (register-staged), 2 = TMA-fed 128 x 128,
-  // 3 = TMA-fed with split-K, offered where the tiles leave SMs idle (the TMA
-  // kernels' eligibility is the caller's operands': an ineligible call falls back)
-  const int ntile = sgemm_tma_split_parts(c, m, n, k) > 1 ? 4 : 3;
+  // 3 = TMA-fed stream-K, offered where whole tiles fill the SMs badly (the
+  // TMA kernels' eligibility is the caller's operands': an ineligible call falls back)
+  const int ntile = sgemm_tma_streamk_useful(c, m, n, k) ? 4 : 3;
   int best = -1;
   float best_ms = 1e30f;
   for (int tile = 0; tile < ntile; ++tile) {

@@ -141,13 +141,15 @@ def test_padded_pitch_takes_tma_path(cuda, monkeypatch, la, lb):
     assert np.all(np.abs(outs[0] - exact) <= 2 * K * EPS32 * scale)
 
 
-@pytest.mark.parametrize("shape", [(1024, 1024, 1024), (300, 200, 4000), (129, 257, 65), (700, 130, 3000)])
+@pytest.mark.parametrize("shape", [(1024, 1024, 1024), (300, 200, 4000), (129, 257, 65), (700, 130, 3000),
+                                   (128, 128, 8192), (2000, 2000, 512), (1, 1, 4096)])
 @pytest.mark.parametrize("la,lb,lc", [(1, 1, 1), (0, 1, 1), (1, 0, 0), (0, 0, 1)])
 def test_split_k_within_bound(cuda, monkeypatch, shape, la, lb, lc):
-    """GBBLAS_FMA_TILE=3: the TMA-fed kernel cut along K where its tiles leave
-    SMs idle (K ranges added into zeroed partials, then into C in order):
+    """GBBLAS_FMA_TILE=3: the TMA-fed kernel in stream-K form (the tiles' K
+    blocks shared out equally among the SMs; a tile split between CTAs is
+    summed over its segments in K order by the segment that finishes last):
     within the same bound as the unsplit kernels and the same bits on every
-    run.  Shapes too short in K for a split run unsplit."""
+    run."""
     M, N, K = shape
     rng = np.random.default_rng(M + N + K + la + 2 * lb + 4 * lc)
     A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
