@@ -69,8 +69,14 @@ typedef enum gbblas_accuracy {
                                  column of B), kind::f8f6f4 tcgen05 products, FP32
                                  accumulation; ~3 significand bits per operand and
                                  values below 2^-9 of their block's max flush to 0 */
-  GBBLAS_ACCURACY_AUTO = 3,   /* BF16X6 where the shape suits the tensor-core tiles,
-                                 FP32 otherwise */
+  GBBLAS_ACCURACY_AUTO = 3,   /* FP32-accurate, whichever path the autotuner measured
+                                 faster for the shape: FP32, or FP16X3 with a guard -
+                                 outputs in a row of A (column of B) whose nonzero
+                                 magnitudes span more than 14 + log2(K) binades, or
+                                 that holds Inf / NaN, are recomputed with FP32 FMAs,
+                                 so the error stays within (2^-19 + 2 K eps32) (|A||B|)_ij.
+                                 GBBLAS_GEMM_AUTO=0 / 1 forces the FP32 / FP16X3 choice.
+                                 Grouped, batched and served GEMMs: BF16X6 */
   GBBLAS_ACCURACY_BF16X6 = 4, /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
                                  the six products p_i*p_j with i + j < 3 on tcgen05 */
   /* Double-precision GEMM (gbblas_dgemm_ex) only: */

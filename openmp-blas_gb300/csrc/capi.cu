@@ -277,11 +277,11 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
     }
   }
   if constexpr (std::is_same_v<T, float>) {
-    // BF16X3 / BF16X6 / FP8 always take the tensor cores.  AUTO: whichever
-    // FP32-accurate path the autotuner measured faster for this shape bucket
-    // (FMA kernel or split-BF16 with six products).
+    // BF16X3 / BF16X6 / FP16X3 / FP8 always take the tensor cores.  AUTO:
+    // whichever FP32-accurate path the autotuner measured faster for this
+    // shape bucket (FMA kernel or the guarded FP16 split).
     int mode = tc_mode(acc);
-    if (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1) mode = tc_mode(GBBLAS_ACCURACY_BF16X6);
+    if (acc == GBBLAS_ACCURACY_AUTO && tuned_gemm_auto(c, M, N, K) == 1) mode = kTcModeF16Guard;
     if (mode != 0) return launch_gemm_tc(c, mode, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
     // FP32 on the FMA pipe: the tile shape the autotuner measured faster
     return launch_gemm_fma<T>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s, 0,

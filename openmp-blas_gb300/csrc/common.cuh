@@ -92,6 +92,8 @@ constexpr size_t kScratchZeroBytes = 256;
 constexpr size_t kErrWordOffset = 64;
 // Byte offset of the persistent kernels' tile counter (reset before each launch).
 constexpr size_t kTileCounterOffset = 128;
+// Byte offset of the FP16 split guard's two list counts (reset before each launch).
+constexpr size_t kGuardCountOffset = 136;
 gbblas_status get_scratch(DeviceCtx* c, cudaStream_t stream, size_t bytes, void** out);
 
 // Free the scratch of `stream` (stream-ordered) and forget it.
@@ -159,6 +161,11 @@ bool sgemm_tma_streamk_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 // 2 / 3 = FP32 operands split into that many BF16 pieces, 8 = FP8-E4M3 with
 // per-128-K-block power-of-two scales; 0 = not a tensor-core accuracy.
 int tc_mode(gbblas_accuracy acc);
+// The tensor-core mode GBBLAS_ACCURACY_AUTO takes for a single float GEMM:
+// the FP16 split with its guard (rows of A / columns of B whose magnitudes
+// span more binades than the split's error bound allows are recomputed with
+// FP32 FMAs).
+constexpr int kTcModeF16Guard = 13;
 // Device bytes of the operand arena one problem needs in `mode`.
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K);
 
@@ -220,7 +227,7 @@ gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, bool guarded, int64_
 // per problem (batch.cu).
 gbblas_status launch_gemv_group(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count, cudaStream_t s);
 
-// Autotuner (tune.cu): AUTO accuracy -> 1 = split-BF16 six products, 0 = FMA.
+// Autotuner (tune.cu): AUTO accuracy -> 1 = the guarded FP16 split (kTcModeF16Guard), 0 = FMA.
 int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 // Autotuner: split-K parts and CTA form of one tensor-core GEMM.
 TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, cudaStream_t stream);

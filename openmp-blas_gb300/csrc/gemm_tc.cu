@@ -108,6 +108,8 @@ constexpr size_t kSmemLimit = 232448;             // 227 KB per CTA
 // split into two FP16 pieces (11 significand bits each), three products.
 constexpr int kModeFp8 = 8;
 constexpr int kModeF16 = 12;
+// kModeF16 with the AUTO guard (host-side plan mode; the kernels run kModeF16)
+constexpr int kModeF16Guard = kTcModeF16Guard;
 
 template <int MODE>
 struct ModeTraits {
@@ -243,38 +245,59 @@ struct PrepTile {
 // One CTA per tile.  Interior tiles of 16-byte-aligned sources are read with
 // 128-bit loads along whichever dimension is contiguous; edge tiles and other
 // strides element by element (still coalesced along the contiguous side).
-// FP16 split: e[R] for every arena row R = the frexp exponent of the row's
-// largest magnitude (so the row, scaled by 2^(15 - e), lies below 2^15 and
-// inside FP16's range).  Same tiles as the preparation; magnitudes compared
-// as bit patterns; the rows' maxima of a tile combined in shared memory and
-// then atomicMax-ed into e (which starts filled with the byte 0x80: a row no
-// tile wrote, all zero or padding, reads as 0).
+// FP16 split: every row is scaled by 2^(15 - e), e the frexp exponent of its
+// largest magnitude (f16_scale_kernel), so it lies below 2^15 and inside
+// FP16's range.
 constexpr int kF16ScaleTop = 15;
 
+// Magnitude bits of a float (comparable as unsigned integers), and the same
+// with zero mapped above every finite magnitude (for the smallest nonzero).
+__device__ __forceinline__ unsigned mag_bits(float v) { return __float_as_uint(v) & 0x7FFFFFFFu; }
+__device__ __forceinline__ unsigned nz_bits(float v) {
+  const unsigned m = mag_bits(v);
+  return m ? m : 0xFFFFFFFFu;
+}
+
 // Edge / strided tiles of f16_scale_kernel: value i of a thread (element
-// tid + 256 i of the 64 x 64 tile) into the rows' maxima.  K contiguous: it
-// lies in row tid / 64 + 4 i and a warp's 32 lanes hold 32 K of that row (one
-// shared atomic per warp and row); otherwise all 16 lie in row tid % 64.
-__device__ __forceinline__ void f16_scale_tile_rows(const unsigned (&m)[16], int tid, bool k_contig,
-                                                    unsigned* rmax) {
+// tid + 256 i of the 64 x 64 tile, as magnitude bits mx / nonzero bits mn)
+// into the rows' maxima and nonzero minima.  K contiguous: it lies in row
+// tid / 64 + 4 i and a warp's 32 lanes hold 32 K of that row (one shared
+// atomic per warp and row); otherwise all 16 lie in row tid % 64.
+__device__ __forceinline__ void f16_scale_tile_rows(const unsigned (&mx)[16], const unsigned (&mn)[16], int tid,
+                                                    bool k_contig, unsigned* rmax, unsigned* rmin) {
   if (k_contig) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      const unsigned w = __reduce_max_sync(0xffffffffu, m[i]);
-      if ((tid & 31) == 0 && w) atomicMax(&rmax[tid / 64 + 4 * i], w);
+      const unsigned w = __reduce_max_sync(0xffffffffu, mx[i]);
+      const unsigned v = __reduce_min_sync(0xffffffffu, mn[i]);
+      if ((tid & 31) == 0) {
+        if (w) atomicMax(&rmax[tid / 64 + 4 * i], w);
+        if (v != 0xFFFFFFFFu) atomicMin(&rmin[tid / 64 + 4 * i], v);
+      }
     }
   } else {
-    unsigned w = 0u;
+    unsigned w = 0u, v = 0xFFFFFFFFu;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) w = max(w, m[i]);
+    for (int i = 0; i < 16; ++i) {
+      w = max(w, mx[i]);
+      v = min(v, mn[i]);
+    }
     if (w) atomicMax(&rmax[tid % 64], w);
+    if (v != 0xFFFFFFFFu) atomicMin(&rmin[tid % 64], v);
   }
 }
 
+// For every arena row R: e[R] = the frexp exponent of the row's largest
+// magnitude, and (emin non-null, for the AUTO guard) emin[R] = the
+// magnitude bits of its smallest nonzero element.  Same tiles as the
+// preparation; magnitudes compared as bit patterns; the rows' extremes of a
+// tile combined in shared memory, then atomicMax-ed into e (which starts
+// filled with the byte 0x80: a row no tile wrote, all zero or padding, reads
+// as 0) and atomicMin-ed into emin (which starts at 0xFFFFFFFF).
 __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restrict__ jobs, int njobs,
-                                                        int* __restrict__ e_out) {
+                                                        int* __restrict__ e_out, unsigned* __restrict__ emin_out) {
   constexpr int TK = 64, TR = 64;
-  __shared__ unsigned int rmax[TR];
+  __shared__ unsigned int rmax[TR], rmin[TR];
   __shared__ int sjob;
   const int t = blockIdx.x, tid = threadIdx.x;
   if (tid == 0) {
@@ -288,68 +311,87 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restri
     }
     sjob = lo;
   }
-  if (tid < TR) rmax[tid] = 0u;
+  if (tid < TR) {
+    rmax[tid] = 0u;
+    rmin[tid] = 0xFFFFFFFFu;
+  }
   __syncthreads();
   const SplitJob& j = jobs[sjob];
   const int local = t - j.tile_start;
   const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
   const bool full = r0 + TR <= j.rows && k0 + TK <= j.K;
   const bool al16 = (reinterpret_cast<uintptr_t>(j.src) & 15) == 0;
-  auto mag4 = [](float4 v) {
-    return max(max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu),
-               max(__float_as_uint(v.z) & 0x7FFFFFFFu, __float_as_uint(v.w) & 0x7FFFFFFFu));
-  };
   if (full && al16 && j.cs == 1 && (j.rs & 3) == 0) {
     // interior tile, K contiguous: 128-bit loads, float4 i of a thread in row
     // tid / 16 + 16 i; the 16 lanes of a half-warp share that row
-    unsigned w[4];
+    unsigned w[4], v[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i;
-      w[i] = mag4(dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + idx / 16) * j.rs + k0 + 4 * (idx % 16))));
+      const float4 x =
+          dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + idx / 16) * j.rs + k0 + 4 * (idx % 16)));
+      w[i] = max(max(mag_bits(x.x), mag_bits(x.y)), max(mag_bits(x.z), mag_bits(x.w)));
+      v[i] = min(min(nz_bits(x.x), nz_bits(x.y)), min(nz_bits(x.z), nz_bits(x.w)));
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
 #pragma unroll
-      for (int o = 8; o > 0; o >>= 1) w[i] = max(w[i], __shfl_xor_sync(0xffffffffu, w[i], o));
-      if ((tid & 15) == 0 && w[i]) atomicMax(&rmax[tid / 16 + 16 * i], w[i]);
+      for (int o = 8; o > 0; o >>= 1) {
+        w[i] = max(w[i], __shfl_xor_sync(0xffffffffu, w[i], o));
+        v[i] = min(v[i], __shfl_xor_sync(0xffffffffu, v[i], o));
+      }
+      if ((tid & 15) == 0) {
+        if (w[i]) atomicMax(&rmax[tid / 16 + 16 * i], w[i]);
+        if (v[i] != 0xFFFFFFFFu) atomicMin(&rmin[tid / 16 + 16 * i], v[i]);
+      }
     }
   } else if (full && al16 && j.rs == 1 && (j.cs & 3) == 0) {
     // interior tile, rows contiguous: 128-bit loads of rows 4 (tid % 16) .. + 3,
     // the same four rows for all of a thread's loads; lanes l and l ^ 16 too
-    unsigned w[4] = {0u, 0u, 0u, 0u};
+    unsigned w[4] = {0u, 0u, 0u, 0u}, v[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i;
-      const float4 v =
+      const float4 x =
           dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + idx / 16) * j.cs + r0 + 4 * (idx % 16)));
-      w[0] = max(w[0], __float_as_uint(v.x) & 0x7FFFFFFFu);
-      w[1] = max(w[1], __float_as_uint(v.y) & 0x7FFFFFFFu);
-      w[2] = max(w[2], __float_as_uint(v.z) & 0x7FFFFFFFu);
-      w[3] = max(w[3], __float_as_uint(v.w) & 0x7FFFFFFFu);
+      w[0] = max(w[0], mag_bits(x.x));
+      w[1] = max(w[1], mag_bits(x.y));
+      w[2] = max(w[2], mag_bits(x.z));
+      w[3] = max(w[3], mag_bits(x.w));
+      v[0] = min(v[0], nz_bits(x.x));
+      v[1] = min(v[1], nz_bits(x.y));
+      v[2] = min(v[2], nz_bits(x.z));
+      v[3] = min(v[3], nz_bits(x.w));
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       w[q] = max(w[q], __shfl_xor_sync(0xffffffffu, w[q], 16));
-      if ((tid & 31) < 16 && w[q]) atomicMax(&rmax[4 * (tid % 16) + q], w[q]);
+      v[q] = min(v[q], __shfl_xor_sync(0xffffffffu, v[q], 16));
+      if ((tid & 31) < 16) {
+        if (w[q]) atomicMax(&rmax[4 * (tid % 16) + q], w[q]);
+        if (v[q] != 0xFFFFFFFFu) atomicMin(&rmin[4 * (tid % 16) + q], v[q]);
+      }
     }
   } else {
-    unsigned int m[16];
+    unsigned mx[16], mn[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int idx = tid + 256 * i;
       const int r = j.cs == 1 ? idx / TK : idx % TR, k = j.cs == 1 ? idx % TK : idx / TR;
-      m[i] = (r0 + r < j.rows && k0 + k < j.K)
-                 ? (__float_as_uint(__ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs)) & 0x7FFFFFFFu)
-                 : 0u;
+      const float x = (r0 + r < j.rows && k0 + k < j.K) ? __ldg(j.src + (r0 + r) * j.rs + (k0 + k) * j.cs) : 0.f;
+      mx[i] = mag_bits(x);
+      mn[i] = nz_bits(x);
     }
-    f16_scale_tile_rows(m, tid, j.cs == 1, rmax);
+    f16_scale_tile_rows(mx, mn, tid, j.cs == 1, rmax, rmin);
   }
   __syncthreads();
-  if (tid < TR && r0 + tid < j.rows && rmax[tid] != 0u) {
-    int e;
-    (void)frexpf(__uint_as_float(rmax[tid] >= 0x7F800000u ? 0x7F7FFFFFu : rmax[tid]), &e);  // Inf / NaN: the top exponent
-    atomicMax(e_out + j.dst_row + r0 + tid, e);
+  if (tid < TR && r0 + tid < j.rows) {
+    if (rmax[tid] != 0u) {
+      int e;
+      (void)frexpf(__uint_as_float(rmax[tid] >= 0x7F800000u ? 0x7F7FFFFFu : rmax[tid]), &e);  // Inf / NaN: the top exponent
+      atomicMax(e_out + j.dst_row + r0 + tid, e);
+    }
+    if (emin_out && rmin[tid] != 0xFFFFFFFFu) atomicMin(emin_out + j.dst_row + r0 + tid, rmin[tid]);
   }
 }
 
@@ -365,10 +407,35 @@ __device__ __forceinline__ int f16_row_exp(const int* e, int64_t row) {
   return v == (int)0x80808080 ? 0 : v;
 }
 
+// The guard of the FP16 split under GBBLAS_ACCURACY_AUTO, per operand.  An
+// element of a row scaled by 2^(15 - e) keeps 22 significant bits while its
+// low piece stays a normal FP16 number; below that its absolute error is at
+// most 2^-25 of FP16's subnormal step, 2^(e - 40).  In a row whose nonzero
+// magnitudes span at most S binades (floor(log2 max) - floor(log2 min)),
+// that is at most 2^(S - 39) |a|, so over a K-term dot the FP16 split's
+// error stays within 3 * 2^-22 + 2 K eps32 of (|A||B|)_ij - the FP32 GEMM
+// rule - when 2^(S - 38) <= K 2^-24, i.e. S <= 14 + floor(log2 K).  Rows (of A,
+// and columns of B) beyond that span, or holding Inf or NaN, are "out of
+// span": flags[R] = 1 and R goes onto `list`; the GEMM leaves their outputs
+// alone and f16_guard_fixup_kernel computes them with FP32 FMAs.
+struct F16Guard {
+  const unsigned* emin = nullptr;  // smallest nonzero magnitude bits per arena row (f16_scale_kernel)
+  int* flags = nullptr;            // per arena row: 1 = out of span (every row written)
+  int* list = nullptr;             // out-of-span arena rows, in no particular order
+  int* count = nullptr;            // entries in list
+};
+
+// floor(log2 x) + 127 for the magnitude bits of a nonzero float (subnormals
+// included).
+__device__ __forceinline__ int biased_log2(unsigned bits) {
+  return bits >= 0x00800000u ? (int)(bits >> 23) : 9 - __clz(bits);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
                                                          void* __restrict__ out, int64_t piece_stride, int64_t pitch,
-                                                         uint32_t* __restrict__ scales, int64_t scale_stride) {
+                                                         uint32_t* __restrict__ scales, int64_t scale_stride,
+                                                         F16Guard guard) {
   using PT = PrepTile<MODE>;
   constexpr int TK = PT::TK, TR = PT::TR, LD = PT::LD;
   __shared__ __align__(16) float tile[TR * LD];
@@ -458,6 +525,18 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
     // h = fp16_rn(v), l = fp16_rn(v - h) (v - h exact in FP32)
     __half* ph = static_cast<__half*>(out);
     const int* erow = reinterpret_cast<const int*>(scales);
+    if (guard.flags && k0 == 0 && tid < TR) {  // the guard: one decision per row, by its first K tile
+      const int64_t row = j.dst_row + r0 + tid;
+      int out_of_span = 0;
+      if (r0 + tid < j.rows) {
+        const int e = f16_row_exp(erow, row);  // floor(log2 max) + 1; 128 for Inf / NaN (or >= 2^127)
+        const unsigned mn = guard.emin[row];
+        const int span_max = 14 + (63 - __clzll((unsigned long long)(j.K > 0 ? j.K : 1)));  // 14 + floor(log2 K)
+        out_of_span = e >= 128 || (mn != 0xFFFFFFFFu && (e - 1) - (biased_log2(mn) - 127) > span_max);
+      }
+      guard.flags[row] = out_of_span;
+      if (out_of_span) guard.list[atomicAdd(guard.count, 1)] = (int)row;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = warp * 8 + 2 * i + (lane >> 4), kk = (lane & 15) * 4;
@@ -550,7 +629,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                       const TcProblem* __restrict__ probs, int nprob, int total_tiles, int64_t sf_stride,
                       int* __restrict__ tile_counter, int* __restrict__ err,
-                      const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb) {
+                      const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
+                      const int* __restrict__ guard_a, const int* __restrict__ guard_b) {
   using MT = ModeTraits<MODE>;
   using CF = TcCfg<MODE, PAIR>;
   constexpr int P = MT::P;
@@ -941,6 +1021,11 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       if (!ok) break;
       const int aborted = __shfl_sync(0xffffffffu, *abort_flag, 0);
       if (aborted) break;
+      // FP16 split under the AUTO guard: outputs of out-of-span rows of A /
+      // columns of B are left to f16_guard_fixup_kernel (bit c of skip_cols
+      // = column col0 + c of the tile)
+      bool skip_row = false;
+      uint64_t skip_cols = 0;
       if constexpr (MT::f16) {
         // undo the row and column scales: acc * 2^(e_i + f_j - 30)
         const int* ea = reinterpret_cast<const int*>(sa);
@@ -949,6 +1034,12 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
 #pragma unroll
         for (int c = 0; c < kCols; ++c)
           acc[c] = scale_pow2(acc[c], ei + f16_row_exp(eb, (int64_t)pr.b_row + n0 + col0 + c));
+        if (guard_a) {
+          skip_row = guard_a[(int64_t)pr.a_row + m0 + q * 32 + lane] != 0;
+#pragma unroll
+          for (int c = 0; c < kCols; ++c)
+            if (__ldg(guard_b + (int64_t)pr.b_row + n0 + col0 + c)) skip_cols |= uint64_t(1) << c;
+        }
       }
       if constexpr (MT::fp8) {
         if (pr.c_tma) {
@@ -975,10 +1066,10 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         }
       }
       const int row = m0 + q * 32 + lane;
-      if (row < pr.M) {
+      if (row < pr.M && !skip_row) {
         float* crow = pr.C + (int64_t)row * pr.rsc;
-        const bool vec =
-            (pr.csc == 1) && ((pr.rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(pr.C) & 15) == 0);
+        const bool vec = (pr.csc == 1) && ((pr.rsc & 3) == 0) && ((reinterpret_cast<uintptr_t>(pr.C) & 15) == 0) &&
+                         skip_cols == 0;
         const int cn = n0 + col0;
         // C += acc; a split-K partial (overwrite) is stored instead, into
         // dense 16-byte-aligned rows
@@ -1005,7 +1096,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
         } else {
 #pragma unroll
           for (int j = 0; j < kCols; ++j)
-            if (cn + j < pr.N) {
+            if (cn + j < pr.N && !((skip_cols >> j) & 1)) {
               float* q = crow + (int64_t)(cn + j) * pr.csc;
               *q = add ? *q + acc[j] : acc[j];
             }
@@ -1048,6 +1139,65 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       tmem_dealloc(tmem, CF::kTmemCols);
   }
   if constexpr (PAIR) cluster_sync_all();
+}
+
+// The FP16 split's guard, second half: C += A B for the outputs the GEMM
+// left alone - every column of each out-of-span row of A, and every row (not
+// itself out of span) of each out-of-span column of B - as FP32 FMA dot
+// products, one warp per output: lane l sums k = l, l + 32, ... in order,
+// then the lanes' sums meet in a fixed shuffle tree.  Error at most
+// (K / 32 + 5) eps32 (|A||B|)_ij, order fixed: the same bits on every run.
+// CTAs take the listed rows in turn; with empty lists every CTA returns at
+// once.  jobs: the A jobs then the B^T jobs of a group without split-K
+// (problem i = job i).
+__global__ void __launch_bounds__(256) f16_guard_fixup_kernel(const SplitJob* __restrict__ jobs, int njobs,
+                                                              const TcProblem* __restrict__ probs,
+                                                              const int* __restrict__ list_a,
+                                                              const int* __restrict__ list_b,
+                                                              const int* __restrict__ counts,
+                                                              const int* __restrict__ flags_a) {
+  const int na = counts[0], nb = counts[1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  auto job_of = [&](const SplitJob* js, int64_t row) {  // last job with dst_row <= row
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (js[mid].dst_row <= row)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return lo;
+  };
+  auto dot = [&](const SplitJob& ja, int64_t i, const SplitJob& jb, int64_t jcol) {
+    float s = 0.f;
+    for (int64_t k = lane; k < ja.K; k += 32) s = fmaf(ja.src[i * ja.rs + k * ja.cs], jb.src[jcol * jb.rs + k * jb.cs], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+  };
+  for (int e = blockIdx.x; e < na + nb; e += gridDim.x) {
+    const bool row_entry = e < na;
+    const int64_t r = row_entry ? list_a[e] : list_b[e - na];
+    const int ji = job_of(row_entry ? jobs : jobs + njobs, r);
+    const SplitJob& ja = jobs[ji];
+    const SplitJob& jb = jobs[njobs + ji];
+    const TcProblem& p = probs[ji];
+    if (row_entry) {
+      const int64_t i = r - ja.dst_row;  // every column of row i
+      for (int64_t jc = warp; jc < p.N; jc += nwarps) {
+        const float v = dot(ja, i, jb, jc);
+        if (lane == 0) p.C[i * p.rsc + jc * p.csc] += v;
+      }
+    } else {
+      const int64_t jc = r - jb.dst_row;  // every row of column jc, but the out-of-span rows' (done above)
+      for (int64_t i = warp; i < p.M; i += nwarps) {
+        if (flags_a[ja.dst_row + i]) continue;
+        const float v = dot(ja, i, jb, jc);
+        if (lane == 0) p.C[i * p.rsc + jc * p.csc] += v;
+      }
+    }
+  }
 }
 
 // Split-K: C += part[0] + part[1] + ... (in that order) for every element of
@@ -1164,6 +1314,8 @@ struct TcGroupPlan {
   bool owned = false;    // base allocated by the plan (graph plans)
   CUtensorMap map_a, map_b;
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
+  bool guard = false;  // FP16 split with the AUTO guard (F16Guard, f16_guard_fixup_kernel)
+  size_t off_gmin = 0, off_gflag = 0, off_glist = 0;  // guard arrays: A rows then B rows each
   bool fp8() const { return mode == kModeFp8; }
   bool f16() const { return mode == kModeF16; }
   int planes() const { return fp8() ? 1 : (f16() ? 2 : mode); }
@@ -1185,10 +1337,12 @@ namespace {
 // GBBLAS_TC_PAIR setting).
 gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcGroupPlan& pl,
                          const TcLaunchOpts& opt = TcLaunchOpts()) {
-  if (mode != 2 && mode != 3 && mode != kModeFp8 && mode != kModeF16) {
+  if (mode != 2 && mode != 3 && mode != kModeFp8 && mode != kModeF16 && mode != kModeF16Guard) {
     set_error("tensor-core gemm: unknown mode %d", mode);
     return GBBLAS_STATUS_INVALID_VALUE;
   }
+  pl.guard = mode == kModeF16Guard;
+  if (pl.guard) mode = kModeF16;
   pl.mode = mode;
   const int64_t sk = pl.slice_k(), pk = pl.pad_k(), jk = pl.job_k(), jr = 4096 / jk;
   std::vector<int64_t> order;
@@ -1230,7 +1384,8 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     const gbblas_gemm_desc& g = d[order[i]];
     const int64_t Mp = round_up(g.M, bmt), Np = round_up(g.N, kBN), Kp = round_up(g.K, pk);
     const int num_kt = (int)(Kp / sk);  // pk is a multiple of sk
-    const int parts = std::max(1, std::min(opt.split, num_kt));
+    // (the guard's fixup pairs problem i with job i: no split-K under it)
+    const int parts = pl.guard ? 1 : std::max(1, std::min(opt.split, num_kt));
     const int64_t ppitch = round_up(g.N, 4);  // partial rows stay 16-byte aligned
     if (parts > 1) {
       pl.reds.push_back({g.C, g.rsc, g.csc, nullptr, (int)g.M, (int)g.N, (int)ppitch, parts});
@@ -1289,7 +1444,11 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
   // 4-byte power-of-two exponent per row
   const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : (pl.f16() ? 1 : 0);
   pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
-  pl.off_ws = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
+  const size_t guard_rows = pl.guard ? (size_t)(pl.a_rows + pl.b_rows) : 0;
+  pl.off_gmin = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
+  pl.off_gflag = pl.off_gmin + align256(guard_rows * sizeof(uint32_t));
+  pl.off_glist = pl.off_gflag + align256(guard_rows * sizeof(int));
+  pl.off_ws = pl.off_glist + align256(guard_rows * sizeof(int));
   pl.bytes = pl.off_ws + align256((size_t)ws);
   return GBBLAS_STATUS_SUCCESS;
 }
@@ -1376,8 +1535,10 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
     if (units > cap) units = cap;
   }
   if constexpr (!PAIR) {
+    const int* ga = pl.guard ? reinterpret_cast<const int*>(pl.base + pl.off_gflag) : nullptr;
     gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
-        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.kpad, counter, err, scales_a(pl), scales_b(pl));
+        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.kpad, counter, err, scales_a(pl), scales_b(pl), ga,
+        ga ? ga + pl.a_rows : nullptr);
     return check_launch("gemm_split_kernel");
   } else {
   cudaLaunchConfig_t cfg = {};
@@ -1394,7 +1555,8 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   cfg.numAttrs = 1;
   const cudaError_t e =
       cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                         pl.kpad, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl));
+                         pl.kpad, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl),
+                         (const int*)nullptr, (const int*)nullptr);
   if (e != cudaSuccess) {
     count_launch();
     set_error("launch of gemm_split_kernel (CTA pairs) failed: %s", cudaGetErrorString(e));
@@ -1410,23 +1572,36 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+  F16Guard ga, gb;  // AUTO guard arrays (A rows, then B^T rows)
+  int* gcounts = reinterpret_cast<int*>(pl.base + kGuardCountOffset);
   if constexpr (MODE == kModeF16) {
-    // per-row exponents of A's and B^T's arena rows, then the pieces
+    if (pl.guard) {
+      unsigned* gmin = reinterpret_cast<unsigned*>(pl.base + pl.off_gmin);
+      int* gflag = reinterpret_cast<int*>(pl.base + pl.off_gflag);
+      int* glist = reinterpret_cast<int*>(pl.base + pl.off_glist);
+      ga = F16Guard{gmin, gflag, glist, gcounts};
+      gb = F16Guard{gmin + pl.a_rows, gflag + pl.a_rows, glist + pl.a_rows, gcounts + 1};
+      GB_CUDA_TRY(cudaMemsetAsync(gmin, 0xFF, sizeof(unsigned) * (size_t)(pl.a_rows + pl.b_rows), stream));
+      GB_CUDA_TRY(cudaMemsetAsync(gcounts, 0, 2 * sizeof(int), stream));
+    }
+    // per-row exponents of A's and B^T's arena rows (and the guard's minima), then the pieces
     GB_CUDA_TRY(cudaMemsetAsync(scales_a(pl), 0x80, sizeof(int) * (size_t)pl.a_rows, stream));
     GB_CUDA_TRY(cudaMemsetAsync(scales_b(pl), 0x80, sizeof(int) * (size_t)pl.b_rows, stream));
-    f16_scale_kernel<<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, reinterpret_cast<int*>(scales_a(pl)));
+    f16_scale_kernel<<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, reinterpret_cast<int*>(scales_a(pl)),
+                                                     const_cast<unsigned*>(ga.emin));
     GB_TRY(check_launch("f16_scale_kernel(A)"));
-    f16_scale_kernel<<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, reinterpret_cast<int*>(scales_b(pl)));
+    f16_scale_kernel<<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, reinterpret_cast<int*>(scales_b(pl)),
+                                                     const_cast<unsigned*>(gb.emin));
     GB_TRY(check_launch("f16_scale_kernel(B)"));
   }
   // FP8 scale words: 128 per K-block of each 128-row block, i.e. `kpad` per row block
   prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, arena_a(pl),
                                                           (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
-                                                          pl.kpad);
+                                                          pl.kpad, ga);
   GB_TRY(check_launch("prep_group_kernel(A)"));
   prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, arena_b(pl),
                                                           (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
-                                                          pl.kpad);
+                                                          pl.kpad, gb);
   GB_TRY(check_launch("prep_group_kernel(B)"));
   gbblas_status st;
   if constexpr (MODE != kModeFp8 && MODE != kModeF16) {
@@ -1434,6 +1609,12 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                  : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
   } else {
     st = launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
+  }
+  if (st == GBBLAS_STATUS_SUCCESS && pl.guard) {
+    f16_guard_fixup_kernel<<<2 * c->num_sms, 256, 0, stream>>>(
+        djobs, pl.njobs, reinterpret_cast<const TcProblem*>(pl.base + pl.off_probs), ga.list, gb.list, gcounts,
+        ga.flags);
+    st = check_launch("f16_guard_fixup_kernel");
   }
   if (st != GBBLAS_STATUS_SUCCESS || pl.reds.empty()) return st;
   int64_t most = 0;
@@ -1447,6 +1628,7 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
 }  // namespace
 
 int tc_stage_k(int mode) {
+  if (mode == kModeF16Guard) mode = kModeF16;
   return mode == kModeFp8 ? ModeTraits<kModeFp8>::kBKe : (mode == 3 ? ModeTraits<3>::kBKe : ModeTraits<2>::kBKe);
 }
 
@@ -1461,11 +1643,13 @@ int tc_mode(gbblas_accuracy acc) {
 }
 
 size_t tc_arena_bytes(int mode, int64_t M, int64_t N, int64_t K) {
+  const bool guard = mode == kModeF16Guard;
+  if (guard) mode = kModeF16;
   const bool fp8 = mode == kModeFp8;
   const int64_t planes = fp8 ? 1 : (mode == kModeF16 ? 2 : mode), sk = fp8 ? ModeTraits<kModeFp8>::kBKe : kBK;
   const int64_t rows = round_up(M, 2 * kBM) + round_up(N, kBN), Kp = round_up(K, sk);
   return (size_t)(rows * (Kp * (fp8 ? 1 : 2) + kPitchPadBytes) * planes + (fp8 ? rows * (Kp / 128) * 4 : 0) +
-                  (mode == kModeF16 ? rows * 4 : 0));
+                  (mode == kModeF16 ? rows * 4 : 0) + (guard ? rows * 12 : 0));
 }
 
 void tc_prepare(DeviceCtx* c) {
@@ -1558,7 +1742,9 @@ gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64
                              int64_t csc, cudaStream_t stream) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   gbblas_gemm_desc d{M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc};
-  return launch_gemm_tc_opts(c, mode, d, tuned_tc_opts(c, mode, M, N, K, stream), stream);
+  // (the guarded FP16 split runs single CTAs without split-K: nothing to tune)
+  return launch_gemm_tc_opts(c, mode, d, mode == kModeF16Guard ? TcLaunchOpts() : tuned_tc_opts(c, mode, M, N, K, stream),
+                             stream);
 }
 
 }  // namespace gbblas

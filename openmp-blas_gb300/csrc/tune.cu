@@ -16,9 +16,9 @@
 // Tuned choices:
 //   gemv_group_rows  rows per warp item of the grouped row-streaming GEMV
 //                    (1, 2, 4, 8), bucketed by median log2 rows / cols;
-//   gemm_auto        for GBBLAS_ACCURACY_AUTO, FP32 FMA kernel or split-BF16
-//                    (six products) - both FP32-accurate - bucketed by
-//                    log2 M, N, K;
+//   gemm_auto        for GBBLAS_ACCURACY_AUTO, FP32 FMA kernel or the guarded
+//                    FP16 split (three products) - both FP32-accurate -
+//                    bucketed by log2 M, N, K;
 //   gemm_tc          per tensor-core mode and log2 M, N, K bucket: split-K
 //                    parts (1, 2, 4, 8, 16; offered when K >= 4 max(M, N) and
 //                    the output tiles fill at most half the SMs) and the CTA
@@ -26,7 +26,7 @@
 //                    GBBLAS_TC_SPLITK=n forces n parts;
 //   gemm_fma_tile    FP32 FMA kernel and CTA tile per bucket: 64 x 64 or
 //                    128 x 128 register-staged, the TMA-fed 128 x 128, or
-//                    that with split-K where its tiles leave SMs idle;
+//                    that in stream-K form where whole tiles fill the SMs badly;
 //                    GBBLAS_FMA_TILE=0 / 1 / 2 / 3 forces one.
 // Nothing is timed while the caller's stream is being captured into a graph
 // (the defaults apply); single-call paths consult the tuner, grouped,
@@ -252,10 +252,11 @@ int tuned_gemv_group_rows(DeviceCtx* c, const gbblas_gemv_desc* d, int64_t count
 // 1 = split-BF16 (six products), 0 = FP32 FMA, for an AUTO-accuracy GEMM of
 // this shape.  Without tuning: the tensor cores once the work fills them.
 int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
+  if (const char* e = std::getenv("GBBLAS_GEMM_AUTO"); e && (e[0] == '0' || e[0] == '1')) return e[0] - '0';
   const int fallback = (M >= 256 && N >= 256 && K >= 256 && (double)M * N * K >= 1.0e9) ? 1 : 0;
   Tuner& t = Tuner::get();
   const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
-  const std::string key = "gemm_auto|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
+  const std::string key = "gemm_auto_f16g|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
                           "|k" + std::to_string(bk) + "|f32";
   int v = t.lookup(key);
   if (v >= 0) return v;
@@ -281,7 +282,7 @@ int tuned_gemm_auto(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
   float best_ms[2] = {1e30f, 1e30f};
   for (int choice = 0; choice < 2; ++choice) {
     auto run = [&]() {
-      return choice == 1 ? launch_gemm_tc(c, tc_mode(GBBLAS_ACCURACY_BF16X6), m, n, k, A, k, 1, B, n, 1, C, n, 1, s)
+      return choice == 1 ? launch_gemm_tc(c, kTcModeF16Guard, m, n, k, A, k, 1, B, n, 1, C, n, 1, s)
                          : launch_gemm_fma<float>(c, m, n, k, A, k, 1, B, n, 1, C, n, 1, s);
     };
     if (run() != GBBLAS_STATUS_SUCCESS) continue;  // warm-up

@@ -139,15 +139,102 @@ def test_1024_error_vs_plain_fp32(cuda):
 
 def test_auto_accuracy_picks_an_fp32_accurate_path(cuda):
     """AUTO runs whichever FP32-accurate path the autotuner measured faster
-    for the shape bucket: its result is bit-identical to that path's."""
+    for the shape bucket: its result is bit-identical to that path's (on
+    U[-1,1) operands at K = 1024 every row and column is within the FP16
+    split's span, so its guard changes nothing)."""
     rng = np.random.default_rng(10)
     A = rng.uniform(-1, 1, (1024, 1024)).astype(np.float32)
     B = rng.uniform(-1, 1, (1024, 1024)).astype(np.float32)
     Z = np.zeros((1024, 1024), np.float32)
     auto = run(cuda, A, B, Z, 1, 1, 1, accuracy=3)
-    six = run(cuda, A, B, Z, 1, 1, 1, accuracy=BF16X6)
+    f16 = run(cuda, A, B, Z, 1, 1, 1, accuracy=FP16X3)
     fma = run(cuda, A, B, Z, 1, 1, 1, accuracy=0)
-    assert np.array_equal(auto, six) or np.array_equal(auto, fma)
+    assert np.array_equal(auto, f16) or np.array_equal(auto, fma)
+
+
+def _auto_tc(torch, monkeypatch, A, B, C0, la=1, lb=1, lc=1):
+    monkeypatch.setenv("GBBLAS_GEMM_AUTO", "1")  # AUTO on the tensor cores: the guarded FP16 split
+    return run(torch, A, B, C0, la, lb, lc, accuracy=3)
+
+
+@pytest.mark.parametrize("lc,la,lb", [(1, 1, 1), (0, 0, 0), (1, 0, 1)])
+def test_auto_guard_recomputes_out_of_span_rows_and_columns(cuda, monkeypatch, lc, la, lb):
+    """Rows of A and columns of B mixing magnitudes far apart (one entry of
+    2^20 among entries of 2^-20, beyond the FP16 split's span at this K) fall
+    back to FP32 FMAs: AUTO meets (2^-19 + 2 K eps32)(|A||B|) everywhere,
+    while the plain FP16 split misses it on those rows and columns (the big
+    entry meets a zero on the other side, so the small entries, which the
+    row's scale pushes into FP16's subnormal range, make the whole result);
+    every other output equals the plain FP16 split's bit for bit."""
+    rng = np.random.default_rng(21)
+    M, N, K = 300, 260, 512
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    bad_rows, bad_cols = [3, 150, 299], [0, 77, 259]
+    for r in bad_rows:
+        A[r] = rng.uniform(-1, 1, K).astype(np.float32) * 2.0 ** -20
+        A[r, r % K] = 2.0 ** 20
+        B[r % K, :] = 0.0
+    for c in bad_cols:
+        B[:, c] = rng.uniform(-1, 1, K).astype(np.float32) * 2.0 ** -20
+        B[(7 * c) % K, c] = 2.0 ** 20
+        A[:, (7 * c) % K] = 0.0
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    got = _auto_tc(cuda, monkeypatch, A, B, C0, la, lb, lc).astype(np.float64)
+    plain = run(cuda, A, B, C0, la, lb, lc, accuracy=FP16X3).astype(np.float64)
+    exact = A.astype(np.float64) @ B.astype(np.float64) + C0
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
+    tol = (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * scale
+    assert np.all(np.abs(got - exact) <= tol), np.max(np.abs(got - exact) / tol)
+    assert np.any(np.abs(plain - exact) > tol)  # the guard was needed
+    keep = np.ones((M, N), bool)
+    keep[bad_rows, :] = False
+    keep[:, bad_cols] = False
+    np.testing.assert_array_equal(got[keep], plain[keep])
+
+
+def test_auto_guard_inf_and_nan_rows(cuda, monkeypatch):
+    """Rows holding Inf or NaN are recomputed with FP32 FMAs: their outputs
+    are non-finite exactly where the FMA path's are; other rows stay finite
+    and within the bound."""
+    rng = np.random.default_rng(22)
+    M, N, K = 256, 256, 256
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    A[5, 9] = np.inf
+    A[200, 0] = np.nan
+    Z = np.zeros((M, N), np.float32)
+    got = _auto_tc(cuda, monkeypatch, A, B, Z)
+    fma = run(cuda, A, B, Z, 1, 1, 1, accuracy=0)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(fma))
+    np.testing.assert_array_equal(np.isinf(got), np.isinf(fma))
+    ok = np.ones(M, bool)
+    ok[[5, 200]] = False
+    exact = A[ok].astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A[ok]).astype(np.float64) @ np.abs(B).astype(np.float64)
+    assert np.all(np.abs(got[ok] - exact) <= (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * scale)
+
+
+@pytest.mark.parametrize("K", [16, 1024])
+def test_auto_guard_wide_range_operands(cuda, monkeypatch, K):
+    """s * m * 2^e operands (e in [-10, 10]: rows span up to 20 binades): at
+    K = 16 the FP16 split's span is 14 + 4 = 18 and most rows and columns are
+    recomputed with FP32 FMAs; at K = 1024 (span 24) none is and the result
+    is the plain FP16 split's.  Both within the bound."""
+    rng = np.random.default_rng(23 + K)
+    M = N = 320
+
+    def wide(shape):
+        return (rng.choice([-1.0, 1.0], shape) * rng.uniform(1, 2, shape) *
+                np.exp2(rng.integers(-10, 11, shape))).astype(np.float32)
+    A, B = wide((M, K)), wide((K, N))
+    Z = np.zeros((M, N), np.float32)
+    got = _auto_tc(cuda, monkeypatch, A, B, Z).astype(np.float64)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    assert np.all(np.abs(got - exact) <= (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * scale)
+    if K == 1024:
+        np.testing.assert_array_equal(got, run(cuda, A, B, Z, 1, 1, 1, accuracy=FP16X3))
 
 
 def test_auto_accuracy_small_uses_fp32_path(cuda):
