@@ -50,7 +50,8 @@ typedef enum gbblas_status {
   GBBLAS_STATUS_CUDA_ERROR = 4,      /* a CUDA runtime call or launch failed */
   GBBLAS_STATUS_TIMEOUT = 5,         /* a bounded device-side wait gave up */
   GBBLAS_STATUS_NOT_SUPPORTED = 6,   /* combination not provided (e.g. FP8 with double) */
-  GBBLAS_STATUS_NO_DEVICE = 7        /* no sm_103 device visible */
+  GBBLAS_STATUS_NO_DEVICE = 7,       /* no sm_103 device visible */
+  GBBLAS_STATUS_CANCELLED = 8        /* a served request was cancelled before it ran */
 } gbblas_status;
 
 typedef enum gbblas_layout {
@@ -445,6 +446,22 @@ gbblas_status gbblas_server_wait(gbblas_server s, uint64_t ticket, double* laten
 gbblas_status gbblas_server_run_trace(gbblas_server s, const gbblas_request* reqs, const double* arrival_s,
                                       int64_t n, double* latency_s);
 gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out);
+/* Cancel a request the server has not started: it leaves the queue and its
+ * wait returns GBBLAS_STATUS_CANCELLED.  A request already admitted to a
+ * round (its work may be on the GPU) or finished cannot be cancelled:
+ * GBBLAS_STATUS_NOT_SUPPORTED, and its wait reports how it ended. */
+gbblas_status gbblas_server_cancel(gbblas_server s, uint64_t ticket);
+
+/* Host-side failure injection, for testing how a caller (and the server)
+ * handle errors: nothing on the GPU is made to fail.  The next `count`
+ * events of `kind` fail as if the CUDA call behind them had failed; the
+ * server stays usable and later events succeed. */
+typedef enum gbblas_inject {
+  GBBLAS_INJECT_ALLOC = 0, /* gbblas_server_alloc returns GBBLAS_STATUS_ALLOC_FAILED */
+  GBBLAS_INJECT_LAUNCH = 1 /* a round's launch fails before enqueuing anything: its requests
+                              complete with GBBLAS_STATUS_CUDA_ERROR */
+} gbblas_inject;
+gbblas_status gbblas_server_inject(gbblas_server s, int32_t kind, int32_t count);
 gbblas_status gbblas_server_destroy(gbblas_server s);
 
 /* ------------------------------------------------ host-buffer entry points

@@ -631,6 +631,7 @@ const char* gbblas_status_string(gbblas_status s) {
     case GBBLAS_STATUS_TIMEOUT: return "GBBLAS_STATUS_TIMEOUT";
     case GBBLAS_STATUS_NOT_SUPPORTED: return "GBBLAS_STATUS_NOT_SUPPORTED";
     case GBBLAS_STATUS_NO_DEVICE: return "GBBLAS_STATUS_NO_DEVICE";
+    case GBBLAS_STATUS_CANCELLED: return "GBBLAS_STATUS_CANCELLED";
   }
   return "GBBLAS_STATUS_UNKNOWN";
 }

@@ -164,6 +164,8 @@ struct gbblas_server_s {
   std::thread scheduler;
   gbblas_server_stats stats{};
   int64_t round_reqs_total = 0;
+  // host-side failure injection (gbblas_server_inject): events left to fail
+  std::atomic<int> inject_alloc{0}, inject_launch{0};
 };
 
 namespace {
@@ -345,7 +347,13 @@ void scheduler_main(gbblas_server_s* s) {
         if (heavy) rd->max_ctas = std::max(1, s->ctx->num_sms * s->cfg.heavy_sm_percent / 100);
         cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
         lk.unlock();
-        gbblas_status e = launch_round(s, rd, st);
+        gbblas_status e;
+        if (s->inject_launch.load() > 0 && s->inject_launch.fetch_sub(1) > 0) {
+          set_error("server: injected launch failure");
+          e = GBBLAS_STATUS_CUDA_ERROR;
+        } else {
+          e = launch_round(s, rd, st);
+        }
         lk.lock();
         if (e != GBBLAS_STATUS_SUCCESS) {  // the host function never runs: finish here
           rd->status = e;
@@ -423,6 +431,10 @@ gbblas_status gbblas_server_alloc(gbblas_server s, int64_t bytes, void** ptr) {
     set_error("gbblas_server_alloc: bad arguments");
     return GBBLAS_STATUS_INVALID_VALUE;
   }
+  if (s->inject_alloc.load() > 0 && s->inject_alloc.fetch_sub(1) > 0) {
+    set_error("gbblas_server_alloc of %lld bytes failed: injected failure", (long long)bytes);
+    return GBBLAS_STATUS_ALLOC_FAILED;
+  }
   cudaError_t e = cudaMallocFromPoolAsync(ptr, (size_t)(bytes ? bytes : 1), s->pool, s->alloc_stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->alloc_stream);
   if (e != cudaSuccess) {
@@ -496,7 +508,9 @@ gbblas_status gbblas_server_wait(gbblas_server s, uint64_t ticket, double* laten
   Req* q = s->all[ticket].get();
   s->cv_done.wait(lk, [&] { return q->done; });
   if (latency_s) latency_s[0] = std::chrono::duration<double>(q->t_done - q->t_submit).count();
-  if (q->status != GBBLAS_STATUS_SUCCESS) set_error("gbblas_server: request %llu failed", (unsigned long long)ticket);
+  if (q->status != GBBLAS_STATUS_SUCCESS)
+    set_error("gbblas_server: request %llu %s", (unsigned long long)ticket,
+              q->status == GBBLAS_STATUS_CANCELLED ? "was cancelled" : "failed");
   return q->status;
 }
 
@@ -540,6 +554,46 @@ gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out)
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->stats;
   out->mean_round_size = s->stats.rounds ? (double)s->round_reqs_total / (double)s->stats.rounds : 0.0;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_cancel(gbblas_server s, uint64_t ticket) {
+  if (!s) {
+    set_error("gbblas_server_cancel: null server");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (ticket >= s->all.size()) {
+      set_error("gbblas_server_cancel: unknown ticket");
+      return GBBLAS_STATUS_INVALID_VALUE;
+    }
+    Req* q = s->all[ticket].get();
+    std::deque<Req*>& dq = q->heavy ? s->heavy_pending : s->pending;
+    auto it = std::find(dq.begin(), dq.end(), q);
+    if (it == dq.end()) {
+      set_error("gbblas_server_cancel: request %llu already %s", (unsigned long long)ticket,
+                q->done ? "finished" : "running");
+      return GBBLAS_STATUS_NOT_SUPPORTED;
+    }
+    dq.erase(it);
+    q->status = GBBLAS_STATUS_CANCELLED;
+    q->t_done = Clock::now();
+    q->done = true;
+    // a queue head that waited for memory may have been this one
+    s->budget_blocked = false;
+  }
+  s->cv_done.notify_all();
+  s->cv.notify_one();
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_inject(gbblas_server s, int32_t kind, int32_t count) {
+  if (!s || count < 0 || (kind != GBBLAS_INJECT_ALLOC && kind != GBBLAS_INJECT_LAUNCH)) {
+    set_error("gbblas_server_inject: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  (kind == GBBLAS_INJECT_ALLOC ? s->inject_alloc : s->inject_launch).store(count);
   return GBBLAS_STATUS_SUCCESS;
 }
 

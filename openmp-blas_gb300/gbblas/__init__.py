@@ -30,7 +30,7 @@ ACCURACY_FP16X3 = 8        # float GEMM: scaled FP16 hi + lo, three tcgen05 prod
 
 STATUS = {
     0: "SUCCESS", 1: "INVALID_VALUE", 2: "SHAPE_MISMATCH", 3: "ALLOC_FAILED",
-    4: "CUDA_ERROR", 5: "TIMEOUT", 6: "NOT_SUPPORTED", 7: "NO_DEVICE",
+    4: "CUDA_ERROR", 5: "TIMEOUT", 6: "NOT_SUPPORTED", 7: "NO_DEVICE", 8: "CANCELLED",
 }
 
 LIB_PATH = _build.LIB
@@ -76,6 +76,8 @@ SIGNATURES = {
     "gbblas_server_run_trace": (_int, [_vp, _vp, _vp, _i64, _vp]),
     "gbblas_server_get_stats": (_int, [_vp, _vp]),
     "gbblas_server_destroy": (_int, [_vp]),
+    "gbblas_server_cancel": (_int, [_vp, ctypes.c_uint64]),
+    "gbblas_server_inject": (_int, [_vp, ctypes.c_int32, ctypes.c_int32]),
     "gbblas_sgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
     "gbblas_dgemm_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]),
     "gbblas_dgemm_ex_host": (_int, [_i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int]),
@@ -103,6 +105,9 @@ SIGNATURES = {
     "gbblas_dew_host": (_int, [_int, _i64, _vp, _vp, _vp]),
     "gbblas_seeded_fill": (_int, [ctypes.c_uint64, ctypes.c_int32, _i64, _vp, _vp, _vp]),
 }
+
+INJECT_ALLOC = 0   # gbblas_server_inject: pool allocations fail
+INJECT_LAUNCH = 1  # gbblas_server_inject: round launches fail
 
 FILL_UNIFORM = 0  # U[-1, 1)
 FILL_WIDE = 1     # s * m * 2^e, m in [1, 2), e in [-10, 10]
@@ -348,6 +353,19 @@ class Server:
         lat = np.zeros(max(1, n), np.float64)
         call("gbblas_server_run_trace", self.handle, ctypes.addressof(arr), t.ctypes.data, n, lat.ctypes.data)
         return lat[:n]
+
+    def cancel(self, ticket: int) -> int:
+        """gbblas_server_cancel: the raw status (0, or NOT_SUPPORTED when the
+        request already runs or ran)."""
+        return status_of("gbblas_server_cancel", self.handle, ticket)
+
+    def wait_status(self, ticket: int) -> int:
+        """gbblas_server_wait, returning the request's status instead of raising."""
+        lat = ctypes.c_double()
+        return status_of("gbblas_server_wait", self.handle, ticket, ctypes.byref(lat))
+
+    def inject(self, kind: int, count: int) -> None:
+        call("gbblas_server_inject", self.handle, kind, count)
 
     def stats(self) -> dict:
         st = ServerStats()

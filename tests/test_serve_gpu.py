@@ -192,3 +192,118 @@ def test_server_f64_gemm_on_tensor_core_digits(cuda):
         c.check(a)
         assert torch.equal(a, c.outs[-1]), f"alone != mix for {c.kind} {c.dims}"
     srv.close()
+
+
+# ---------------------------------------------------------------- failure handling
+# Every failure below is made on the host (an injected allocation or launch
+# failure, a malformed request, a cancellation, an exhausted budget); nothing
+# on the GPU faults.  Each must come back as a status, and the same server
+# must then serve correct results.
+
+def _healthy(torch, srv, rng):
+    """The server still serves: a small GEMM and a dot, checked."""
+    import gbblas
+    cases = [ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 1, (96, 80, 64), accuracy=FP32),
+             ReqCase(torch, rng, gbblas.OP_DOT, gbblas.F64, 1, (5000,))]
+    lat = srv.run_trace([c.request() for c in cases], np.zeros(len(cases)))
+    assert np.all(lat > 0)
+    for c in cases:
+        c.check(c.outs[-1])
+
+
+def test_server_injected_alloc_failure(cuda):
+    import gbblas
+    torch = cuda
+    srv = gbblas.Server(streams=2)
+    srv.inject(gbblas.INJECT_ALLOC, 2)
+    for _ in range(2):
+        with pytest.raises(gbblas.GbblasError) as e:
+            srv.alloc(1 << 20)
+        assert e.value.status == 3  # GBBLAS_STATUS_ALLOC_FAILED
+    p = srv.alloc(1 << 20)  # the injection is used up
+    srv.free(p)
+    _healthy(torch, srv, np.random.default_rng(31))
+    srv.close()
+
+
+def test_server_injected_launch_failure(cuda):
+    """A round whose launch fails reports CUDA_ERROR for its requests; the
+    next rounds run normally."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(32)
+    srv = gbblas.Server(streams=1, max_group=1)
+    srv.inject(gbblas.INJECT_LAUNCH, 1)
+    bad = ReqCase(torch, rng, gbblas.OP_DOT, gbblas.F32, 1, (1000,))
+    t = srv.submit(bad.request())
+    assert srv.wait_status(t) == 4  # GBBLAS_STATUS_CUDA_ERROR
+    assert bad.outs[-1].item() == 0.0  # nothing ran
+    _healthy(torch, srv, rng)
+    srv.close()
+
+
+@pytest.mark.parametrize("field,value", [("op", 9), ("dtype", 2), ("layout", 5), ("accuracy", 42), ("M", -1),
+                                         ("A", None)])
+def test_server_malformed_request(cuda, field, value):
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(33)
+    srv = gbblas.Server(streams=2)
+    req = ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (64, 64)).request()
+    setattr(req, field, value)
+    with pytest.raises(gbblas.GbblasError) as e:
+        srv.submit(req)
+    assert e.value.status == 1  # GBBLAS_STATUS_INVALID_VALUE
+    assert srv.stats()["submitted"] == 0
+    _healthy(torch, srv, rng)
+    srv.close()
+
+
+def test_server_cancel(cuda):
+    """Requests held back by the budget can be cancelled: their waits return
+    CANCELLED and their outputs stay untouched; a request that already ran
+    cannot be; the rest complete correctly."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(34)
+    # each 1536 x 1536 f32 GEMV holds ~9.4 MiB: with a 10 MiB budget one runs at a time
+    srv = gbblas.Server(streams=1, max_group=1, budget_bytes=10 << 20)
+    cases = [ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (1536, 1536)) for _ in range(40)]
+    tickets = [srv.submit(c.request()) for c in cases]
+    # from the back of the queue, which the scheduler reaches last
+    cancelled = [t for t in reversed(tickets[10:]) if srv.cancel(t) == 0]
+    assert len(cancelled) >= 20
+    for c, t in zip(cases, tickets):
+        st = srv.wait_status(t)
+        if t in cancelled:
+            assert st == 8  # GBBLAS_STATUS_CANCELLED
+            assert torch.count_nonzero(c.outs[-1]).item() == 0
+        else:
+            assert st == 0
+            c.check(c.outs[-1])
+    assert srv.cancel(tickets[0]) == 6  # finished: GBBLAS_STATUS_NOT_SUPPORTED
+    assert srv.cancel(10 ** 9) == 1  # unknown ticket
+    _healthy(torch, srv, rng)
+    srv.close()
+
+
+def test_server_budget_exhaustion_recovers(cuda):
+    """Far more work than the budget holds at once is admitted piece by piece
+    as memory frees up; an oversize request is refused and counted; then the
+    server serves normally."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(35)
+    srv = gbblas.Server(streams=4, max_group=4, budget_bytes=20 << 20)
+    cases = [ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (1536, 1536)) for _ in range(30)]
+    lat = srv.run_trace([c.request() for c in cases], np.zeros(len(cases)))
+    assert np.all(lat > 0)
+    for c in cases:
+        c.check(c.outs[-1])
+    big = ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (4096, 4096))
+    with pytest.raises(gbblas.GbblasError):
+        srv.submit(big.request())
+    st = srv.stats()
+    assert st["rejected"] == 1 and st["peak_inflight_bytes"] <= 20 << 20
+    _healthy(torch, srv, rng)
+    srv.close()
