@@ -73,6 +73,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -287,19 +288,34 @@ __device__ __forceinline__ void f16_scale_tile_rows(const unsigned (&mx)[16], co
   }
 }
 
-// For every arena row R: e[R] = the frexp exponent of the row's largest
-// magnitude, and (emin non-null, for the AUTO guard) emin[R] = the
-// magnitude bits of its smallest nonzero element.  Same tiles as the
-// preparation; magnitudes compared as bit patterns; the rows' extremes of a
-// tile combined in shared memory, then atomicMax-ed into e (which starts
-// filled with the byte 0x80: a row no tile wrote, all zero or padding, reads
-// as 0) and atomicMin-ed into emin (which starts at 0xFFFFFFFF).
-__global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restrict__ jobs, int njobs,
-                                                        int* __restrict__ e_out, unsigned* __restrict__ emin_out) {
+// Row exponents are stored biased so that zero (what the launch's one
+// memset writes) means "no nonzero element seen": e[R] = kExpBias + the
+// frexp exponent of the row's largest magnitude, emin[R] = ~(magnitude bits
+// of its smallest nonzero element), both combined with atomicMax.
+constexpr int kExpBias = 1024;
+
+// One operand's side of a two-operand preparation launch (A's CTAs first,
+// then B^T's).
+struct ScaleSide {
+  const SplitJob* jobs;
+  int tiles;
+  int* e_out;
+  unsigned* emin_out;  // null: no guard
+};
+
+// For every arena row R of both operands: e[R] (the row's largest
+// magnitude) and, for the AUTO guard, emin[R] (its smallest nonzero one).
+// Same tiles as the preparation; magnitudes compared as bit patterns; the
+// rows' extremes of a tile combined in shared memory, then atomicMax-ed
+// into the encodings above.
+__global__ void __launch_bounds__(256) f16_scale_kernel(ScaleSide side_a, ScaleSide side_b, int njobs) {
   constexpr int TK = 64, TR = 64;
   __shared__ unsigned int rmax[TR], rmin[TR];
   __shared__ int sjob;
-  const int t = blockIdx.x, tid = threadIdx.x;
+  const bool on_b = (int)blockIdx.x >= side_a.tiles;
+  const ScaleSide sd = on_b ? side_b : side_a;
+  const SplitJob* __restrict__ jobs = sd.jobs;
+  const int t = (int)blockIdx.x - (on_b ? side_a.tiles : 0), tid = threadIdx.x;
   if (tid == 0) {
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
@@ -389,9 +405,9 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(const SplitJob* __restri
     if (rmax[tid] != 0u) {
       int e;
       (void)frexpf(__uint_as_float(rmax[tid] >= 0x7F800000u ? 0x7F7FFFFFu : rmax[tid]), &e);  // Inf / NaN: the top exponent
-      atomicMax(e_out + j.dst_row + r0 + tid, e);
+      atomicMax(sd.e_out + j.dst_row + r0 + tid, e + kExpBias);
     }
-    if (emin_out && rmin[tid] != 0xFFFFFFFFu) atomicMin(emin_out + j.dst_row + r0 + tid, rmin[tid]);
+    if (sd.emin_out && rmin[tid] != 0xFFFFFFFFu) atomicMax(sd.emin_out + j.dst_row + r0 + tid, ~rmin[tid]);
   }
 }
 
@@ -404,7 +420,7 @@ __device__ __forceinline__ float scale_pow2(float x, int n) {
 
 __device__ __forceinline__ int f16_row_exp(const int* e, int64_t row) {
   const int v = e[row];
-  return v == (int)0x80808080 ? 0 : v;
+  return v == 0 ? 0 : v - kExpBias;  // all-zero (or padding) rows: scale 2^15
 }
 
 // The guard of the FP16 split under GBBLAS_ACCURACY_AUTO, per operand.  An
@@ -419,7 +435,7 @@ __device__ __forceinline__ int f16_row_exp(const int* e, int64_t row) {
 // span": flags[R] = 1 and R goes onto `list`; the GEMM leaves their outputs
 // alone and f16_guard_fixup_kernel computes them with FP32 FMAs.
 struct F16Guard {
-  const unsigned* emin = nullptr;  // smallest nonzero magnitude bits per arena row (f16_scale_kernel)
+  const unsigned* emin = nullptr;  // ~(smallest nonzero magnitude bits) per arena row (f16_scale_kernel)
   int* flags = nullptr;            // per arena row: 1 = out of span (every row written)
   int* list = nullptr;             // out-of-span arena rows, in no particular order
   int* count = nullptr;            // entries in list
@@ -431,16 +447,32 @@ __device__ __forceinline__ int biased_log2(unsigned bits) {
   return bits >= 0x00800000u ? (int)(bits >> 23) : 9 - __clz(bits);
 }
 
+// One operand's side of a two-operand preparation launch (A's CTAs first,
+// then B^T's): its jobs, tiles, arena, piece stride, scales and guard.
+struct PrepSide {
+  const SplitJob* jobs;
+  int tiles;
+  void* out;
+  int64_t piece_stride;
+  uint32_t* scales;
+  F16Guard guard;
+};
+
 template <int MODE>
-__global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restrict__ jobs, int njobs,
-                                                         void* __restrict__ out, int64_t piece_stride, int64_t pitch,
-                                                         uint32_t* __restrict__ scales, int64_t scale_stride,
-                                                         F16Guard guard) {
+__global__ void __launch_bounds__(256) prep_group_kernel(PrepSide side_a, PrepSide side_b, int njobs, int64_t pitch,
+                                                         int64_t scale_stride) {
   using PT = PrepTile<MODE>;
   constexpr int TK = PT::TK, TR = PT::TR, LD = PT::LD;
   __shared__ __align__(16) float tile[TR * LD];
   __shared__ int sjob;
-  const int t = blockIdx.x;
+  const bool on_b = (int)blockIdx.x >= side_a.tiles;
+  const PrepSide sd = on_b ? side_b : side_a;
+  const SplitJob* __restrict__ jobs = sd.jobs;
+  void* __restrict__ out = sd.out;
+  const int64_t piece_stride = sd.piece_stride;
+  uint32_t* __restrict__ scales = sd.scales;
+  const F16Guard& guard = sd.guard;
+  const int t = (int)blockIdx.x - (on_b ? side_a.tiles : 0);
   const int tid = threadIdx.x;
   if (tid == 0) {  // job = last with tile_start <= t
     int lo = 0, hi = njobs - 1;
@@ -530,7 +562,7 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const SplitJob* __restr
       int out_of_span = 0;
       if (r0 + tid < j.rows) {
         const int e = f16_row_exp(erow, row);  // floor(log2 max) + 1; 128 for Inf / NaN (or >= 2^127)
-        const unsigned mn = guard.emin[row];
+        const unsigned mn = ~guard.emin[row];  // 0xFFFFFFFF: no nonzero element
         const int span_max = 14 + (63 - __clzll((unsigned long long)(j.K > 0 ? j.K : 1)));  // 14 + floor(log2 K)
         out_of_span = e >= 128 || (mn != 0xFFFFFFFFu && (e - 1) - (biased_log2(mn) - 127) > span_max);
       }
@@ -1316,6 +1348,8 @@ struct TcGroupPlan {
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool guard = false;  // FP16 split with the AUTO guard (F16Guard, f16_guard_fixup_kernel)
   size_t off_gmin = 0, off_gflag = 0, off_glist = 0;  // guard arrays: A rows then B rows each
+  size_t off_init_end = 0;  // the launch clears [kTileCounterOffset, off_init_end)
+  std::vector<char> tables;  // host image of [off_probs, off_arena), copied with one memcpy
   bool fp8() const { return mode == kModeFp8; }
   bool f16() const { return mode == kModeF16; }
   int planes() const { return fp8() ? 1 : (f16() ? 2 : mode); }
@@ -1434,19 +1468,33 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     return GBBLAS_STATUS_NOT_SUPPORTED;
   }
   const size_t esize = pl.fp8() ? 1 : sizeof(__nv_bfloat16);
-  pl.off_probs = kScratchZeroBytes;
+  const size_t guard_rows = pl.guard ? (size_t)(pl.a_rows + pl.b_rows) : 0;
+  // FP16 split: the row exponents (and the guard's minima) right after the
+  // zeroed header, so that one memset from the tile counter on clears them
+  size_t off = kScratchZeroBytes;
+  if (pl.f16()) {
+    pl.off_sa = off;
+    off += align256((size_t)pl.a_rows * sizeof(int));
+    pl.off_sb = off;
+    off += align256((size_t)pl.b_rows * sizeof(int));
+    pl.off_gmin = off;
+    off += align256(guard_rows * sizeof(unsigned));
+  }
+  pl.off_init_end = off;
+  pl.off_probs = off;
   pl.off_jobs = pl.off_probs + align256(sizeof(TcProblem) * pl.nprob);
   pl.off_red = pl.off_jobs + align256(sizeof(SplitJob) * 2 * pl.njobs);
   pl.off_arena = pl.off_red + align256(sizeof(SplitReduce) * pl.reds.size());
   const size_t a_plane = (size_t)(pl.a_rows * pl.pitch), b_plane = (size_t)(pl.b_rows * pl.pitch);
-  pl.off_sa = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
-  // FP8: one 4-byte scale word per row and K-block; FP16 split: one
-  // 4-byte power-of-two exponent per row
-  const size_t kb = pl.fp8() ? (size_t)(pl.kpad / 128) : (pl.f16() ? 1 : 0);
-  pl.off_sb = pl.off_sa + align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
-  const size_t guard_rows = pl.guard ? (size_t)(pl.a_rows + pl.b_rows) : 0;
-  pl.off_gmin = pl.off_sb + align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
-  pl.off_gflag = pl.off_gmin + align256(guard_rows * sizeof(uint32_t));
+  off = pl.off_arena + align256((size_t)pl.planes() * (a_plane + b_plane) * esize);
+  if (pl.fp8()) {  // FP8: one 4-byte scale word per row and K-block
+    const size_t kb = (size_t)(pl.kpad / 128);
+    pl.off_sa = off;
+    off += align256(kb * (size_t)pl.a_rows * sizeof(uint32_t));
+    pl.off_sb = off;
+    off += align256(kb * (size_t)pl.b_rows * sizeof(uint32_t));
+  }
+  pl.off_gflag = off;
   pl.off_glist = pl.off_gflag + align256(guard_rows * sizeof(int));
   pl.off_ws = pl.off_glist + align256(guard_rows * sizeof(int));
   pl.bytes = pl.off_ws + align256((size_t)ws);
@@ -1470,16 +1518,17 @@ gbblas_status bind_group(TcGroupPlan& pl, char* base, cudaStream_t stream) {
     if (pl.part_off[i] >= 0) pl.probs[i].C = reinterpret_cast<float*>(base + pl.off_ws + pl.part_off[i]);
   for (size_t r = 0; r < pl.reds.size(); ++r)
     pl.reds[r].part = reinterpret_cast<const float*>(base + pl.off_ws + pl.red_off[r]);
-  // (the host tables must outlive these copies: they live in the plan)
-  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_probs, pl.probs.data(), sizeof(TcProblem) * pl.nprob,
-                              cudaMemcpyHostToDevice, stream));
-  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs, pl.ajobs.data(), sizeof(SplitJob) * pl.njobs,
-                              cudaMemcpyHostToDevice, stream));
-  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_jobs + sizeof(SplitJob) * pl.njobs, pl.bjobs.data(),
-                              sizeof(SplitJob) * pl.njobs, cudaMemcpyHostToDevice, stream));
+  // problems, jobs and reductions as one host image and one copy (the image
+  // lives in the plan, which outlives the copy)
+  pl.tables.assign(pl.off_arena - pl.off_probs, 0);
+  char* h = pl.tables.data();
+  std::memcpy(h, pl.probs.data(), sizeof(TcProblem) * pl.nprob);
+  std::memcpy(h + (pl.off_jobs - pl.off_probs), pl.ajobs.data(), sizeof(SplitJob) * pl.njobs);
+  std::memcpy(h + (pl.off_jobs - pl.off_probs) + sizeof(SplitJob) * pl.njobs, pl.bjobs.data(),
+              sizeof(SplitJob) * pl.njobs);
   if (!pl.reds.empty())
-    GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_red, pl.reds.data(), sizeof(SplitReduce) * pl.reds.size(),
-                                cudaMemcpyHostToDevice, stream));
+    std::memcpy(h + (pl.off_red - pl.off_probs), pl.reds.data(), sizeof(SplitReduce) * pl.reds.size());
+  GB_CUDA_TRY(cudaMemcpyAsync(base + pl.off_probs, h, pl.tables.size(), cudaMemcpyHostToDevice, stream));
   GB_TRY(make_map(&pl.map_a, arena_a(pl), (uint64_t)pl.a_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(), kBM,
                   pl.fp8(), pl.row_bytes()));
   GB_TRY(make_map(&pl.map_b, arena_b(pl), (uint64_t)pl.b_rows, (uint64_t)pl.pitch, (uint64_t)pl.planes(),
@@ -1569,40 +1618,34 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
 template <int MODE>
 gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
-  int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
-  GB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+  // the tile counter, the guard's counts and (FP16 split) the row exponents
+  // and minima: zero, in one memset
+  GB_CUDA_TRY(cudaMemsetAsync(pl.base + kTileCounterOffset, 0, pl.off_init_end - kTileCounterOffset, stream));
   F16Guard ga, gb;  // AUTO guard arrays (A rows, then B^T rows)
   int* gcounts = reinterpret_cast<int*>(pl.base + kGuardCountOffset);
-  if constexpr (MODE == kModeF16) {
-    if (pl.guard) {
-      unsigned* gmin = reinterpret_cast<unsigned*>(pl.base + pl.off_gmin);
-      int* gflag = reinterpret_cast<int*>(pl.base + pl.off_gflag);
-      int* glist = reinterpret_cast<int*>(pl.base + pl.off_glist);
-      ga = F16Guard{gmin, gflag, glist, gcounts};
-      gb = F16Guard{gmin + pl.a_rows, gflag + pl.a_rows, glist + pl.a_rows, gcounts + 1};
-      GB_CUDA_TRY(cudaMemsetAsync(gmin, 0xFF, sizeof(unsigned) * (size_t)(pl.a_rows + pl.b_rows), stream));
-      GB_CUDA_TRY(cudaMemsetAsync(gcounts, 0, 2 * sizeof(int), stream));
-    }
-    // per-row exponents of A's and B^T's arena rows (and the guard's minima), then the pieces
-    GB_CUDA_TRY(cudaMemsetAsync(scales_a(pl), 0x80, sizeof(int) * (size_t)pl.a_rows, stream));
-    GB_CUDA_TRY(cudaMemsetAsync(scales_b(pl), 0x80, sizeof(int) * (size_t)pl.b_rows, stream));
-    f16_scale_kernel<<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, reinterpret_cast<int*>(scales_a(pl)),
-                                                     const_cast<unsigned*>(ga.emin));
-    GB_TRY(check_launch("f16_scale_kernel(A)"));
-    f16_scale_kernel<<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, reinterpret_cast<int*>(scales_b(pl)),
-                                                     const_cast<unsigned*>(gb.emin));
-    GB_TRY(check_launch("f16_scale_kernel(B)"));
+  if (pl.guard) {
+    unsigned* gmin = reinterpret_cast<unsigned*>(pl.base + pl.off_gmin);
+    int* gflag = reinterpret_cast<int*>(pl.base + pl.off_gflag);
+    int* glist = reinterpret_cast<int*>(pl.base + pl.off_glist);
+    ga = F16Guard{gmin, gflag, glist, gcounts};
+    gb = F16Guard{gmin + pl.a_rows, gflag + pl.a_rows, glist + pl.a_rows, gcounts + 1};
   }
-  // FP8 scale words: 128 per K-block of each 128-row block, i.e. `kpad` per row block
-  prep_group_kernel<MODE><<<pl.a_tiles, 256, 0, stream>>>(djobs, pl.njobs, arena_a(pl),
-                                                          (int64_t)(pl.a_rows * pl.pitch), pl.pitch, scales_a(pl),
-                                                          pl.kpad, ga);
-  GB_TRY(check_launch("prep_group_kernel(A)"));
-  prep_group_kernel<MODE><<<pl.b_tiles, 256, 0, stream>>>(djobs + pl.njobs, pl.njobs, arena_b(pl),
-                                                          (int64_t)(pl.b_rows * pl.pitch), pl.pitch, scales_b(pl),
-                                                          pl.kpad, gb);
-  GB_TRY(check_launch("prep_group_kernel(B)"));
+  const int prep_ctas = pl.a_tiles + pl.b_tiles;
+  if constexpr (MODE == kModeF16) {
+    // per-row exponents of A's and B^T's arena rows (and the guard's minima)
+    const ScaleSide sa{djobs, pl.a_tiles, reinterpret_cast<int*>(scales_a(pl)), const_cast<unsigned*>(ga.emin)};
+    const ScaleSide sb{djobs + pl.njobs, pl.b_tiles, reinterpret_cast<int*>(scales_b(pl)),
+                       const_cast<unsigned*>(gb.emin)};
+    f16_scale_kernel<<<prep_ctas, 256, 0, stream>>>(sa, sb, pl.njobs);
+    GB_TRY(check_launch("f16_scale_kernel"));
+  }
+  // the pieces (FP8: values and scale words, 128 per K-block of each 128-row
+  // block, i.e. `kpad` per row block) of both operands
+  const PrepSide pa{djobs, pl.a_tiles, arena_a(pl), (int64_t)(pl.a_rows * pl.pitch), scales_a(pl), ga};
+  const PrepSide pb{djobs + pl.njobs, pl.b_tiles, arena_b(pl), (int64_t)(pl.b_rows * pl.pitch), scales_b(pl), gb};
+  prep_group_kernel<MODE><<<prep_ctas, 256, 0, stream>>>(pa, pb, pl.njobs, pl.pitch, pl.kpad);
+  GB_TRY(check_launch("prep_group_kernel"));
   gbblas_status st;
   if constexpr (MODE != kModeFp8 && MODE != kModeF16) {
     st = pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
