@@ -351,8 +351,8 @@ gbblas_status gbblas_batch_create(const gbblas_gemm_desc* gemms, int64_t ngemm, 
     if (accuracy == GBBLAS_ACCURACY_FP32) {
       b->fma_gemms.assign(gemms, gemms + ngemm);
     } else {
-      // AUTO in a batch: the FP32-accurate six-product split
-      const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode(accuracy);
+      // AUTO in a batch: the FP32-accurate split-FP16 GEMM with its guard
+      const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? kTcModeF16Guard : tc_mode(accuracy);
       if ((st = tc_group_create(c, mode, gemms, ngemm, &b->gemm)) != GBBLAS_STATUS_SUCCESS) return fail(st);
     }
   }

@@ -768,8 +768,8 @@ gbblas_status gbblas_sgemm_grouped(const gbblas_gemm_desc* descs, int64_t count,
     }
     return GBBLAS_STATUS_SUCCESS;
   }
-  // AUTO in a group: the six-product split (FP32-accurate on the tensor cores)
-  const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode(accuracy);
+  // AUTO in a group: the split-FP16 GEMM with its guard (FP32-accurate on the tensor cores)
+  const int mode = accuracy == GBBLAS_ACCURACY_AUTO ? kTcModeF16Guard : tc_mode(accuracy);
   return launch_gemm_tc_group(c, mode, descs, count, s);
 }
 

@@ -5,7 +5,7 @@
 //   scheduler  one native thread: admits pending requests in arrival order
 //              while their working set fits the HBM budget and one of the
 //              `streams` slots is free, coalesces the admitted ones into a
-//              round - split-BF16 GEMMs in one grouped tensor-core launch,
+//              round - tensor-core GEMMs in one grouped launch per mode,
 //              float GEMVs in one grouped launch, FP64 / FMA GEMMs and dots
 //              as their own kernels - and enqueues the round on a free
 //              stream followed by a host function;
@@ -21,6 +21,7 @@
 #include <deque>
 #include <memory>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -59,9 +60,9 @@ struct Round {
 int64_t round_up64(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
 // Tensor-core mode of an FP32 GEMM request that does not ask for the FMA
-// path (AUTO: the FP32-accurate six-product split).
+// path (AUTO: the FP32-accurate split-FP16 GEMM with its guard).
 int server_mode(int32_t acc) {
-  return acc == GBBLAS_ACCURACY_AUTO ? tc_mode(GBBLAS_ACCURACY_BF16X6) : tc_mode((gbblas_accuracy)acc);
+  return acc == GBBLAS_ACCURACY_AUTO ? kTcModeF16Guard : tc_mode((gbblas_accuracy)acc);
 }
 
 // Tensor-core digits of a double GEMM request (0: the FP64 pipes): FP64 means
@@ -100,8 +101,8 @@ int64_t working_set(const gbblas_request& r, int f64_digits, bool f64_guarded) {
 }
 
 // Estimated GPU time (us) of a request from its flops / bytes and the rate of
-// the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, FP8
-// ~600, FP32 FMA ~55, FP64 pipes ~1.2 TFLOP/s, FP64 as tensor-core digits
+// the path it takes on a GB300 (split-BF16 GEMM ~260 / ~430 TFLOP/s, split-FP16
+// ~400, FP8 ~600, FP32 FMA ~55, FP64 pipes ~1.2 TFLOP/s, FP64 as tensor-core digits
 // ~38 TFLOP/s after ~50 us of operand preparation and launches; streaming
 // ~6 TB/s; FP64 GEMV ~1.1 TFLOP/s).
 double estimate_us(const gbblas_request& r, int f64_digits) {
@@ -119,8 +120,10 @@ double estimate_us(const gbblas_request& r, int f64_digits) {
         rate = 430e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP8)
         rate = 600e6;
-      else
+      else if (r.accuracy == GBBLAS_ACCURACY_BF16X6)
         rate = 260e6;
+      else  // split-FP16, AUTO's guarded split-FP16
+        rate = 400e6;
       return launch + fl / rate;
     }
     case GBBLAS_OP_MTV:
@@ -186,7 +189,8 @@ void CUDART_CB on_round_done(void* p) {
 gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
   DeviceCtx* c = s->ctx;
   const int cap = rd->max_ctas;
-  std::vector<gbblas_gemm_desc> split3, split2, fp8;
+  // tensor-core GEMMs of the round, one grouped launch per mode
+  std::vector<std::pair<int, std::vector<gbblas_gemm_desc>>> groups;
   std::vector<gbblas_gemv_desc> gemv;
   gbblas_status first_err = GBBLAS_STATUS_SUCCESS;
   auto note = [&](gbblas_status e) {
@@ -214,7 +218,9 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
         gbblas_gemm_desc d{r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa, static_cast<const float*>(r.B),
                            rsb, csb, static_cast<float*>(r.C), rsc, csc};
         const int mode = server_mode(r.accuracy);
-        (mode == 2 ? split2 : mode == 3 ? split3 : fp8).push_back(d);
+        auto g = std::find_if(groups.begin(), groups.end(), [&](const auto& x) { return x.first == mode; });
+        if (g == groups.end()) g = groups.insert(groups.end(), {mode, {}});
+        g->second.push_back(d);
       }
     } else if (r.op == GBBLAS_OP_MTV || r.op == GBBLAS_OP_VTM) {
       const bool tr = r.op == GBBLAS_OP_VTM;
@@ -242,10 +248,7 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
                                static_cast<float*>(r.C), st));
     }
   }
-  if (!split3.empty()) note(launch_gemm_tc_group(c, 3, split3.data(), (int64_t)split3.size(), st, cap));
-  if (!split2.empty()) note(launch_gemm_tc_group(c, 2, split2.data(), (int64_t)split2.size(), st, cap));
-  if (!fp8.empty())
-    note(launch_gemm_tc_group(c, tc_mode(GBBLAS_ACCURACY_FP8), fp8.data(), (int64_t)fp8.size(), st, cap));
+  for (const auto& g : groups) note(launch_gemm_tc_group(c, g.first, g.second.data(), (int64_t)g.second.size(), st, cap));
   // fixed rows-per-item: no autotuning (timing) inside the serving loop
   if (!gemv.empty()) note(launch_gemv_group_rows_fixed(c, gemv.data(), (int64_t)gemv.size(), st, 4));
   rd->status = first_err;

@@ -14,12 +14,19 @@ PKG = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 
 
 pytestmark = pytest.mark.gpu
 
-BF16X3, BF16X6 = 1, 4
+BF16X3, AUTO, BF16X6, FP16X3 = 1, 3, 4, 8
 
 
 def split_tol(absA, absB, K, mode):
     if mode == BF16X6:
         return (2.0 ** -21 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
+    if mode == AUTO:  # the guarded FP16 split
+        return (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
+    if mode == FP16X3:  # rows / columns scaled into FP16's range; subnormal low pieces
+        sa = np.ldexp(1.0, np.frexp(absA.max(axis=1))[1])
+        sb = np.ldexp(1.0, np.frexp(absB.max(axis=0))[1])
+        return ((2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB) +
+                2.0 ** -38 * max(K, 1) * np.outer(sa, sb))
     return (2.0 ** -14 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
 
 
@@ -43,7 +50,7 @@ SHAPES = [(1, 1, 1), (7, 300, 5), (128, 128, 64), (129, 257, 65), (300, 100, 100
           (1000, 33, 517), (512, 512, 512), (40, 800, 1600), (256, 384, 128)]
 
 
-@pytest.mark.parametrize("mode", [BF16X3, BF16X6])
+@pytest.mark.parametrize("mode", [BF16X3, BF16X6, FP16X3, AUTO])
 def test_gemm_grouped_vs_fp64(cuda, mode):
     import gbblas
     rng = np.random.default_rng(1)
@@ -179,3 +186,40 @@ def test_autotune_cache_written(cuda, tmp_path):
     assert r.returncode == 0, r.stderr
     text = cache.read_text()
     assert "gemv_group_rows|" in text
+
+
+def test_gemm_grouped_auto_guard_across_problems(cuda):
+    """AUTO in a group: out-of-span rows and columns (one entry of 2^20 among
+    entries of 2^-20, meeting zeros on the other side) in some problems of the
+    group are recomputed with FP32 FMAs - the fixup finds each listed row's
+    problem - and every problem meets (2^-19 + 2 K eps32)(|A||B|)."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(7)
+    shapes = [(300, 260, 512), (64, 128, 64), (129, 257, 1000), (500, 40, 300)]
+    descs, host = [], []
+    for i, (M, N, K) in enumerate(shapes):
+        A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+        B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+        if i in (0, 2):  # a few out-of-span rows of A
+            for r in (1, M // 2, M - 1):
+                A[r] = rng.uniform(-1, 1, K).astype(np.float32) * 2.0 ** -20
+                A[r, r % K] = 2.0 ** 20
+                B[r % K, :] = 0.0
+        if i in (2, 3):  # and columns of B
+            for c in (0, N - 1):
+                B[:, c] = rng.uniform(-1, 1, K).astype(np.float32) * 2.0 ** -20
+                B[(3 * c + 5) % K, c] = 2.0 ** 20
+                A[:, (3 * c + 5) % K] = 0.0
+        C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+        tA, tB, tC = (torch.from_numpy(x.copy()).cuda() for x in (A, B, C0))
+        descs.append(gbblas.gemm_desc(tA, tB, tC))
+        host.append((A, B, C0, tA, tB, tC))
+    gbblas.gemm_grouped(descs, accuracy=AUTO)
+    gbblas.call("gbblas_check_stream", None)
+    for (A, B, C0, _, _, tC), (M, N, K) in zip(host, shapes):
+        got = tC.cpu().numpy().astype(np.float64)
+        exact = A.astype(np.float64) @ B.astype(np.float64) + C0
+        tol = split_tol(np.abs(A).astype(np.float64), np.abs(B).astype(np.float64), K, AUTO) + \
+            2 * np.finfo(np.float32).eps * np.abs(C0)
+        assert np.all(np.abs(got - exact) <= tol), (M, N, K, float(np.max(np.abs(got - exact) / tol)))
