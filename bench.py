@@ -975,6 +975,9 @@ def batching_report(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
     t_gemm_roof = gemm_flops * products / (peaks["bf16_tflops"] * 1e12)
     t_gemv_roof = gemv_bytes / (peaks["hbm_gbs"] * 1e9)
+    # the GEMMs' HBM floor: A and B read once in FP32, C read and written (C += A B)
+    gemm_bytes = float(((g[:, 0] * g[:, 2] + g[:, 2] * g[:, 1]) * 4 + 2 * g[:, 0] * g[:, 1] * 4).sum())
+    t_gemm_mem = gemm_bytes / (peaks["hbm_gbs"] * 1e9)
 
     def time_batch(batch, iters):
         s = torch.cuda.current_stream()
@@ -1057,7 +1060,11 @@ def batching_report(args):
             "roofline": {"ms": round((t_gemm_roof + t_gemv_roof) * 1e3, 3),
                          "frac": round((t_gemm_roof + t_gemv_roof) / (ms_all / 1e3), 4),
                          "gemm_ms": round(t_gemm_roof * 1e3, 3), "gemv_ms": round(t_gemv_roof * 1e3, 3),
-                         "peaks": "MEASURED_PEAKS.json bf16_tflops (x products) and hbm_gbs"},
+                         "gemm_hbm_floor_ms": round(t_gemm_mem * 1e3, 3),
+                         "gemm_frac_of_tensor_bound": round(t_gemm_roof / (ms_gemm / 1e3), 4),
+                         "gemm_frac_of_hbm_floor": round(t_gemm_mem / (ms_gemm / 1e3), 4),
+                         "peaks": "MEASURED_PEAKS.json bf16_tflops (x products) and hbm_gbs; the GEMMs' HBM "
+                                  "floor reads A and B once in FP32 and C twice (C += A B)"},
             "plan_s": round(plan_s, 2), "gemm_flops": gemm_flops, "gemv_bytes": gemv_bytes,
             "max_normwise_err": {"gemm": gemm_err, "gemv": gemv_err}, "cpu_baseline": cpu,
             "gpu_launches_incl_graphs": int(launches), "clocks": clk.summary(),

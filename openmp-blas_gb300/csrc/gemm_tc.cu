@@ -337,15 +337,19 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(ScaleSide side_a, ScaleS
   const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
   const bool full = r0 + TR <= j.rows && k0 + TK <= j.K;
   const bool al16 = (reinterpret_cast<uintptr_t>(j.src) & 15) == 0;
-  if (full && al16 && j.cs == 1 && (j.rs & 3) == 0) {
-    // interior tile, K contiguous: 128-bit loads, float4 i of a thread in row
-    // tid / 16 + 16 i; the 16 lanes of a half-warp share that row
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (al16 && j.cs == 1 && (j.rs & 3) == 0 && (full || (j.K & 3) == 0)) {
+    // K contiguous (interior tiles, and edge tiles whose K is a multiple of
+    // 4): 128-bit loads, float4 i of a thread in row tid / 16 + 16 i; the 16
+    // lanes of a half-warp share that row
     unsigned w[4], v[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i;
       const float4 x =
-          dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + idx / 16) * j.rs + k0 + 4 * (idx % 16)));
+          (full || (r0 + idx / 16 < j.rows && k0 + 4 * (idx % 16) < j.K))
+              ? dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + idx / 16) * j.rs + k0 + 4 * (idx % 16)))
+              : zero4;
       w[i] = max(max(mag_bits(x.x), mag_bits(x.y)), max(mag_bits(x.z), mag_bits(x.w)));
       v[i] = min(min(nz_bits(x.x), nz_bits(x.y)), min(nz_bits(x.z), nz_bits(x.w)));
     }
@@ -361,15 +365,17 @@ __global__ void __launch_bounds__(256) f16_scale_kernel(ScaleSide side_a, ScaleS
         if (v[i] != 0xFFFFFFFFu) atomicMin(&rmin[tid / 16 + 16 * i], v[i]);
       }
     }
-  } else if (full && al16 && j.rs == 1 && (j.cs & 3) == 0) {
-    // interior tile, rows contiguous: 128-bit loads of rows 4 (tid % 16) .. + 3,
+  } else if (al16 && j.rs == 1 && (j.cs & 3) == 0 && (full || (j.rows & 3) == 0)) {
+    // rows contiguous (likewise): 128-bit loads of rows 4 (tid % 16) .. + 3,
     // the same four rows for all of a thread's loads; lanes l and l ^ 16 too
     unsigned w[4] = {0u, 0u, 0u, 0u}, v[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i;
       const float4 x =
-          dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + idx / 16) * j.cs + r0 + 4 * (idx % 16)));
+          (full || (k0 + idx / 16 < j.K && r0 + 4 * (idx % 16) < j.rows))
+              ? dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + idx / 16) * j.cs + r0 + 4 * (idx % 16)))
+              : zero4;
       w[0] = max(w[0], mag_bits(x.x));
       w[1] = max(w[1], mag_bits(x.y));
       w[2] = max(w[2], mag_bits(x.z));
@@ -491,18 +497,26 @@ __global__ void __launch_bounds__(256) prep_group_kernel(PrepSide side_a, PrepSi
   const int64_t r0 = (int64_t)(local / j.tiles_k) * TR, k0 = (int64_t)(local % j.tiles_k) * TK;
   const bool full = r0 + TR <= j.rows && k0 + TK <= j.K;
   const bool al16 = (reinterpret_cast<uintptr_t>(j.src) & 15) == 0;
-  if (full && al16 && j.cs == 1 && (j.rs & 3) == 0) {  // 128-bit loads along K
+  // 128-bit loads along the contiguous dimension: on interior tiles, and on
+  // edge tiles too where that dimension's extent is a multiple of 4 (each
+  // float4 then lies wholly inside or wholly outside the operand)
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (al16 && j.cs == 1 && (j.rs & 3) == 0 && (full || (j.K & 3) == 0)) {  // along K
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i, r = idx / (TK / 4), k4 = idx % (TK / 4);
-      const float4 v = dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + r) * j.rs + k0 + 4 * k4));
+      const float4 v = (full || (r0 + r < j.rows && k0 + 4 * k4 < j.K))
+                           ? dev::ld_stream(reinterpret_cast<const float4*>(j.src + (r0 + r) * j.rs + k0 + 4 * k4))
+                           : zero4;
       *reinterpret_cast<float4*>(&tile[r * LD + 4 * k4]) = v;
     }
-  } else if (full && al16 && j.rs == 1 && (j.cs & 3) == 0) {  // 128-bit loads along rows
+  } else if (al16 && j.rs == 1 && (j.cs & 3) == 0 && (full || (j.rows & 3) == 0)) {  // along rows
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = tid + 256 * i, k = idx / (TR / 4), r4 = idx % (TR / 4);
-      const float4 v = dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + k) * j.cs + r0 + 4 * r4));
+      const float4 v = (full || (k0 + k < j.K && r0 + 4 * r4 < j.rows))
+                           ? dev::ld_stream(reinterpret_cast<const float4*>(j.src + (k0 + k) * j.cs + r0 + 4 * r4))
+                           : zero4;
       tile[(4 * r4 + 0) * LD + k] = v.x;
       tile[(4 * r4 + 1) * LD + k] = v.y;
       tile[(4 * r4 + 2) * LD + k] = v.z;
