@@ -575,7 +575,7 @@ def default_extras(args, dev, sp):
     secs["batching"] = guarded("batching", lambda: batching_report(b))
     c = copy.copy(args)
     c.rates, c.min_requests, c.max_requests, c.lone_requests, c.seconds = [5000, 10000, 20000], 4000, 4000, 4000, 0.0
-    c.pool_gb, c.f64_accuracy = 16.0, "auto"
+    c.pool_gb, c.f64_accuracy, c.slice_us = 16.0, "auto", 0
     secs["served"] = guarded("served", lambda: serving_report(c))
     out["extras_seconds"] = {k: round(v, 1) for k, v in secs.items()}
     return out
@@ -1102,7 +1102,7 @@ def serving_report(args):
         -1, 1, generator=gen)
     srv = gbblas.Server(streams=args.streams, max_group=args.max_group, budget_bytes=64 << 30,
                         heavy_streams=args.heavy_streams, heavy_us=args.heavy_us,
-                        heavy_sm_percent=args.heavy_sm_percent)
+                        heavy_sm_percent=args.heavy_sm_percent, slice_us=getattr(args, "slice_us", 0))
     # float64 GEMMs: AUTO (the library default: guarded tensor-core digits
     # where the shape suits) or the FP64 pipes
     f64_acc = 5 if args.f64_accuracy == "fp64" else 3
@@ -1188,7 +1188,7 @@ def serving_report(args):
                                     "AUTO: guarded 7-digit tensor-core scheme from 2^21 multiply-adds, FP64 pipes below"),
                        "budget_GiB": 64, "streams": args.streams or 16, "max_group": args.max_group or 256,
                        "heavy_streams": args.heavy_streams or 2, "heavy_sm_percent": args.heavy_sm_percent or 75,
-                       "heavy_us": args.heavy_us or 300}}
+                       "heavy_us": args.heavy_us or 300, "slice_us": getattr(args, "slice_us", 0) or 200}}
     for p in outs:
         srv.free(p)
     srv.close()
@@ -1534,6 +1534,9 @@ def main():
                     help="serving: share of the SMs a heavy request may take (0: the library default)")
     ap.add_argument("--heavy-streams", type=int, default=0,
                     help="serving: heavy requests in flight at once (0: the library default)")
+    ap.add_argument("--slice-us", type=int, default=0,
+                    help="serving: estimated work per slice of a heavy GEMM (0: the library default, "
+                         "-1: no slices, the SM cap)")
     ap.add_argument("--heavy-us", type=int, default=0,
                     help="serving: estimated GPU time (us) above which a request is heavy (0: default)")
     ap.add_argument("--pool-gb", type=float, default=48.0)

@@ -417,12 +417,18 @@ typedef struct gbblas_server_config {
                             requests in flight (default 64 GiB) */
   int64_t scratch_bytes; /* per-stream scratch reserved at start (default 1 GiB) */
   int32_t heavy_streams; /* heavy requests in flight at once (default 2) */
-  int32_t heavy_sm_percent; /* share of the SMs a heavy request's grid may take
-                               (1..100; default 75): light rounds keep the rest */
+  int32_t heavy_sm_percent; /* share of the SMs the grid of a heavy request that is
+                               not sliced may take (1..100; default 75): light
+                               rounds keep the rest */
   int64_t heavy_us;      /* estimated GPU time (us) above which a request is
                             heavy: it runs alone on a low-priority stream while
                             light rounds (capped at this much estimated work)
                             run on high-priority streams (default 300) */
+  int64_t slice_us;      /* a heavy tensor-core or digit GEMM runs on every SM as
+                            launches over tile ranges of about this much estimated
+                            work each, so light rounds get SMs between them
+                            (default 200; < 0: no slices, the heavy_sm_percent
+                            cap instead, which other heavy requests always get) */
 } gbblas_server_config;
 
 typedef struct gbblas_server_stats {

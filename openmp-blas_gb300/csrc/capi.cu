@@ -267,11 +267,13 @@ gbblas_status gemm_any(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const T* A
     // it recomputed on the pipes) where the shape amortises the operand
     // preparation, the FP64 pipes elsewhere.
     if (const int digits = dgemm_digits_count(acc))
-      return launch_dgemm_digits(c, digits, false, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+      return launch_dgemm_digits(c, digits, false, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s, 0,
+                                 gemm_slices_env());
     if (acc == GBBLAS_ACCURACY_AUTO && dgemm_auto_digits(M, N, K, c->num_sms)) {
       // a shape beyond the digit kernels' grid, or digit planes that do not
       // fit in device memory, fall back to the FP64 pipes
-      const gbblas_status st = launch_dgemm_digits(c, 7, true, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s);
+      const gbblas_status st =
+          launch_dgemm_digits(c, 7, true, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, s, 0, gemm_slices_env());
       if (st != GBBLAS_STATUS_ALLOC_FAILED && st != GBBLAS_STATUS_NOT_SUPPORTED) return st;
       cudaGetLastError();  // a failed allocation leaves no sticky error; clear the last one
     }

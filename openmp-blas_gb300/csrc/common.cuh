@@ -191,15 +191,22 @@ gbblas_status launch_gemm_tc_opts(DeviceCtx* c, int mode, const gbblas_gemm_desc
 
 // The same for a group of independent problems in one persistent launch
 // (tables and operand arena in the stream's scratch).
+// slices > 1: the GEMM kernel as that many launches over consecutive ranges
+// of whole waves of tiles, so that higher-priority streams get SMs between
+// them (the serving loop's heavy requests); the same bits.
 gbblas_status launch_gemm_tc_group(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
-                                   cudaStream_t stream, int max_ctas = 0);
+                                   cudaStream_t stream, int max_ctas = 0, int slices = 1);
 
 // A group bound to its own device memory, for repeated (graph-captured)
 // launches: create uploads the tables once; launch only enqueues kernels.
 struct TcGroupPlan;
 gbblas_status tc_group_create(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
                               TcGroupPlan** out);
-gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream, int max_ctas = 0);
+gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* plan, cudaStream_t stream, int max_ctas = 0,
+                              int slices = 1);
+// GBBLAS_GEMM_SLICES=n (n > 1): single tensor-core and digit GEMMs run as n
+// launches over tile ranges (what the serving loop does with heavy requests).
+int gemm_slices_env();
 void tc_group_destroy(TcGroupPlan* plan);
 int* tc_group_error_word(const TcGroupPlan* plan);
 
@@ -221,7 +228,7 @@ void dgemm_digits_prepare(DeviceCtx* c);
 gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, bool guarded, int64_t M, int64_t N, int64_t K,
                                   const double* A, int64_t rsa, int64_t csa, const double* B, int64_t rsb,
                                   int64_t csb, double* C, int64_t rsc, int64_t csc, cudaStream_t stream,
-                                  int max_ctas = 0);
+                                  int max_ctas = 0, int slices = 1);
 
 // Grouped GEMV: row-streaming problems in one persistent launch, the rest
 // per problem (batch.cu).

@@ -128,6 +128,7 @@ struct DgCfg {
 // One GEMM (device-side view).
 struct DgProblem {
   int M, N, num_kt, tiles_m, tiles_n, total_tiles;
+  int tile_begin, tile_end;  // this launch's tiles (a slice of 0 .. total_tiles - 1)
   double* C;
   int64_t rsc, csc;
   const int* ea;  // [rows of A, padded] row scales
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool is_a = warp == 0;
     int n_issued = 0, g_issued = 0;
     bool stop = false;
-    for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
+    for (int t = p.tile_begin + (int)blockIdx.x; t < p.tile_end && !stop; t += gridDim.x) {
       int m0, n0;
       dg_tile(p, t, m0, n0);
       for (int kt = 0; kt < p.num_kt; ++kt) {
@@ -515,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int consumed = 0, chunk_g = 0, g_used = 0;
       bool stop = false;
-      for (int t = blockIdx.x; t < p.total_tiles && !stop; t += gridDim.x) {
+      for (int t = p.tile_begin + (int)blockIdx.x; t < p.tile_end && !stop; t += gridDim.x) {
         for (int kt = 0; kt < p.num_kt; ++kt) {
           const int s = consumed % ST, round = consumed / ST;
           const bool chunk_first = (kt % CF::kChunk) == 0;
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int nchunks = (p.num_kt + CF::kChunk - 1) / CF::kChunk;
     int chunk_g = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < p.total_tiles && ok; t += gridDim.x) {
+    for (int t = p.tile_begin + (int)blockIdx.x; t < p.tile_end && ok; t += gridDim.x) {
       int m0, n0;
       dg_tile(p, t, m0, n0);
       // sum_w G_w 2^(8(S-1-w)) = hi 2^32 + lo, exactly: groups w < S-4 go
@@ -773,7 +774,7 @@ void dg_setup(DeviceCtx* c) {
 template <int S, int G>
 gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const double* A, int64_t rsa,
                             int64_t csa, const double* B, int64_t rsb, int64_t csb, double* C, int64_t rsc,
-                            int64_t csc, cudaStream_t stream, int max_ctas) {
+                            int64_t csc, cudaStream_t stream, int max_ctas, int slices) {
   using CF = DgCfg<S, G>;
   constexpr int NP = CF::NP;
   if (K > CF::kMaxK) {
@@ -857,8 +858,16 @@ gbblas_status launch_digits(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const
   dg_setup<S, G>(c);
   int grid = (int)std::min<int64_t>(tiles, c->num_sms);
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  dgemm_digits_kernel<S, G><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, mga, mgb, p, err);
-  GB_TRY(check_launch("dgemm_digits_kernel"));
+  // slices: consecutive tile ranges of whole waves, one launch each (higher-
+  // priority work on other streams gets the SMs between them)
+  const int64_t waves = (tiles + grid - 1) / grid;
+  const int64_t nsl = std::max<int64_t>(1, std::min<int64_t>(slices, waves));
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    p.tile_begin = (int)(grid * (waves * sl / nsl));
+    p.tile_end = (int)std::min<int64_t>(tiles, grid * (waves * (sl + 1) / nsl));
+    dgemm_digits_kernel<S, G><<<grid, kThreads, CF::kSmem, stream>>>(ma, mb, mga, mgb, p, err);
+    GB_TRY(check_launch("dgemm_digits_kernel"));
+  }
   if constexpr (G) {
     // the rejected blocks (usually none: the kernel reads the count and returns)
     dgemm_fixup_kernel<<<(unsigned)(max_ctas > 0 ? std::min(max_ctas, 2 * c->num_sms) : 2 * c->num_sms), 256, 0,
@@ -894,14 +903,15 @@ void dgemm_digits_prepare(DeviceCtx* c) {
 
 gbblas_status launch_dgemm_digits(DeviceCtx* c, int digits, bool guarded, int64_t M, int64_t N, int64_t K,
                                   const double* A, int64_t rsa, int64_t csa, const double* B, int64_t rsb,
-                                  int64_t csb, double* C, int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas) {
+                                  int64_t csb, double* C, int64_t rsc, int64_t csc, cudaStream_t stream, int max_ctas,
+                                  int slices) {
   if (M == 0 || N == 0 || K == 0) return GBBLAS_STATUS_SUCCESS;
   if (guarded && digits == 7)
-    return launch_digits<7, 1>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    return launch_digits<7, 1>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas, slices);
   if (!guarded && digits == 7)
-    return launch_digits<7, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    return launch_digits<7, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas, slices);
   if (!guarded && digits == 8)
-    return launch_digits<8, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas);
+    return launch_digits<8, 0>(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas, slices);
   set_error("dgemm (FP64 digits): %d digits%s not supported", digits, guarded ? " with the guard" : "");
   return GBBLAS_STATUS_INVALID_VALUE;
 }

@@ -673,7 +673,8 @@ __device__ __forceinline__ void tile_coords(const TcProblem& p, int t, int& m0, 
 template <int MODE, bool PAIR>
 __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     gemm_split_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
-                      const TcProblem* __restrict__ probs, int nprob, int total_tiles, int64_t sf_stride,
+                      const TcProblem* __restrict__ probs, int nprob, int tile_begin, int total_tiles,
+                      int64_t sf_stride,
                       int* __restrict__ tile_counter, int* __restrict__ err,
                       const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
                       const int* __restrict__ guard_a, const int* __restrict__ guard_b) {
@@ -759,10 +760,11 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       for (int it = 0; !stop; ++it) {
         const int slot = it % kTileRing, use = it / kTileRing;
         int t;
+        // this launch's tiles: tile_begin .. total_tiles - 1
         if constexpr (PAIR)
-          t = (int)(blockIdx.x >> 1) + it * (int)(gridDim.x >> 1);
+          t = tile_begin + (int)(blockIdx.x >> 1) + it * (int)(gridDim.x >> 1);
         else
-          t = atomicAdd(tile_counter, 1);
+          t = tile_begin + atomicAdd(tile_counter, 1);
         if (t >= total_tiles) t = -1;
         if (use > 0 && !mbar_wait_bounded(&ring_empty[slot], (use - 1) & 1, abort_flag, kWaitLimitNs)) {
           fail();
@@ -1586,13 +1588,14 @@ int kernel_setup(DeviceCtx* c) {
 }
 
 template <int MODE, bool PAIR>
-gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
+gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas,
+                                 int tile_begin, int tile_end) {
   using CF = TcCfg<MODE, PAIR>;
   int* err = reinterpret_cast<int*>(pl.base + kErrWordOffset);
   int* counter = reinterpret_cast<int*>(pl.base + kTileCounterOffset);
   const auto* dprobs = reinterpret_cast<const TcProblem*>(pl.base + pl.off_probs);
   const int resident = kernel_setup<MODE, PAIR>(c);
-  int units = (int)std::min<int64_t>(pl.tiles, resident);  // CTAs, or CTA pairs
+  int units = (int)std::min<int64_t>(tile_end - tile_begin, resident);  // CTAs, or CTA pairs
   if (max_ctas > 0) {
     const int cap = PAIR ? std::max(1, max_ctas / 2) : max_ctas;
     if (units > cap) units = cap;
@@ -1600,7 +1603,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   if constexpr (!PAIR) {
     const int* ga = pl.guard ? reinterpret_cast<const int*>(pl.base + pl.off_gflag) : nullptr;
     gemm_split_kernel<MODE, false><<<units, ModeTraits<MODE>::kThreads, CF::kSmem, stream>>>(
-        pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles, pl.kpad, counter, err, scales_a(pl), scales_b(pl), ga,
+        pl.map_a, pl.map_b, dprobs, pl.nprob, tile_begin, tile_end, pl.kpad, counter, err, scales_a(pl), scales_b(pl), ga,
         ga ? ga + pl.a_rows : nullptr);
     return check_launch("gemm_split_kernel");
   } else {
@@ -1617,8 +1620,8 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
   cfg.attrs = at;
   cfg.numAttrs = 1;
   const cudaError_t e =
-      cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, (int)pl.tiles,
-                         pl.kpad, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl),
+      cudaLaunchKernelEx(&cfg, gemm_split_kernel<MODE, true>, pl.map_a, pl.map_b, dprobs, pl.nprob, tile_begin,
+                         tile_end, pl.kpad, counter, err, (const uint32_t*)scales_a(pl), (const uint32_t*)scales_b(pl),
                          (const int*)nullptr, (const int*)nullptr);
   if (e != cudaSuccess) {
     count_launch();
@@ -1630,7 +1633,7 @@ gbblas_status launch_gemm_kernel(DeviceCtx* c, const TcGroupPlan& pl, cudaStream
 }
 
 template <int MODE>
-gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas) {
+gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t stream, int max_ctas, int slices) {
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   const auto* djobs = reinterpret_cast<const SplitJob*>(pl.base + pl.off_jobs);
   // the tile counter, the guard's counts and (FP16 split) the row exponents
@@ -1660,12 +1663,26 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   const PrepSide pb{djobs + pl.njobs, pl.b_tiles, arena_b(pl), (int64_t)(pl.b_rows * pl.pitch), scales_b(pl), gb};
   prep_group_kernel<MODE><<<prep_ctas, 256, 0, stream>>>(pa, pb, pl.njobs, pl.pitch, pl.kpad);
   GB_TRY(check_launch("prep_group_kernel"));
-  gbblas_status st;
-  if constexpr (MODE != kModeFp8 && MODE != kModeF16) {
-    st = pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas)
-                 : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
-  } else {
-    st = launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas);
+  // the GEMM, as `slices` launches over consecutive ranges of whole waves of
+  // tiles (higher-priority work on other streams gets the SMs between them);
+  // each launch restarts the tile counter
+  const bool pair = MODE != kModeFp8 && MODE != kModeF16 && pl.pair;
+  int64_t wave = std::min<int64_t>(pl.tiles, pair ? c->num_sms / 2 : c->num_sms);
+  if (max_ctas > 0) wave = std::min<int64_t>(wave, pair ? std::max(1, max_ctas / 2) : max_ctas);
+  wave = std::max<int64_t>(wave, 1);
+  const int64_t waves = (pl.tiles + wave - 1) / wave;
+  const int64_t nsl = std::max<int64_t>(1, std::min<int64_t>(slices, waves));
+  gbblas_status st = GBBLAS_STATUS_SUCCESS;
+  for (int64_t sl = 0; sl < nsl && st == GBBLAS_STATUS_SUCCESS; ++sl) {
+    const int tb = (int)(wave * (waves * sl / nsl)), te = (int)std::min<int64_t>(pl.tiles, wave * (waves * (sl + 1) / nsl));
+    if (sl > 0)
+      GB_CUDA_TRY(cudaMemsetAsync(pl.base + kTileCounterOffset, 0, sizeof(int), stream));
+    if constexpr (MODE != kModeFp8 && MODE != kModeF16) {
+      st = pl.pair ? launch_gemm_kernel<MODE, true>(c, pl, stream, max_ctas, tb, te)
+                   : launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas, tb, te);
+    } else {
+      st = launch_gemm_kernel<MODE, false>(c, pl, stream, max_ctas, tb, te);
+    }
   }
   if (st == GBBLAS_STATUS_SUCCESS && pl.guard) {
     f16_guard_fixup_kernel<<<2 * c->num_sms, 256, 0, stream>>>(
@@ -1683,6 +1700,12 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
 }
 
 }  // namespace
+
+int gemm_slices_env() {
+  const char* e = std::getenv("GBBLAS_GEMM_SLICES");
+  const int v = e ? std::atoi(e) : 1;
+  return v > 1 ? v : 1;
+}
 
 int tc_stage_k(int mode) {
   if (mode == kModeF16Guard) mode = kModeF16;
@@ -1720,12 +1743,12 @@ void tc_prepare(DeviceCtx* c) {
   kernel_setup<3, true>(c);
 }
 
-gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas) {
+gbblas_status tc_group_launch(DeviceCtx* c, const TcGroupPlan* pl, cudaStream_t stream, int max_ctas, int slices) {
   switch (pl->mode) {
-    case 3: return launch_bound<3>(c, *pl, stream, max_ctas);
-    case kModeFp8: return launch_bound<kModeFp8>(c, *pl, stream, max_ctas);
-    case kModeF16: return launch_bound<kModeF16>(c, *pl, stream, max_ctas);
-    default: return launch_bound<2>(c, *pl, stream, max_ctas);
+    case 3: return launch_bound<3>(c, *pl, stream, max_ctas, slices);
+    case kModeFp8: return launch_bound<kModeFp8>(c, *pl, stream, max_ctas, slices);
+    case kModeF16: return launch_bound<kModeF16>(c, *pl, stream, max_ctas, slices);
+    default: return launch_bound<2>(c, *pl, stream, max_ctas, slices);
   }
 }
 
@@ -1773,14 +1796,14 @@ int* tc_group_error_word(const TcGroupPlan* pl) {
 }
 
 gbblas_status launch_gemm_tc_group(DeviceCtx* c, int mode, const gbblas_gemm_desc* descs, int64_t count,
-                                   cudaStream_t stream, int max_ctas) {
+                                   cudaStream_t stream, int max_ctas, int slices) {
   TcGroupPlan pl;
   GB_TRY(plan_group(mode, descs, count, pl));
   if (pl.nprob == 0) return GBBLAS_STATUS_SUCCESS;
   void* s = nullptr;
   GB_TRY(get_scratch(c, stream, pl.bytes, &s));
   GB_TRY(bind_group(pl, static_cast<char*>(s), stream));
-  return tc_group_launch(c, &pl, stream, max_ctas);
+  return tc_group_launch(c, &pl, stream, max_ctas, slices);
 }
 
 gbblas_status launch_gemm_tc_opts(DeviceCtx* c, int mode, const gbblas_gemm_desc& d, const TcLaunchOpts& opt,
@@ -1791,7 +1814,7 @@ gbblas_status launch_gemm_tc_opts(DeviceCtx* c, int mode, const gbblas_gemm_desc
   void* s = nullptr;
   GB_TRY(get_scratch(c, stream, pl.bytes, &s));
   GB_TRY(bind_group(pl, static_cast<char*>(s), stream));
-  return tc_group_launch(c, &pl, stream, 0);
+  return tc_group_launch(c, &pl, stream, 0, gemm_slices_env());
 }
 
 gbblas_status launch_gemm_tc(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,

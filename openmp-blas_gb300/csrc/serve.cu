@@ -15,6 +15,7 @@
 // while others run joins the next round as soon as a slot and memory free up.
 // Operands come from a CUDA memory pool owned by the server (kept resident).
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -54,6 +55,7 @@ struct Round {
   int stream_slot = 0;
   bool heavy = false;
   int max_ctas = 0;  // grid cap for the round's GEMMs (0 = whole GPU)
+  int slices = 1;    // a heavy GEMM's launches over consecutive tile ranges
   gbblas_status status = GBBLAS_STATUS_SUCCESS;
 };
 
@@ -205,7 +207,7 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
       if (q->f64_digits) {
         note(launch_dgemm_digits(c, q->f64_digits, q->f64_guarded, r.M, r.N, r.K,
                                  static_cast<const double*>(r.A), rsa, csa, static_cast<const double*>(r.B), rsb, csb,
-                                 static_cast<double*>(r.C), rsc, csc, st, cap));
+                                 static_cast<double*>(r.C), rsc, csc, st, cap, rd->slices));
       } else if (r.dtype == GBBLAS_F64) {
         note(launch_gemm_fma<double>(c, r.M, r.N, r.K, static_cast<const double*>(r.A), rsa, csa,
                                      static_cast<const double*>(r.B), rsb, csb, static_cast<double*>(r.C), rsc,
@@ -248,7 +250,8 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
                                static_cast<float*>(r.C), st));
     }
   }
-  for (const auto& g : groups) note(launch_gemm_tc_group(c, g.first, g.second.data(), (int64_t)g.second.size(), st, cap));
+  for (const auto& g : groups)
+    note(launch_gemm_tc_group(c, g.first, g.second.data(), (int64_t)g.second.size(), st, cap, rd->slices));
   // fixed rows-per-item: no autotuning (timing) inside the serving loop
   if (!gemv.empty()) note(launch_gemv_group_rows_fixed(c, gemv.data(), (int64_t)gemv.size(), st, 4));
   rd->status = first_err;
@@ -347,7 +350,19 @@ void scheduler_main(gbblas_server_s* s) {
         // of the GPU.  (Capping only while light work was already queued let
         // later arrivals wait behind whole heavy kernels: p99 2.3x the lone
         // p99 at 1 k req/s against 1.1x with the permanent cap.)
-        if (heavy) rd->max_ctas = std::max(1, s->ctx->num_sms * s->cfg.heavy_sm_percent / 100);
+        if (heavy) {
+          // A heavy tensor-core or digit GEMM runs on the whole GPU as slices
+          // of about slice_us each: between slices the block scheduler serves
+          // the high-priority light streams first.  Other heavy requests keep
+          // the SM cap.
+          Req* h = rd->reqs[0];
+          const bool sliceable = h->r.op == GBBLAS_OP_MTM &&
+                                 (h->f64_digits || (h->r.dtype == GBBLAS_F32 && h->r.accuracy != GBBLAS_ACCURACY_FP32));
+          if (sliceable && s->cfg.slice_us > 0)
+            rd->slices = (int)std::max(1.0, std::ceil(h->est_us / (double)s->cfg.slice_us));
+          else
+            rd->max_ctas = std::max(1, s->ctx->num_sms * s->cfg.heavy_sm_percent / 100);
+        }
         cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
         lk.unlock();
         gbblas_status e;
@@ -393,7 +408,9 @@ gbblas_status gbblas_server_create(const gbblas_server_config* cfg, gbblas_serve
   s->cfg.heavy_streams = 2;
   s->cfg.heavy_us = 300;
   s->cfg.heavy_sm_percent = 75;
+  s->cfg.slice_us = 200;
   if (cfg) {
+    if (cfg->slice_us != 0) s->cfg.slice_us = cfg->slice_us;
     if (cfg->heavy_streams > 0) s->cfg.heavy_streams = cfg->heavy_streams;
     if (cfg->heavy_sm_percent > 0) s->cfg.heavy_sm_percent = std::min(cfg->heavy_sm_percent, 100);
     if (cfg->heavy_us > 0) s->cfg.heavy_us = cfg->heavy_us;

@@ -309,7 +309,7 @@ class Request(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("streams", ctypes.c_int32), ("max_group", ctypes.c_int32), ("budget_bytes", _i64),
                 ("scratch_bytes", _i64), ("heavy_streams", ctypes.c_int32), ("heavy_sm_percent", ctypes.c_int32),
-                ("heavy_us", _i64)]
+                ("heavy_us", _i64), ("slice_us", _i64)]
 
 
 class ServerStats(ctypes.Structure):
@@ -321,8 +321,9 @@ class Server:
     """gbblas_server_*: continuous-batching request loop on the current device."""
 
     def __init__(self, streams=0, max_group=0, budget_bytes=0, scratch_bytes=0, heavy_streams=0, heavy_us=0,
-                 heavy_sm_percent=0):
-        cfg = ServerConfig(streams, max_group, budget_bytes, scratch_bytes, heavy_streams, heavy_sm_percent, heavy_us)
+                 heavy_sm_percent=0, slice_us=0):
+        cfg = ServerConfig(streams, max_group, budget_bytes, scratch_bytes, heavy_streams, heavy_sm_percent, heavy_us,
+                           slice_us)
         h = ctypes.c_void_p()
         call("gbblas_server_create", ctypes.byref(cfg), ctypes.byref(h))
         self.handle = h

@@ -359,3 +359,24 @@ def test_auto_bit_exact_where_the_guard_keeps_the_digits(cuda, kind):
     np.testing.assert_array_equal(got[keep], want[keep])
     ref = O.gemm(A, B, C0, 1, 1, 1)
     assert (np.abs(got - ref)[~keep] <= fp64_tol(A, B, C0)[~keep]).all()
+
+
+@pytest.mark.parametrize("accuracy", [D7, D8, 3])
+def test_sliced_launches_give_the_same_bits(cuda, monkeypatch, accuracy):
+    """GBBLAS_GEMM_SLICES=n runs the digit GEMM as n launches over
+    consecutive ranges of tiles (the serving loop's heavy requests): the
+    same bits, the guard's fix-up list included (one row with a 2^40 entry
+    against a zero row of B sends blocks to the FP64 pipes under AUTO)."""
+    rng = np.random.default_rng(50 + accuracy)
+    M, N, K = 1100, 700, 512
+    A = rng.uniform(-1, 1, (M, K))
+    B = rng.uniform(-1, 1, (K, N))
+    C0 = rng.uniform(-1, 1, (M, N))
+    if accuracy == 3:
+        A[5, 3] = 2.0 ** 40
+        B[3, :] = 0.0
+    whole = run_any(cuda, A, B, C0, accuracy)
+    for n in (2, 7):
+        monkeypatch.setenv("GBBLAS_GEMM_SLICES", str(n))
+        np.testing.assert_array_equal(run_any(cuda, A, B, C0, accuracy), whole)
+    monkeypatch.delenv("GBBLAS_GEMM_SLICES")

@@ -269,3 +269,28 @@ def test_six_products_at_most_fp32_max_relative_error(cuda, dataset, mode):
     r32 = np.max(np.abs(run(cuda, A, B, Z, 1, 1, 1, accuracy=0) - exact) / denom)
     print(f"{dataset}: max relative error mode {mode} {r6:.3e}  fp32 {r32:.3e}")
     assert r6 <= r32
+
+
+@pytest.mark.parametrize("mode", [BF16X3, BF16X6, FP16X3, 3, 2])
+def test_sliced_launches_give_the_same_bits(cuda, monkeypatch, mode):
+    """GBBLAS_GEMM_SLICES=n runs the GEMM kernel as n launches over
+    consecutive tile ranges (what the serving loop does with heavy requests):
+    every tile is computed the same way, so the bits do not change."""
+    rng = np.random.default_rng(40 + mode)
+    M, N, K = 1000, 700, 600
+    if mode == 2:  # FP8: small integers, exact
+        A = rng.integers(-8, 9, (M, K)).astype(np.float32)
+        B = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    else:
+        A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+        B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    if mode == 3:
+        monkeypatch.setenv("GBBLAS_GEMM_AUTO", "1")
+        A[17] *= 2.0 ** -30  # one out-of-span row under AUTO's guard
+        A[17, 0] = 1.0
+    whole = run(cuda, A, B, C0, 1, 1, 1, accuracy=mode)
+    for n in (2, 5):
+        monkeypatch.setenv("GBBLAS_GEMM_SLICES", str(n))
+        np.testing.assert_array_equal(run(cuda, A, B, C0, 1, 1, 1, accuracy=mode), whole)
+    monkeypatch.delenv("GBBLAS_GEMM_SLICES")

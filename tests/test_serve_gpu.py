@@ -307,3 +307,29 @@ def test_server_budget_exhaustion_recovers(cuda):
     assert st["rejected"] == 1 and st["peak_inflight_bytes"] <= 20 << 20
     _healthy(torch, srv, rng)
     srv.close()
+
+
+@pytest.mark.parametrize("slice_us", [-1, 10])
+def test_server_heavy_gemms_sliced_or_capped(cuda, slice_us):
+    """Heavy GEMMs (estimated beyond heavy_us) run as slices over tile
+    ranges on every SM (slice_us > 0) or as one capped launch (slice_us < 0),
+    next to light requests: every result matches FP64 / the oracle, and a
+    heavy result is the same bits as the same request run alone."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(36)
+    srv = gbblas.Server(streams=4, heavy_us=20, slice_us=slice_us)
+    heavy = [ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 1, (1536, 1024, 1024)),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 1, (2048, 2048, 1024)),
+             ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 0, (2048, 1536, 1024), accuracy=BF16X6)]
+    light = [ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (700, 900)) for _ in range(20)]
+    mix = heavy + light
+    lat = srv.run_trace([c.request() for c in mix], np.linspace(0, 2e-3, len(mix)))
+    assert np.all(lat > 0)
+    for c in mix:
+        c.check(c.outs[-1])
+    for c in heavy:
+        in_mix = c.outs[-1].clone()
+        srv.wait(srv.submit(c.request()))
+        assert torch.equal(c.outs[-1], in_mix)
+    srv.close()
