@@ -53,7 +53,16 @@ constexpr int kStages = 6;
 constexpr uint32_t kTileBytes = kBM * kBK * 4;    // 16 KB, A or B
 constexpr uint32_t kStageBytes = 2 * kTileBytes;  // A then B
 constexpr int kComputeWarps = 8;
-constexpr int kThreads = 32 * (kComputeWarps + 1);
+// Two compute warpgroups (warps 0-7) and one producer warpgroup (warps 8-11,
+// of which warp 8 issues the copies).  Registers: the kernel launches with
+// 168 per thread (384 x 168 = 64512 of the SM's 65536); at the start the
+// producer warpgroup gives back down to 40 and the compute warpgroups take
+// 232: 128 x 40 + 256 x 232 = 64512, exactly the launch's total.
+constexpr int kThreads = 32 * (kComputeWarps + 4);
+constexpr int kLaunchRegs = 168, kProducerRegs = 40, kComputeRegs = 232;
+static_assert(kThreads * kLaunchRegs <= 65536, "launch registers exceed the SM's");
+static_assert(128 * kProducerRegs + 32 * kComputeWarps * kComputeRegs <= kThreads * kLaunchRegs,
+              "register split exceeds what the block launched with");
 constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + 256 /*barriers*/;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 static_assert(kSmem <= 232448, "exceeds 227 KB of shared memory");
@@ -176,8 +185,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int64_t pos0 = streamk ? range_b : blockIdx.x;
   int issued = 0;
 
-  if (warp == kComputeWarps) {
-    if (lane == 0) {
+  if (warp >= kComputeWarps) {
+    // the producer warpgroup: registers back to the pool (warpgroup-wide, one
+    // instruction for all four warps), then warp 8 lane 0 streams the tiles
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kProducerRegs));
+    if (warp == kComputeWarps && lane == 0) {
       bool stop = false;
       int t, kb, ke;
       for (int64_t pos = pos0; !stop && seg(pos, t, kb, ke);) {
@@ -202,8 +214,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           ++issued;
         }
       }
+      // after an abort, let this CTA's copies in flight land before it exits
+      if (*abort_flag) {
+        int never = 0;
+        const int from = issued > kStages ? issued - kStages : 0;
+        for (int k = from; k < issued; ++k)
+          (void)mbar_wait_bounded(&full[k % kStages], (k / kStages) & 1, &never, kWaitLimitNs / 2);
+      }
     }
-  } else {
+    return;
+  }
+  {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kComputeRegs));
     const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
     int consumed = 0;
     bool ok = true;
@@ -391,13 +413,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   }
 
-  // after an abort, let this CTA's copies in flight land before it exits
-  if (warp == kComputeWarps && lane == 0 && *abort_flag) {
-    int never = 0;
-    const int from = issued > kStages ? issued - kStages : 0;
-    for (int k = from; k < issued; ++k)
-      (void)mbar_wait_bounded(&full[k % kStages], (k / kStages) & 1, &never, kWaitLimitNs / 2);
-  }
 }
 
 // The four kernels' shared-memory attribute, once per device (before any
