@@ -1088,7 +1088,9 @@ def serving_report(args):
     accuracy (AUTO = six-product split-BF16), 20 % float64; operands device
     resident (inputs are windows of a U[-1,1) pool, outputs from the server's
     pool), 64 GiB admission budget.  Per rate: achieved throughput, p50/p99
-    latency (overall and per class) against the same requests run alone."""
+    latency (overall and per class) against the same requests run alone
+    (one request set: each rate replays a prefix of it), and where the
+    slowest 1 % of requests spent their time (queued, host launch, device)."""
     import numpy as np
     import torch
 
@@ -1143,37 +1145,59 @@ def serving_report(args):
     warm = [make_request() for _ in range(64)]
     srv.run_trace([r for _, r in warm], np.zeros(len(warm)))
 
-    # lone latency: the same kind of requests, one in the system at a time
-    lone_set = [make_request() for _ in range(args.lone_requests)]
-    lone = {"all": []}
-    for cls, r in lone_set:
-        lat = srv.wait(srv.submit(r))
-        lone["all"].append(lat)
-        lone.setdefault(cls, []).append(lat)
+    # One request set for every measurement: each rate replays a prefix of it
+    # with Poisson arrivals, and the lone latencies are those of the same
+    # requests run one at a time (one in the system), so every p99 ratio
+    # compares the same requests.
+    n_max = int(max(args.max_requests, args.lone_requests))
+    shared = [make_request() for _ in range(n_max)]
+    lone_lat = np.empty(n_max)
+    for i, (_, r) in enumerate(shared):
+        lone_lat[i] = srv.wait(srv.submit(r))
 
     def pct(v, q):
         return float(np.percentile(np.asarray(v), q)) * 1e3 if len(v) else None
 
-    lone_p = {k: {"p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in lone.items()}
+    def by_class(lat, reqs):
+        out = {"all": lat}
+        for cls in ("mtm", "mtv", "dot"):
+            out[cls] = lat[[i for i, (c, _) in enumerate(reqs) if c == cls]]
+        return out
+
+    lone_p = {k: {"p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in by_class(lone_lat, shared).items()}
+    lone_p["requests"] = n_max
     results = []
     for rate in args.rates:
-        n = int(min(args.max_requests, max(args.min_requests, rate * args.seconds)))
-        reqs = [make_request() for _ in range(n)]
+        n = int(min(n_max, max(args.min_requests, rate * args.seconds)))
+        reqs = shared[:n]
         arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        base = srv.stats()["submitted"]
         t0 = time.perf_counter()
         lat = srv.run_trace([r for _, r in reqs], arrivals)
         wall = time.perf_counter() - t0
-        by = {"all": lat}
-        for cls in ("mtm", "mtv", "dot"):
-            by[cls] = lat[[i for i, (c, _) in enumerate(reqs) if c == cls]]
-        for p in outs:
-            srv.free(p)
-        outs.clear()
+        parts = np.array([srv.request_times(base + i) for i in range(n)])
+        by = by_class(lat, reqs)
+        lone_n = lone_lat[:n]
         res = {"rate": rate, "requests": n, "throughput_rps": round(n / wall, 1),
                "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
-               "p99_over_lone_p99": round(pct(lat, 99) / lone_p["all"]["p99_ms"], 3),
+               "lone_p99_ms": pct(lone_n, 99),
+               "p99_over_lone_p99": round(pct(lat, 99) / pct(lone_n, 99), 3),
+               "p99_slowdown": round(float(np.percentile(lat / lone_n, 99)), 3),
                "per_class": {k: {"p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in by.items() if k != "all"}}
+        # where the tail's time went: the requests at or above the p99 latency
+        tail = lat >= np.percentile(lat, 99)
+        res["tail_breakdown_ms"] = {
+            "queued": round(float(parts[tail, 0].mean()) * 1e3, 4),
+            "host_launch": round(float(parts[tail, 1].mean()) * 1e3, 4),
+            "device_and_completion": round(float(parts[tail, 2].mean()) * 1e3, 4),
+            "round_size": round(float(parts[tail, 3].mean()), 2),
+            "classes": {c: int(sum(1 for i in np.nonzero(tail)[0] if reqs[i][0] == c)) for c in ("mtm", "mtv", "dot")}}
+        res["p99_parts_ms"] = {"queued": pct(parts[:, 0], 99), "host_launch": pct(parts[:, 1], 99),
+                               "device_and_completion": pct(parts[:, 2], 99)}
         results.append(res)
+    for p in outs:
+        srv.free(p)
+    outs.clear()
     sustained = [r for r in results if r["p99_over_lone_p99"] <= 2.0]
     st = srv.stats()
     line = {"metric": "served p99 latency", "unit": "ms", "higher_is_better": False,
@@ -1189,8 +1213,6 @@ def serving_report(args):
                        "budget_GiB": 64, "streams": args.streams or 16, "max_group": args.max_group or 256,
                        "heavy_streams": args.heavy_streams or 2, "heavy_sm_percent": args.heavy_sm_percent or 75,
                        "heavy_us": args.heavy_us or 300, "slice_us": getattr(args, "slice_us", 0) or 200}}
-    for p in outs:
-        srv.free(p)
     srv.close()
     del pool32, pool64
     torch.cuda.empty_cache()
@@ -1525,7 +1547,8 @@ def main():
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--min-requests", type=int, default=400)
     ap.add_argument("--max-requests", type=int, default=4000)
-    ap.add_argument("--lone-requests", type=int, default=200)
+    ap.add_argument("--lone-requests", type=int, default=200,
+                    help="serving: size of the shared request set is the larger of this and --max-requests")
     ap.add_argument("--streams", type=int, default=0,
                     help="serving: light rounds in flight at once (0: the library default)")
     ap.add_argument("--max-group", type=int, default=0,

@@ -453,6 +453,12 @@ gbblas_status gbblas_server_wait(gbblas_server s, uint64_t ticket, double* laten
 gbblas_status gbblas_server_run_trace(gbblas_server s, const gbblas_request* reqs, const double* arrival_s,
                                       int64_t n, double* latency_s);
 gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out);
+/* Where a finished request's latency went (seconds), for tail analysis:
+ * times[0] queued (submit -> its round was formed), times[1] host launch
+ * (the round's kernels being enqueued), times[2] device and completion
+ * (enqueued -> the completion stamp), times[3] requests in its round.
+ * A request that never ran (cancelled, rejected launch) reports zeros. */
+gbblas_status gbblas_server_request_times(gbblas_server s, uint64_t ticket, double* times);
 /* Cancel a request the server has not started: it leaves the queue and its
  * wait returns GBBLAS_STATUS_CANCELLED.  A request already admitted to a
  * round (its work may be on the GPU) or finished cannot be cancelled:

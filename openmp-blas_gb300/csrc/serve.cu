@@ -43,7 +43,8 @@ struct Req {
   bool heavy = false;
   int f64_digits = 0;         // double GEMM on tensor-core digits (0: the FP64 pipes)
   bool f64_guarded = false;   // ... in the guarded form
-  Clock::time_point t_submit, t_done;
+  Clock::time_point t_submit, t_round, t_enqueued, t_done;
+  int round_size = 0;
   bool done = false;
   gbblas_status status = GBBLAS_STATUS_SUCCESS;
 };
@@ -364,6 +365,11 @@ void scheduler_main(gbblas_server_s* s) {
             rd->max_ctas = std::max(1, s->ctx->num_sms * s->cfg.heavy_sm_percent / 100);
         }
         cudaStream_t st = heavy ? s->heavy_streams[slot] : s->streams[slot];
+        const auto t_round = Clock::now();
+        for (Req* r : rd->reqs) {
+          r->t_round = t_round;
+          r->round_size = (int)rd->reqs.size();
+        }
         lk.unlock();
         gbblas_status e;
         if (s->inject_launch.load() > 0 && s->inject_launch.fetch_sub(1) > 0) {
@@ -372,9 +378,15 @@ void scheduler_main(gbblas_server_s* s) {
         } else {
           e = launch_round(s, rd, st);
         }
+        const auto t_enq = Clock::now();
         lk.lock();
+        for (Req* r : rd->reqs) r->t_enqueued = t_enq;
         if (e != GBBLAS_STATUS_SUCCESS) {  // the host function never runs: finish here
           rd->status = e;
+          for (Req* r : rd->reqs) {
+            r->t_done = t_enq;
+            r->round_size = 0;  // it never ran
+          }
           s->finished.push_back(rd);
         }
         progress = true;
@@ -574,6 +586,35 @@ gbblas_status gbblas_server_get_stats(gbblas_server s, gbblas_server_stats* out)
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->stats;
   out->mean_round_size = s->stats.rounds ? (double)s->round_reqs_total / (double)s->stats.rounds : 0.0;
+  return GBBLAS_STATUS_SUCCESS;
+}
+
+gbblas_status gbblas_server_request_times(gbblas_server s, uint64_t ticket, double* times) {
+  if (!s || !times) {
+    set_error("gbblas_server_request_times: bad arguments");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (ticket >= s->all.size()) {
+    set_error("gbblas_server_request_times: unknown ticket");
+    return GBBLAS_STATUS_INVALID_VALUE;
+  }
+  const Req* q = s->all[ticket].get();
+  if (!q->done) {
+    set_error("gbblas_server_request_times: request %llu has not finished", (unsigned long long)ticket);
+    return GBBLAS_STATUS_NOT_SUPPORTED;
+  }
+  auto sec = [](Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+  if (q->round_size == 0) {
+    times[0] = times[1] = times[2] = times[3] = 0.0;
+  } else {
+    times[0] = sec(q->t_submit, q->t_round);
+    times[1] = sec(q->t_round, q->t_enqueued);
+    // the completion stamp can precede the enqueue stamp by the few
+    // microseconds between the round's last launch and the scheduler's clock
+    times[2] = std::max(0.0, sec(q->t_enqueued, q->t_done));
+    times[3] = (double)q->round_size;
+  }
   return GBBLAS_STATUS_SUCCESS;
 }
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "gbblas_server_wait": (_int, [_vp, ctypes.c_uint64, _vp]),
     "gbblas_server_run_trace": (_int, [_vp, _vp, _vp, _i64, _vp]),
     "gbblas_server_get_stats": (_int, [_vp, _vp]),
+    "gbblas_server_request_times": (_int, [_vp, ctypes.c_uint64, _vp]),
     "gbblas_server_destroy": (_int, [_vp]),
     "gbblas_server_cancel": (_int, [_vp, ctypes.c_uint64]),
     "gbblas_server_inject": (_int, [_vp, ctypes.c_int32, ctypes.c_int32]),
@@ -354,6 +355,14 @@ class Server:
         lat = np.zeros(max(1, n), np.float64)
         call("gbblas_server_run_trace", self.handle, ctypes.addressof(arr), t.ctypes.data, n, lat.ctypes.data)
         return lat[:n]
+
+    def request_times(self, ticket: int):
+        """gbblas_server_request_times: (queued, host launch, device and
+        completion) seconds and the size of the request's round."""
+        import numpy as np
+        t = np.zeros(4, np.float64)
+        call("gbblas_server_request_times", self.handle, ticket, t.ctypes.data)
+        return float(t[0]), float(t[1]), float(t[2]), int(t[3])
 
     def cancel(self, ticket: int) -> int:
         """gbblas_server_cancel: the raw status (0, or NOT_SUPPORTED when the

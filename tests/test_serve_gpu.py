@@ -333,3 +333,35 @@ def test_server_heavy_gemms_sliced_or_capped(cuda, slice_us):
         srv.wait(srv.submit(c.request()))
         assert torch.equal(c.outs[-1], in_mix)
     srv.close()
+
+
+def test_server_request_times(cuda):
+    """gbblas_server_request_times splits a finished request's latency into
+    queued + host launch + device-and-completion, which add up to the latency
+    wait() reports; a request that never ran
+    (its launch failed) reports zeros; an unfinished or unknown ticket is an
+    error."""
+    import gbblas
+    torch = cuda
+    rng = np.random.default_rng(36)
+    srv = gbblas.Server(streams=2, max_group=4)
+    cases = [ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F32, 1, (256, 192, 320)),
+             ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (700, 900)),
+             ReqCase(torch, rng, gbblas.OP_DOT, gbblas.F64, 1, (100000,))]
+    for c in cases:
+        t = srv.submit(c.request())
+        lat = srv.wait(t)
+        q, launch, dev, size = srv.request_times(t)
+        assert q >= 0 and launch >= 0 and dev >= 0 and size >= 1
+        # equal, except that the device part is clamped at zero when the
+        # completion stamp came a few microseconds before the enqueue stamp
+        assert abs((q + launch + dev) - lat) <= 50e-6 + 1e-3 * lat, (q, launch, dev, lat)
+        c.check(c.outs[-1])
+    srv.inject(gbblas.INJECT_LAUNCH, 1)
+    bad = ReqCase(torch, rng, gbblas.OP_DOT, gbblas.F32, 1, (1000,))
+    t = srv.submit(bad.request())
+    assert srv.wait_status(t) == 4  # GBBLAS_STATUS_CUDA_ERROR
+    assert srv.request_times(t) == (0.0, 0.0, 0.0, 0)
+    with pytest.raises(gbblas.GbblasError):
+        srv.request_times(10 ** 9)
+    srv.close()
