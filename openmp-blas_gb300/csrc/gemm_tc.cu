@@ -175,7 +175,7 @@ struct TcCfg {
   static_assert(ModeTraits<MODE>::kBufs * ModeTraits<MODE>::kBufCols <= kTmemCols, "chunk buffers exceed TMEM");
   static_assert(!ModeTraits<MODE>::fp8 || ModeTraits<MODE>::kSfCol0 + 8 * kSub * kStages <= kTmemCols,
                 "scale slots exceed TMEM");
-  static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 1) * 8 + (kTileRing + 2) * 4 <= kBarBytes,
+  static_assert((2 * kMaxStages + 2 * 4 + 2 * kTileRing + 1) * 8 + (kTileRing + 3) * 4 <= kBarBytes,
                 "barrier area too small");
   static_assert(kStages >= 2, "need at least a double-buffered stage ring");
   static_assert(kSmem <= kSmemLimit, "exceeds the 227 KB per-CTA shared memory limit");
@@ -217,6 +217,7 @@ struct SplitJob {
   int64_t dst_row;          // first row in the arena
   int tiles_r, tiles_k;     // preparation tiles (PrepTile) covering padded rows x padded K
   int tile_start;
+  int col_start;            // first CTA of f16_col_scale_kernel (operands whose rows are contiguous)
 };
 
 // ------------------------------------------------------ operand preparation
@@ -632,6 +633,194 @@ __global__ void __launch_bounds__(256) prep_group_kernel(PrepSide side_a, PrepSi
   }
 }
 
+// Row exponents of the FP16 split for operands whose rows are contiguous
+// (row-major B seen as B^T, column-major A): f16_scale_kernel's results by
+// a column reduction.  A CTA covers 1024 consecutive rows (4 per thread, as
+// one float4) and kColScaleK of K; each thread keeps 8 loads in flight and
+// its rows' extremes in registers, then atomicMax-es them into e[R] and
+// emin[R] once.  Conditions (host side, per operand): every job has rows
+// contiguous, 16-byte aligned columns and a row count that is a multiple of
+// 4 (each float4 wholly inside or outside the operand).
+constexpr int kColScaleK = 128;
+
+__global__ void __launch_bounds__(256, 4) f16_col_scale_kernel(ScaleSide side_a, ScaleSide side_b, int njobs) {
+  const bool on_b = (int)blockIdx.x >= side_a.tiles;
+  const ScaleSide& sd = on_b ? side_b : side_a;
+  const int t = (int)blockIdx.x - (on_b ? side_a.tiles : 0);
+  int lo = 0, hi = njobs - 1;  // job: the last whose first CTA is <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sd.jobs[mid].col_start <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const SplitJob& j = sd.jobs[lo];
+  const int local = t - j.col_start;
+  const int kblocks = (int)((j.K + kColScaleK - 1) / kColScaleK);
+  const int64_t r = (int64_t)(local / kblocks) * 1024 + 4 * threadIdx.x;  // this thread's first row
+  const int64_t k0 = (int64_t)(local % kblocks) * kColScaleK;
+  const int64_t k1 = min(k0 + kColScaleK, j.K);
+  if (r >= j.rows) return;
+  const float* __restrict__ src = j.src + r;
+  unsigned w[4] = {0u, 0u, 0u, 0u}, v[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+  for (int64_t k = k0; k < k1; k += 8) {
+    float4 x[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      x[u] = k + u < k1 ? dev::ld_stream(reinterpret_cast<const float4*>(src + (k + u) * j.cs))
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      w[0] = max(w[0], mag_bits(x[u].x));
+      w[1] = max(w[1], mag_bits(x[u].y));
+      w[2] = max(w[2], mag_bits(x[u].z));
+      w[3] = max(w[3], mag_bits(x[u].w));
+      v[0] = min(v[0], nz_bits(x[u].x));
+      v[1] = min(v[1], nz_bits(x[u].y));
+      v[2] = min(v[2], nz_bits(x[u].z));
+      v[3] = min(v[3], nz_bits(x[u].w));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t row = j.dst_row + r + q;
+    if (w[q] != 0u) {
+      // frexp's exponent of a positive finite float (subnormals included):
+      // floor(log2 x) + 1; Inf / NaN take the top exponent, as elsewhere
+      const int e = biased_log2(w[q] >= 0x7F800000u ? 0x7F7FFFFFu : w[q]) - 126;
+      atomicMax(sd.e_out + row, e + kExpBias);
+    }
+    if (sd.emin_out && v[q] != 0xFFFFFFFFu) atomicMax(sd.emin_out + row, ~v[q]);
+  }
+}
+
+// Split-FP16 preparation in one pass for operands whose K is contiguous
+// (row-major A, column-major B): one CTA per arena row reads the row once
+// into registers (kRowPrepNV float4 per thread), finds its largest and its
+// smallest nonzero magnitude (warp shuffles, then the 8 warps' values in
+// shared memory), records e[R] (and, under the guard, emin[R] and the
+// row's out-of-span decision) exactly as f16_scale_kernel and
+// prep_group_kernel do, then scales the row by 2^(15 - e) and writes its two
+// FP16 pieces - the same bits as the two-kernel path, from one read of the
+// operand instead of two.  Padding rows (beyond the job's rows) get zero
+// pieces.  Conditions (host side, per operand): every job K contiguous,
+// 16-byte aligned rows, K a multiple of 4 and at most 1024 kRowPrepNV.
+constexpr int kRowPrepNV = 8;
+constexpr int64_t kRowPrepMinK = 1024;  // shorter rows: the tile kernels (a CTA per row would idle)
+
+struct RowPrepSide {
+  const SplitJob* jobs;
+  int rows;  // arena rows prepared here (0: this operand takes the tile kernels)
+  __half* out;
+  int64_t piece_stride;
+  int* e_out;
+  F16Guard guard;
+};
+
+__global__ void __launch_bounds__(256) f16_row_prep_kernel(RowPrepSide side_a, RowPrepSide side_b, int njobs,
+                                                           int64_t pitch) {
+  constexpr int NV = kRowPrepNV;
+  __shared__ unsigned red_max[8], red_min[8];
+  __shared__ int sh_shift;
+  const bool on_b = (int)blockIdx.x >= side_a.rows;
+  const RowPrepSide& sd = on_b ? side_b : side_a;
+  const int64_t R = (int64_t)blockIdx.x - (on_b ? side_a.rows : 0);  // arena row
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int lo = 0, hi = njobs - 1;  // job: the last whose first arena row is <= R
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sd.jobs[mid].dst_row <= R)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const SplitJob& j = sd.jobs[lo];
+  const int64_t local = R - j.dst_row;
+  const int64_t kp = (int64_t)j.tiles_k * PrepTile<kModeF16>::TK;  // the job's padded K
+  __half* __restrict__ ph = sd.out + R * pitch;
+  if (local >= j.rows) {  // padding row of the job's last tile
+    for (int64_t k = 4 * tid; k < kp; k += 1024) {
+      *reinterpret_cast<uint2*>(ph + k) = make_uint2(0u, 0u);
+      *reinterpret_cast<uint2*>(ph + sd.piece_stride + k) = make_uint2(0u, 0u);
+    }
+    if (sd.guard.flags && tid == 0) sd.guard.flags[R] = 0;
+    return;
+  }
+  const float* __restrict__ src = j.src + local * j.rs;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 x[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const int64_t k = 4 * (tid + 256 * i);
+    x[i] = k < j.K ? dev::ld_stream(reinterpret_cast<const float4*>(src + k)) : zero4;
+  }
+  unsigned mx = 0u, mn = 0xFFFFFFFFu;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    mx = max(mx, max(max(mag_bits(x[i].x), mag_bits(x[i].y)), max(mag_bits(x[i].z), mag_bits(x[i].w))));
+    mn = min(mn, min(min(nz_bits(x[i].x), nz_bits(x[i].y)), min(nz_bits(x[i].z), nz_bits(x[i].w))));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  }
+  if (lane == 0) {
+    red_max[warp] = mx;
+    red_min[warp] = mn;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned w = red_max[0], v = red_min[0];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+      w = max(w, red_max[i]);
+      v = min(v, red_min[i]);
+    }
+    int e_store = 0;  // what f16_scale_kernel leaves: kExpBias + exponent, 0 for an all-zero row
+    if (w != 0u) {
+      int e;
+      (void)frexpf(__uint_as_float(w >= 0x7F800000u ? 0x7F7FFFFFu : w), &e);  // Inf / NaN: the top exponent
+      e_store = e + kExpBias;
+    }
+    sd.e_out[R] = e_store;
+    const int e = e_store == 0 ? 0 : e_store - kExpBias;
+    if (sd.guard.flags) {
+      const_cast<unsigned*>(sd.guard.emin)[R] = v != 0xFFFFFFFFu ? ~v : 0u;
+      const int span_max = 14 + (63 - __clzll((unsigned long long)(j.K > 0 ? j.K : 1)));  // 14 + floor(log2 K)
+      const int out_of_span = e >= 128 || (v != 0xFFFFFFFFu && (e - 1) - (biased_log2(v) - 127) > span_max);
+      sd.guard.flags[R] = out_of_span;
+      if (out_of_span) sd.guard.list[atomicAdd(sd.guard.count, 1)] = (int)R;
+    }
+    sh_shift = kF16ScaleTop - e;
+  }
+  __syncthreads();
+  const int sh = sh_shift;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const int64_t k = 4 * (tid + 256 * i);
+    if (k < kp) {
+      float4 v = make_float4(scale_pow2(x[i].x, sh), scale_pow2(x[i].y, sh), scale_pow2(x[i].z, sh),
+                             scale_pow2(x[i].w, sh));
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const __half2 h01 = __floats2half2_rn(v.x, v.y);
+        const __half2 h23 = __floats2half2_rn(v.z, v.w);
+        uint2 w;
+        w.x = *reinterpret_cast<const uint32_t*>(&h01);
+        w.y = *reinterpret_cast<const uint32_t*>(&h23);
+        *reinterpret_cast<uint2*>(ph + p * sd.piece_stride + k) = w;
+        const float2 f01 = __half22float2(h01), f23 = __half22float2(h23);
+        v.x -= f01.x;
+        v.y -= f01.y;
+        v.z -= f23.x;
+        v.w -= f23.y;
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------- GEMM
 __device__ __forceinline__ int find_problem(const TcProblem* __restrict__ probs, int nprob, int t) {
   int lo = 0, hi = nprob - 1;
@@ -710,6 +899,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   int* ring = reinterpret_cast<int*>(accf + 1);  // [kTileRing] tile ids, -1 = no more work
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kTileRing);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* b_issued_slot = abort_flag + 1;  // single CTAs: K slices the B producer issued (teardown)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = PAIR ? cluster_ctarank() : 0u;  // 0 = the CTA that issues the MMAs
@@ -729,6 +919,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     }
     mbar_init(accf, 1);
     *abort_flag = 0;
+    *b_issued_slot = 0;
     fence_mbar_init();
     prefetch_tensormap(&tm_a);
     prefetch_tensormap(&tm_b);
@@ -855,6 +1046,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
           ++bissued;
         }
       }
+      *b_issued_slot = bissued;
     }
   } else if (warp == 1) {
     if (lane == 0 && PAIR && rank != 0) {
@@ -1157,10 +1349,23 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
   // make sure every tcgen05 op finished, free TMEM.  (In a pair, every copy of
   // both CTAs completes on the even CTA's stage barriers, so it drains for
   // both, and the odd CTA leaves only after the cluster barrier below.)
+  // Single CTAs have two producers, each of which may have stopped at a
+  // different slice: after the barrier below neither issues any more, and
+  // the slices only one of them issued (at most a ring's worth, since each
+  // waits for the consumer that needs both halves) get the missing arrival,
+  // so every issued slice's stage completes once its copies have landed.
+  if constexpr (!PAIR) __syncthreads();
   if (warp == 0 && lane == 0 && rank == 0 && *abort_flag) {
     int never = 0;
-    const int from = issued > ST ? issued - ST : 0;
-    for (int k = from; k < issued; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
+    int hi = issued;
+    if constexpr (!PAIR) {
+      const int ib = *b_issued_slot;
+      const int lo = issued < ib ? issued : ib;
+      hi = issued < ib ? ib : issued;
+      for (int k = lo; k < hi; ++k) mbar_arrive(&full[k % ST]);
+    }
+    const int from = hi > ST ? hi - ST : 0;
+    for (int k = from; k < hi; ++k) (void)mbar_wait_bounded(&full[k % ST], (k / ST) & 1, &never, kWaitLimitNs / 2);
   }
   if constexpr (PAIR) {
     // after an abort the odd CTA cannot see when its last copies (counted on
@@ -1363,6 +1568,9 @@ struct TcGroupPlan {
   CUtensorMap map_a, map_b;
   bool pair = false;  // CTA pairs computing 256 x 128 tiles (see gemm_split_kernel)
   bool guard = false;  // FP16 split with the AUTO guard (F16Guard, f16_guard_fixup_kernel)
+  bool row_prep_a = false, row_prep_b = false;  // FP16 split: operand prepared by f16_row_prep_kernel
+  bool col_scale_a = false, col_scale_b = false;  // FP16 split: exponents by f16_col_scale_kernel
+  int a_col_ctas = 0, b_col_ctas = 0;
   size_t off_gmin = 0, off_gflag = 0, off_glist = 0;  // guard arrays: A rows then B rows each
   size_t off_init_end = 0;  // the launch clears [kTileCounterOffset, off_init_end)
   std::vector<char> tables;  // host image of [off_probs, off_arena), copied with one memcpy
@@ -1478,6 +1686,35 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     pl.b_rows += Np;
   }
   pl.nprob = (int)pl.probs.size();
+  if (pl.f16()) {
+    // one-pass preparation where every job of an operand has K contiguous,
+    // 16-byte aligned rows, K a multiple of 4 within the kernel's reach
+    auto row_ok = [](const SplitJob& j) {
+      return j.cs == 1 && (j.rs & 3) == 0 && (reinterpret_cast<uintptr_t>(j.src) & 15) == 0 && (j.K & 3) == 0 &&
+             j.K >= kRowPrepMinK && (int64_t)j.tiles_k * PrepTile<kModeF16>::TK <= 1024 * kRowPrepNV;
+    };
+    pl.row_prep_a = std::all_of(pl.ajobs.begin(), pl.ajobs.end(), row_ok);
+    pl.row_prep_b = std::all_of(pl.bjobs.begin(), pl.bjobs.end(), row_ok);
+    // the exponents of an operand whose rows are contiguous by a column
+    // reduction (its pieces still come from the tile kernel)
+    auto col_ok = [](const SplitJob& j) {
+      return j.rs == 1 && (j.cs & 3) == 0 && (reinterpret_cast<uintptr_t>(j.src) & 15) == 0 && (j.rows & 3) == 0;
+    };
+    auto number = [](std::vector<SplitJob>& jobs) {
+      int64_t n = 0;
+      for (SplitJob& j : jobs) {
+        j.col_start = (int)n;
+        n += ((j.rows + 1023) / 1024) * ((j.K + kColScaleK - 1) / kColScaleK);
+      }
+      return n;
+    };
+    pl.col_scale_a = !pl.row_prep_a && std::all_of(pl.ajobs.begin(), pl.ajobs.end(), col_ok);
+    pl.col_scale_b = !pl.row_prep_b && std::all_of(pl.bjobs.begin(), pl.bjobs.end(), col_ok);
+    const int64_t na = pl.col_scale_a ? number(pl.ajobs) : 0, nb = pl.col_scale_b ? number(pl.bjobs) : 0;
+    if (na + nb >= (1ll << 31)) pl.col_scale_a = pl.col_scale_b = false;
+    pl.a_col_ctas = pl.col_scale_a ? (int)na : 0;
+    pl.b_col_ctas = pl.col_scale_b ? (int)nb : 0;
+  }
   if ((double)(pl.a_rows + pl.b_rows) * pl.planes() >= 2.0e9 || pl.tiles >= (1ll << 31) ||
       (double)pl.a_tiles >= 2.0e9 || (double)pl.b_tiles >= 2.0e9) {
     set_error("tensor-core gemm: group too large for one launch");
@@ -1648,21 +1885,48 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
     ga = F16Guard{gmin, gflag, glist, gcounts};
     gb = F16Guard{gmin + pl.a_rows, gflag + pl.a_rows, glist + pl.a_rows, gcounts + 1};
   }
-  const int prep_ctas = pl.a_tiles + pl.b_tiles;
+  // tiles of the operands the tile kernels prepare (the FP16 split's
+  // one-pass operands are done by f16_row_prep_kernel instead)
+  const int a_tiles = pl.row_prep_a ? 0 : pl.a_tiles, b_tiles = pl.row_prep_b ? 0 : pl.b_tiles;
+  const int prep_ctas = a_tiles + b_tiles;
   if constexpr (MODE == kModeF16) {
-    // per-row exponents of A's and B^T's arena rows (and the guard's minima)
-    const ScaleSide sa{djobs, pl.a_tiles, reinterpret_cast<int*>(scales_a(pl)), const_cast<unsigned*>(ga.emin)};
-    const ScaleSide sb{djobs + pl.njobs, pl.b_tiles, reinterpret_cast<int*>(scales_b(pl)),
-                       const_cast<unsigned*>(gb.emin)};
-    f16_scale_kernel<<<prep_ctas, 256, 0, stream>>>(sa, sb, pl.njobs);
-    GB_TRY(check_launch("f16_scale_kernel"));
+    if (pl.row_prep_a || pl.row_prep_b) {
+      const RowPrepSide ra{djobs, pl.row_prep_a ? (int)pl.a_rows : 0, reinterpret_cast<__half*>(arena_a(pl)),
+                           (int64_t)(pl.a_rows * pl.pitch), reinterpret_cast<int*>(scales_a(pl)), ga};
+      const RowPrepSide rb{djobs + pl.njobs, pl.row_prep_b ? (int)pl.b_rows : 0,
+                           reinterpret_cast<__half*>(arena_b(pl)), (int64_t)(pl.b_rows * pl.pitch),
+                           reinterpret_cast<int*>(scales_b(pl)), gb};
+      f16_row_prep_kernel<<<ra.rows + rb.rows, 256, 0, stream>>>(ra, rb, pl.njobs, pl.pitch);
+      GB_TRY(check_launch("f16_row_prep_kernel"));
+    }
+    // per-row exponents of A's and B^T's arena rows (and the guard's
+    // minima) for the operands the tile kernel prepares: by the column
+    // reduction where the rows are contiguous, else by tiles
+    const int a_cols = pl.col_scale_a ? pl.a_col_ctas : 0, b_cols = pl.col_scale_b ? pl.b_col_ctas : 0;
+    if (a_cols + b_cols > 0) {
+      const ScaleSide sa{djobs, a_cols, reinterpret_cast<int*>(scales_a(pl)), const_cast<unsigned*>(ga.emin)};
+      const ScaleSide sb{djobs + pl.njobs, b_cols, reinterpret_cast<int*>(scales_b(pl)),
+                         const_cast<unsigned*>(gb.emin)};
+      f16_col_scale_kernel<<<a_cols + b_cols, 256, 0, stream>>>(sa, sb, pl.njobs);
+      GB_TRY(check_launch("f16_col_scale_kernel"));
+    }
+    const int a_st = pl.col_scale_a ? 0 : a_tiles, b_st = pl.col_scale_b ? 0 : b_tiles;
+    if (a_st + b_st > 0) {
+      const ScaleSide sa{djobs, a_st, reinterpret_cast<int*>(scales_a(pl)), const_cast<unsigned*>(ga.emin)};
+      const ScaleSide sb{djobs + pl.njobs, b_st, reinterpret_cast<int*>(scales_b(pl)),
+                         const_cast<unsigned*>(gb.emin)};
+      f16_scale_kernel<<<a_st + b_st, 256, 0, stream>>>(sa, sb, pl.njobs);
+      GB_TRY(check_launch("f16_scale_kernel"));
+    }
   }
   // the pieces (FP8: values and scale words, 128 per K-block of each 128-row
   // block, i.e. `kpad` per row block) of both operands
-  const PrepSide pa{djobs, pl.a_tiles, arena_a(pl), (int64_t)(pl.a_rows * pl.pitch), scales_a(pl), ga};
-  const PrepSide pb{djobs + pl.njobs, pl.b_tiles, arena_b(pl), (int64_t)(pl.b_rows * pl.pitch), scales_b(pl), gb};
-  prep_group_kernel<MODE><<<prep_ctas, 256, 0, stream>>>(pa, pb, pl.njobs, pl.pitch, pl.kpad);
-  GB_TRY(check_launch("prep_group_kernel"));
+  if (prep_ctas > 0) {
+    const PrepSide pa{djobs, a_tiles, arena_a(pl), (int64_t)(pl.a_rows * pl.pitch), scales_a(pl), ga};
+    const PrepSide pb{djobs + pl.njobs, b_tiles, arena_b(pl), (int64_t)(pl.b_rows * pl.pitch), scales_b(pl), gb};
+    prep_group_kernel<MODE><<<prep_ctas, 256, 0, stream>>>(pa, pb, pl.njobs, pl.pitch, pl.kpad);
+    GB_TRY(check_launch("prep_group_kernel"));
+  }
   // the GEMM, as `slices` launches over consecutive ranges of whole waves of
   // tiles (higher-priority work on other streams gets the SMs between them);
   // each launch restarts the tile counter

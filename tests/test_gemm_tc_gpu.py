@@ -157,17 +157,20 @@ def _auto_tc(torch, monkeypatch, A, B, C0, la=1, lb=1, lc=1):
     return run(torch, A, B, C0, la, lb, lc, accuracy=3)
 
 
+@pytest.mark.parametrize("K", [512, 2048])
 @pytest.mark.parametrize("lc,la,lb", [(1, 1, 1), (0, 0, 0), (1, 0, 1)])
-def test_auto_guard_recomputes_out_of_span_rows_and_columns(cuda, monkeypatch, lc, la, lb):
+def test_auto_guard_recomputes_out_of_span_rows_and_columns(cuda, monkeypatch, lc, la, lb, K):
     """Rows of A and columns of B mixing magnitudes far apart (one entry of
     2^20 among entries of 2^-20, beyond the FP16 split's span at this K) fall
     back to FP32 FMAs: AUTO meets (2^-19 + 2 K eps32)(|A||B|) everywhere,
     while the plain FP16 split misses it on those rows and columns (the big
     entry meets a zero on the other side, so the small entries, which the
     row's scale pushes into FP16's subnormal range, make the whole result);
-    every other output equals the plain FP16 split's bit for bit."""
+    every other output equals the plain FP16 split's bit for bit.  At
+    K = 2048 the K-contiguous operands (row-major A, column-major B) take the
+    one-pass preparation, which makes the guard's decisions itself."""
     rng = np.random.default_rng(21)
-    M, N, K = 300, 260, 512
+    M, N = 300, 260
     A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
     B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
     bad_rows, bad_cols = [3, 150, 299], [0, 77, 259]
@@ -180,6 +183,9 @@ def test_auto_guard_recomputes_out_of_span_rows_and_columns(cuda, monkeypatch, l
         B[(7 * c) % K, c] = 2.0 ** 20
         A[:, (7 * c) % K] = 0.0
     C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    # the guarded split never cuts K; the plain one must not either for the
+    # bit-for-bit comparison below (split-K sums K in parts)
+    monkeypatch.setenv("GBBLAS_TC_SPLITK", "1")
     got = _auto_tc(cuda, monkeypatch, A, B, C0, la, lb, lc).astype(np.float64)
     plain = run(cuda, A, B, C0, la, lb, lc, accuracy=FP16X3).astype(np.float64)
     exact = A.astype(np.float64) @ B.astype(np.float64) + C0
@@ -294,3 +300,106 @@ def test_sliced_launches_give_the_same_bits(cuda, monkeypatch, mode):
         monkeypatch.setenv("GBBLAS_GEMM_SLICES", str(n))
         np.testing.assert_array_equal(run(cuda, A, B, C0, 1, 1, 1, accuracy=mode), whole)
     monkeypatch.delenv("GBBLAS_GEMM_SLICES")
+
+
+def _sgemm_strided(torch, A, B, lda, ldb, accuracy):
+    """C = A B with A row-major of row stride lda >= K and B column-major of
+    column stride ldb >= K (both K contiguous), C row-major, from zero."""
+    import gbblas
+    M, K = A.shape
+    N = B.shape[1]
+    hA = np.zeros((M, lda), np.float32)
+    hA[:, :K] = A
+    hB = np.zeros((N, ldb), np.float32)
+    hB[:, :K] = B.T
+    tA, tB = torch.from_numpy(hA).cuda(), torch.from_numpy(hB).cuda()
+    tC = torch.zeros(M * N, device="cuda")
+    gbblas.call("gbblas_sgemm", M, N, K, tA.data_ptr(), lda, 1, tB.data_ptr(), 1, ldb, tC.data_ptr(), N, 1,
+                accuracy, None)
+    gbblas.call("gbblas_check_stream", None)
+    return tC.cpu().numpy().reshape(M, N)
+
+
+@pytest.mark.parametrize("accuracy", [FP16X3, 3])
+@pytest.mark.parametrize("shape", [(192, 320, 1024), (130, 260, 2052), (64, 96, 8192)])
+def test_one_pass_preparation_matches_tile_preparation(cuda, monkeypatch, shape, accuracy):
+    """The FP16 split prepares operands whose K is contiguous in one pass
+    (16-byte aligned rows, K a multiple of 4, 1024 <= K <= 8192: row-major A,
+    column-major B).  The same values with a row stride of K + 1 go through
+    the scale and tile kernels instead.  Both write the same exponents and
+    pieces (and, under AUTO's guard, the same out-of-span decisions: one
+    row of A and one column of B are out of span here), so C is the same
+    bit for bit."""
+    if accuracy == 3:
+        monkeypatch.setenv("GBBLAS_GEMM_AUTO", "1")  # AUTO on the tensor cores: the guarded FP16 split
+    M, N, K = shape
+    rng = np.random.default_rng(M + N + K)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    A[5] *= np.float32(2.0 ** -30)
+    A[5, 3] = 2.0 ** 10
+    B[:, 7] *= np.float32(2.0 ** -30)
+    B[11, 7] = 2.0 ** 10
+    one_pass = _sgemm_strided(cuda, A, B, K, K, accuracy)
+    tiles = _sgemm_strided(cuda, A, B, K + 1, K + 1, accuracy)
+    np.testing.assert_array_equal(one_pass, tiles)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    absA, absB = np.abs(A).astype(np.float64), np.abs(B).astype(np.float64)
+    if accuracy == 3:
+        tol = (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
+    else:
+        tol = split_tol(absA, absB, K, FP16X3)
+        tol[5, :] = np.inf  # out of the plain split's span (the guard's rows)
+        tol[:, 7] = np.inf
+    assert np.all(np.abs(one_pass - exact) <= tol)
+
+
+def _sgemm_mn_major(torch, A, B, lda, ldb, accuracy):
+    """C = A B with A column-major of column stride lda >= M and B row-major
+    of row stride ldb >= N (rows of A and of B^T contiguous), C row-major."""
+    import gbblas
+    M, K = A.shape
+    N = B.shape[1]
+    hA = np.zeros((K, lda), np.float32)
+    hA[:, :M] = A.T
+    hB = np.zeros((K, ldb), np.float32)
+    hB[:, :N] = B
+    tA, tB = torch.from_numpy(hA).cuda(), torch.from_numpy(hB).cuda()
+    tC = torch.zeros(M * N, device="cuda")
+    gbblas.call("gbblas_sgemm", M, N, K, tA.data_ptr(), 1, lda, tB.data_ptr(), ldb, 1, tC.data_ptr(), N, 1,
+                accuracy, None)
+    gbblas.call("gbblas_check_stream", None)
+    return tC.cpu().numpy().reshape(M, N)
+
+
+@pytest.mark.parametrize("accuracy", [FP16X3, 3])
+@pytest.mark.parametrize("shape", [(128, 256, 64), (1028, 2052, 300), (96, 4100, 1000)])
+def test_column_scale_matches_tile_scale(cuda, monkeypatch, shape, accuracy):
+    """The FP16 split finds the row exponents of an operand whose rows are
+    contiguous (column-major A, row-major B; 16-byte aligned, row count a
+    multiple of 4) by a column reduction; with a leading dimension of
+    M + 1 (N + 1) the tile kernel finds them.  Same exponents, same guard
+    decisions (one row of A and one column of B out of span), so C is the
+    same bit for bit."""
+    if accuracy == 3:
+        monkeypatch.setenv("GBBLAS_GEMM_AUTO", "1")  # AUTO on the tensor cores: the guarded FP16 split
+    M, N, K = shape
+    rng = np.random.default_rng(M + 2 * N + 3 * K)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    A[5] *= np.float32(2.0 ** -30)
+    A[5, 3] = 2.0 ** 10
+    B[:, 7] *= np.float32(2.0 ** -30)
+    B[11, 7] = 2.0 ** 10
+    col = _sgemm_mn_major(cuda, A, B, M, N, accuracy)
+    tiles = _sgemm_mn_major(cuda, A, B, M + 1, N + 1, accuracy)
+    np.testing.assert_array_equal(col, tiles)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    absA, absB = np.abs(A).astype(np.float64), np.abs(B).astype(np.float64)
+    if accuracy == 3:
+        tol = (2.0 ** -19 + 2 * K * np.finfo(np.float32).eps) * (absA @ absB)
+    else:
+        tol = split_tol(absA, absB, K, FP16X3)
+        tol[5, :] = np.inf  # out of the plain split's span (the guard's rows)
+        tol[:, 7] = np.inf
+    assert np.all(np.abs(col - exact) <= tol)

@@ -260,19 +260,23 @@ def test_server_malformed_request(cuda, field, value):
 
 
 def test_server_cancel(cuda):
-    """Requests held back by the budget can be cancelled: their waits return
-    CANCELLED and their outputs stay untouched; a request that already ran
-    cannot be; the rest complete correctly."""
+    """Queued requests can be cancelled: their waits return CANCELLED and
+    their outputs stay untouched; a request that already ran cannot be; the
+    rest complete correctly.  One stream and one request per round: a
+    double GEMM on the FP64 pipes (milliseconds) runs first, so the GEMVs
+    behind it are still queued when the test cancels them."""
     import gbblas
     torch = cuda
     rng = np.random.default_rng(34)
-    # each 1536 x 1536 f32 GEMV holds ~9.4 MiB: with a 10 MiB budget one runs at a time
-    srv = gbblas.Server(streams=1, max_group=1, budget_bytes=10 << 20)
+    srv = gbblas.Server(streams=1, max_group=1, heavy_us=1 << 40)
+    first = ReqCase(torch, rng, gbblas.OP_MTM, gbblas.F64, 1, (1536, 1536, 2048), accuracy=5)  # FP64 pipes, ~8 ms
     cases = [ReqCase(torch, rng, gbblas.OP_MTV, gbblas.F32, 1, (1536, 1536)) for _ in range(40)]
+    t_first = srv.submit(first.request())
     tickets = [srv.submit(c.request()) for c in cases]
     # from the back of the queue, which the scheduler reaches last
     cancelled = [t for t in reversed(tickets[10:]) if srv.cancel(t) == 0]
     assert len(cancelled) >= 20
+    assert srv.wait_status(t_first) == 0
     for c, t in zip(cases, tickets):
         st = srv.wait_status(t)
         if t in cancelled:
