@@ -171,9 +171,10 @@ struct TcCfg {
   static constexpr uint32_t kBStageBytes = P * kSub * kBBytes + kSfBytes / 2;
   static constexpr uint32_t kTmemCols = 512;
   static constexpr size_t kBarBytes = 1024;  // mbarriers, tile ring, TMEM slot, abort flag
-  // FP8: per epilogue warp one 32 x 32 float block (4 KB, 1024-aligned) that
-  // a TMA reduce-add store adds into C
-  static constexpr size_t kEpiScratch = ModeTraits<MODE>::fp8 ? (size_t)ModeTraits<MODE>::kEpiWarps * 4096 : 0;
+  // Single CTAs: per epilogue warp one 32 x 32 float block (4 KB, 1024-aligned)
+  // that a TMA reduce-add store adds into C (where C's layout allows it)
+  static constexpr bool kTmaC = !PAIR;
+  static constexpr size_t kEpiScratch = kTmaC ? (size_t)ModeTraits<MODE>::kEpiWarps * 4096 : 0;
   static constexpr int kStagesFit = (int)((kSmemLimit - 1024 - kBarBytes - kEpiScratch) / kStageBytes);
   static constexpr int kStages = kStagesFit > kMaxStages ? kMaxStages : kStagesFit;
   static constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + kEpiScratch + kBarBytes;
@@ -904,7 +905,7 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
     return smem + (size_t)s * CF::kStageBytes + (size_t)NT * (CF::kABytes + CF::kBBytes) +
            (size_t)op * 512 * MT::kSub;
   };
-  float* epi_scratch = reinterpret_cast<float*>(smem + (size_t)ST * CF::kStageBytes);  // FP8, 1024-aligned
+  float* epi_scratch = reinterpret_cast<float*>(smem + (size_t)ST * CF::kStageBytes);  // single CTAs, 1024-aligned
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)ST * CF::kStageBytes + CF::kEpiScratch);
   uint64_t* full = bars;                   // [ST]  TMA -> MMA
   uint64_t* empty = full + ST;             // [ST]  MMA -> TMA
@@ -1298,10 +1299,21 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
             if (__ldg(guard_b + (int64_t)pr.b_row + n0 + col0 + c)) skip_cols |= uint64_t(1) << c;
         }
       }
-      if constexpr (MT::fp8) {
+      if constexpr (CF::kTmaC) {
         if (pr.c_tma) {
           // C += the warp's 32 rows, 32 columns at a time, by TMA reduce-add
-          // from a 128-byte-swizzled block (16-byte chunk c of row r at c ^ (r % 8))
+          // from a 128-byte-swizzled block (16-byte chunk c of row r at c ^ (r % 8)).
+          // The warps hand C's update to the TMA unit and go back to folding
+          // the next tile's chunks at once.  Outputs the AUTO guard leaves to
+          // its fix-up add -0.0, which leaves every C value (-0.0 included)
+          // as it was.
+          if constexpr (MT::f16) {
+            if (skip_row || skip_cols) {
+#pragma unroll
+              for (int c = 0; c < kCols; ++c)
+                if (skip_row || ((skip_cols >> c) & 1)) acc[c] = -0.0f;
+            }
+          }
           float* scr = epi_scratch + (warp - 2) * 1024;
 #pragma unroll
           for (int cb = 0; cb < kCols; cb += 32) {
@@ -1393,8 +1405,8 @@ __global__ void __launch_bounds__(ModeTraits<MODE>::kThreads, 1)
       }
     }
   }
-  // FP8: the epilogue's TMA reduce-add stores into C have completed
-  if constexpr (MT::fp8) {
+  // the epilogue's TMA reduce-add stores into C have completed
+  if constexpr (CF::kTmaC) {
     if (warp >= 2 && warp < 2 + MT::kEpiWarps && lane == 0) bulk_wait_group0();
   }
   tc_fence_before();
@@ -1682,9 +1694,10 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
       p.rsc = parts > 1 ? ppitch : g.rsc;
       p.csc = parts > 1 ? 1 : g.csc;
       p.c_tma = 0;
-      // FP8 adds its results into C with TMA reduce-add stores where C rows
-      // are contiguous, 16-byte aligned and 16-byte-multiple apart
-      if (pl.fp8() && parts == 1 && g.csc == 1 && g.rsc >= g.N && (g.rsc % 4) == 0 &&
+      // single CTAs add their results into C with TMA reduce-add stores
+      // where C rows are contiguous, 16-byte aligned and 16-byte-multiple
+      // apart (split-K partials are stored by the register path)
+      if (!pl.pair && parts == 1 && g.csc == 1 && g.rsc >= g.N && (g.rsc % 4) == 0 &&
           (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
           make_map_f32_2d(&p.c_map, g.C, (uint64_t)g.N, (uint64_t)g.M, (uint64_t)g.rsc, 32, 32, true) ==
               GBBLAS_STATUS_SUCCESS)
