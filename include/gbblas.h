@@ -77,7 +77,9 @@ typedef enum gbblas_accuracy {
                                  that holds Inf / NaN, are recomputed with FP32 FMAs,
                                  so the error stays within (2^-19 + 2 K eps32) (|A||B|)_ij.
                                  GBBLAS_GEMM_AUTO=0 / 1 forces the FP32 / FP16X3 choice.
-                                 Grouped, batched and served GEMMs: FP16X3 with the guard */
+                                 Grouped and batched GEMMs: FP16X3 with the guard; served
+                                 GEMMs the same, or one FP32 FMA kernel below 2^26
+                                 multiply-adds */
   GBBLAS_ACCURACY_BF16X6 = 4, /* FP32-accurate: a = p0 + p1 + p2 in BF16 (all 24 bits),
                                  the six products p_i*p_j with i + j < 3 on tcgen05 */
   /* Double-precision GEMM (gbblas_dgemm_ex) only: */
@@ -400,7 +402,8 @@ typedef enum gbblas_dtype { GBBLAS_F32 = 0, GBBLAS_F64 = 1 } gbblas_dtype;
 typedef struct gbblas_request {
   int32_t op;       /* gbblas_op */
   int32_t dtype;    /* gbblas_dtype */
-  int32_t accuracy; /* gbblas_accuracy of an MTM: float - AUTO = guarded split-FP16;
+  int32_t accuracy; /* gbblas_accuracy of an MTM: float - AUTO = guarded split-FP16
+                       (one FP32 FMA kernel below 2^26 multiply-adds);
                        double - FP64 = the FP64 pipes, FP64_DIGITS7 / 8 = unguarded
                        tensor-core digits, any other value gbblas_dgemm's default */
   int32_t layout;   /* gbblas_layout of the matrices */

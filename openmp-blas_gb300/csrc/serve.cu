@@ -68,6 +68,18 @@ int server_mode(int32_t acc) {
   return acc == GBBLAS_ACCURACY_AUTO ? kTcModeF16Guard : tc_mode((gbblas_accuracy)acc);
 }
 
+// An AUTO float GEMM below 2^26 multiply-adds (about 400^3) runs as one FP32
+// FMA kernel: the guarded split-FP16 chain is five launches (clears,
+// exponents, pieces, GEMM, guard fix-up) whose fixed cost exceeds the whole
+// FMA kernel at that size, and FMA arithmetic is FP32-accurate by
+// definition.  The choice depends on the shape alone, so a request computes
+// the same bits alone and in a mix.
+constexpr double kServeAutoFmaMacs = 67108864.0;
+bool server_auto_fma(const gbblas_request& r) {
+  return r.op == GBBLAS_OP_MTM && r.dtype == GBBLAS_F32 && r.accuracy == GBBLAS_ACCURACY_AUTO &&
+         (double)r.M * (double)r.N * (double)r.K < kServeAutoFmaMacs;
+}
+
 // Tensor-core digits of a double GEMM request (0: the FP64 pipes): FP64 means
 // the pipes, FP64_DIGITS7 / 8 those digits, anything else (the float-only
 // modes included) the library default - gbblas_dgemm's guarded 7-digit
@@ -90,7 +102,7 @@ int64_t working_set(const gbblas_request& r, int f64_digits, bool f64_guarded) {
   switch (r.op) {
     case GBBLAS_OP_MTM: {
       int64_t b = (r.M * r.K + r.K * r.N + r.M * r.N) * s;
-      if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32)
+      if (r.dtype == GBBLAS_F32 && r.accuracy != GBBLAS_ACCURACY_FP32 && !server_auto_fma(r))
         b += (int64_t)tc_arena_bytes(server_mode(r.accuracy), r.M, r.N, r.K);
       if (f64_digits) b += (int64_t)dgemm_digits_scratch_bytes(f64_digits, f64_guarded, r.M, r.N, r.K);
       return b;
@@ -119,6 +131,8 @@ double estimate_us(const gbblas_request& r, int f64_digits) {
         rate = 1.2e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP32)
         rate = 55e6;
+      else if (server_auto_fma(r))
+        rate = 20e6;  // the FMA kernel on shapes below 2^26 multiply-adds
       else if (r.accuracy == GBBLAS_ACCURACY_BF16X3)
         rate = 430e6;
       else if (r.accuracy == GBBLAS_ACCURACY_FP8)
@@ -213,7 +227,7 @@ gbblas_status launch_round(gbblas_server_s* s, Round* rd, cudaStream_t st) {
         note(launch_gemm_fma<double>(c, r.M, r.N, r.K, static_cast<const double*>(r.A), rsa, csa,
                                      static_cast<const double*>(r.B), rsb, csb, static_cast<double*>(r.C), rsc,
                                      csc, st, cap));
-      } else if (r.accuracy == GBBLAS_ACCURACY_FP32) {
+      } else if (r.accuracy == GBBLAS_ACCURACY_FP32 || server_auto_fma(r)) {
         note(launch_gemm_fma<float>(c, r.M, r.N, r.K, static_cast<const float*>(r.A), rsa, csa,
                                     static_cast<const float*>(r.B), rsb, csb, static_cast<float*>(r.C), rsc, csc,
                                     st, cap));
