@@ -301,12 +301,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int64_t c0 = ((int64_t)t * nk + 1) * G - 1;
         const int first = (int)(c0 / kt_total), last = (int)((((int64_t)t * nk + nk) * G - 1) / kt_total);
         const int sidx = (int)blockIdx.x - first, nseg = last - first + 1;
-        float* slot = slots + ((int64_t)t * max_seg + sidx) * (kBM * kBN);
+        // slots are thread-major: float4 v of compute thread tid (its
+        // acc[v / 2][4 (v % 2) .. + 3]) at float4 index 256 v + tid, so a
+        // warp's 32 lanes store and load 512 contiguous bytes at a time;
+        // every segment of a tile uses the same thread-to-output mapping
+        float4* slot = reinterpret_cast<float4*>(slots + ((int64_t)t * max_seg + sidx) * (kBM * kBN));
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            __stcg(slot + owned<A_KMAJ>(ty, i) * kBN + owned<B_KMAJ>(tx, j), acc[i][j]);
+        for (int v = 0; v < 16; ++v)
+          __stcg(slot + 256 * v + threadIdx.x,
+                 make_float4(acc[v / 2][4 * (v % 2)], acc[v / 2][4 * (v % 2) + 1], acc[v / 2][4 * (v % 2) + 2],
+                             acc[v / 2][4 * (v % 2) + 3]));
         // every compute warp's slot stores, then one count per segment
         // (bounded waits on two barriers: an aborted warp never leaves the
         // others waiting)
@@ -332,14 +336,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         // the last segment: the tile's sum over its slots in K order (this
         // segment's own slot included), then into C below
         for (int q = 0; q < nseg; ++q) {
-          const float* sq = slots + ((int64_t)t * max_seg + q) * (kBM * kBN);
+          const float4* sq = reinterpret_cast<const float4*>(slots + ((int64_t)t * max_seg + q) * (kBM * kBN));
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const float v = __ldcg(sq + owned<A_KMAJ>(ty, i) * kBN + owned<B_KMAJ>(tx, j));
-              acc[i][j] = q == 0 ? v : acc[i][j] + v;
-            }
+          for (int v = 0; v < 16; ++v) {
+            const float4 x = __ldcg(sq + 256 * v + threadIdx.x);
+            float* a = &acc[v / 2][4 * (v % 2)];
+            a[0] = q == 0 ? x.x : a[0] + x.x;
+            a[1] = q == 0 ? x.y : a[1] + x.y;
+            a[2] = q == 0 ? x.z : a[2] + x.z;
+            a[3] = q == 0 ? x.w : a[3] + x.w;
+          }
         }
       }
       // C += acc (rows / columns outside the matrix dropped).  Loads of C for
