@@ -149,13 +149,17 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
 bool sgemm_tma_eligible(int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa, int64_t csa, const float* B,
                         int64_t rsb, int64_t csb);
 void sgemm_tma_prepare(DeviceCtx* c);  // kernel attributes, before any stream capture
-// streamk != 0: the tiles' K blocks shared out equally among the CTAs
+// streamk = 1: the tiles' K blocks shared out equally among the CTAs
 // (stream-K; sgemm_tma_streamk_useful says where whole tiles fill the SMs
-// badly enough for it to be worth trying).
+// badly enough for it to be worth trying); 2: clusters of two CTAs, each
+// with half of one tile's K blocks, adding through distributed shared
+// memory (sgemm_tma_pairs_useful: where two CTAs per tile fill the SMs in
+// one wave; stream-K where they cannot).
 gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, const float* A, int64_t rsa,
                                int64_t csa, const float* B, int64_t rsb, int64_t csb, float* C, int64_t rsc,
                                int64_t csc, cudaStream_t stream, int max_ctas = 0, int streamk = 0);
 bool sgemm_tma_streamk_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
+bool sgemm_tma_pairs_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K);
 
 // C += A*B on the tcgen05 tensor cores (gemm_tc.cu).  mode = tc_mode(acc):
 // 2 / 3 = FP32 operands split into that many BF16 pieces, 8 = FP8-E4M3 with

@@ -353,6 +353,8 @@ gbblas_status launch_gemm_fma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, con
     if (tile < 0)
       tile = (tma && csb == 1 && big_tiles >= (int64_t)c->num_sms) ? 2
                                                                    : (big_tiles >= 2 * (int64_t)c->num_sms ? 1 : 0);
+    if (tile == 4 && tma)
+      return launch_sgemm_tma(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas, 2);
     if (tile == 3 && tma)
       return launch_sgemm_tma(c, M, N, K, A, rsa, csa, B, rsb, csb, C, rsc, csc, stream, max_ctas, 1);
     if (tile >= 2 && tma)

@@ -66,7 +66,7 @@ static_assert(128 * kProducerRegs + 32 * kComputeWarps * kComputeRegs <= kThread
 constexpr size_t kSmem = 1024 /*alignment slack*/ + (size_t)kStages * kStageBytes + 256 /*barriers*/;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 static_assert(kSmem <= 232448, "exceeds 227 KB of shared memory");
-static_assert((2 * kStages + 2) * 8 + 4 <= 256, "barrier area too small");
+static_assert((2 * kStages + 4) * 8 + 4 <= 256, "barrier area too small");
 
 // The 8 values (one per owned row or column i) of 4 consecutive k (kq*4..+3)
 // from a tile: v[i][kk].
@@ -133,7 +133,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* empty = full + kStages;
   uint64_t* seg_stored = empty + kStages;   // stream-K: every compute warp stored its part of a segment
   uint64_t* seg_decided = seg_stored + 1;  // stream-K: the tile count was taken
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(seg_decided + 1);
+  uint64_t* xfree = seg_decided + 1;       // cluster pairs (odd CTA): the even CTA's ring may be written
+  uint64_t* xready = xfree + 1;            // cluster pairs (even CTA): the odd CTA's sums are in its ring
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(xready + 1);
   auto a_tile = [&](int s) { return smem + (size_t)s * kStageBytes; };
   auto b_tile = [&](int s) { return smem + (size_t)s * kStageBytes + kTileBytes; };
 
@@ -145,12 +147,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     mbar_init(seg_stored, kComputeWarps);
     mbar_init(seg_decided, 1);
+    mbar_init(xfree, 32 * kComputeWarps);  // one arrival per compute thread of the other CTA
+    mbar_init(xready, 32 * kComputeWarps);
     *abort_flag = 0;
     fence_mbar_init();
     prefetch_tensormap(&tm_a);
     prefetch_tensormap(&tm_b);
   }
   __syncthreads();
+  // cluster pairs: both CTAs' barriers exist before either signals the other
+  if (streamk == 2) cluster_sync_all();
+  const uint32_t crank = streamk == 2 ? cluster_ctarank() : 0u;
 
   auto fail = [&]() {
     *abort_flag = 1;
@@ -163,15 +170,23 @@ __global__ void __launch_bounds__(kThreads, 1)
   // K blocks laid end to end.  seg(i, t, kb, ke) gives segment i; false when
   // there is none.
   const int64_t kt_total = (int64_t)ntiles * nk;
-  const int64_t range_b = streamk ? kt_total * blockIdx.x / gridDim.x : 0;
-  const int64_t range_e = streamk ? kt_total * (blockIdx.x + 1) / gridDim.x : 0;
+  const int64_t range_b = streamk == 1 ? kt_total * blockIdx.x / gridDim.x : 0;
+  const int64_t range_e = streamk == 1 ? kt_total * (blockIdx.x + 1) / gridDim.x : 0;
   auto seg = [&](int64_t& pos, int& t, int& kb, int& ke) -> bool {
-    if (!streamk) {
+    if (streamk == 0) {
       t = (int)pos;
       if (t >= ntiles) return false;
       kb = 0;
       ke = nk;
       pos += gridDim.x;
+      return true;
+    }
+    if (streamk == 2) {  // cluster pairs: CTA 2t + r computes half r of tile t's K blocks
+      if (pos != (int64_t)blockIdx.x) return false;
+      t = (int)(blockIdx.x >> 1);
+      kb = crank ? nk / 2 : 0;
+      ke = crank ? nk : nk / 2;
+      ++pos;
       return true;
     }
     if (pos >= range_e) return false;
@@ -182,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     pos += ke - kb;
     return true;
   };
-  const int64_t pos0 = streamk ? range_b : blockIdx.x;
+  const int64_t pos0 = streamk == 1 ? range_b : blockIdx.x;
   int issued = 0;
 
   if (warp >= kComputeWarps) {
@@ -231,6 +246,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     bool ok = true;
     int t, kb, ke;
     int nparts = 0;              // stream-K segments this CTA finished (phases of the two barriers)
+    bool xwaited = false;        // cluster pairs, odd CTA: waited for the even CTA's arrivals
     __shared__ int seg_last;     // stream-K: 1 if this segment is its tile's last to finish
     for (int64_t pos = pos0; ok && seg(pos, t, kb, ke);) {
       int m0, n0;
@@ -293,7 +309,48 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&empty[s]);
       }
       if (!ok) break;
-      if (kb != 0 || ke != nk) {
+      if (streamk == 2) {
+        // cluster pair: the odd CTA's sums (second half of K) move into the
+        // first 64 KB of the even CTA's stage ring - idle once the even CTA's
+        // own K loop is done - thread-major (float4 v of thread tid at
+        // 256 v + tid), and the even CTA adds them to its own, always in that
+        // order, then updates C.  Both waits are bounded.
+        // Neither exchange wait gives up early on this CTA's abort flag: a CTA
+        // leaves only after the other's accesses to its shared memory landed
+        // (or the bound ran out).
+        float4* xbuf = reinterpret_cast<float4*>(smem);
+        int never = 0;
+        if (crank == 0) {
+          mbar_arrive_cluster(mapa_shared(smem_u32(xfree), 1));  // release: this CTA is done reading its ring
+          if (!__all_sync(0xffffffffu, mbar_wait_cluster_bounded(xready, 0, &never, kWaitLimitNs))) {
+            if (lane == 0) fail();
+            break;
+          }
+#pragma unroll
+          for (int v = 0; v < 16; ++v) {
+            const float4 x = xbuf[256 * v + threadIdx.x];
+            float* a = &acc[v / 2][4 * (v % 2)];
+            a[0] += x.x;
+            a[1] += x.y;
+            a[2] += x.z;
+            a[3] += x.w;
+          }
+        } else {
+          xwaited = true;
+          if (!__all_sync(0xffffffffu, mbar_wait_cluster_bounded(xfree, 0, &never, kWaitLimitNs))) {
+            if (lane == 0) fail();
+            break;
+          }
+          const uint32_t base = mapa_shared(smem_u32(xbuf), 0);
+#pragma unroll
+          for (int v = 0; v < 16; ++v)
+            st_cluster_v4(base + 16u * (uint32_t)(256 * v + threadIdx.x),
+                          make_float4(acc[v / 2][4 * (v % 2)], acc[v / 2][4 * (v % 2) + 1],
+                                      acc[v / 2][4 * (v % 2) + 2], acc[v / 2][4 * (v % 2) + 3]));
+          mbar_arrive_cluster(mapa_shared(smem_u32(xready), 0));  // release: the sums are in
+          continue;  // the even CTA adds both halves into C
+        }
+      } else if (kb != 0 || ke != nk) {
         // stream-K segment of tile t: segments are numbered in K order by
         // the CTA that holds their first K block (the largest c with
         // range_b(c) <= x is ((x + 1) G - 1) / T)
@@ -417,6 +474,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
+    // cluster pairs, odd CTA that stopped before the exchange: the even CTA
+    // may still signal this CTA's barrier; leave only after its arrivals
+    // landed (or the bound ran out)
+    if (streamk == 2 && crank == 1 && !xwaited) {
+      int never = 0;
+      (void)mbar_wait_cluster_bounded(xfree, 0, &never, kWaitLimitNs);
+    }
   }
 
 }
@@ -441,8 +505,25 @@ gbblas_status launch_cfg(DeviceCtx* c, const CUtensorMap& ma, const CUtensorMap&
                          int streamk, int max_seg, float* slots, int* tile_cnt) {
   set_attributes(c);
   const int tiles_m = (int)((M + kBM - 1) / kBM), tiles_n = (int)((N + kBN - 1) / kBN);
-  sgemm_tma_kernel<AK, BK><<<(unsigned)grid, kThreads, kSmem, stream>>>(
-      ma, mb, (int)M, (int)N, (int)K, C, rsc, csc, tiles_m, tiles_n, streamk, max_seg, slots, tile_cnt, err);
+  if (streamk == 2) {  // clusters of two CTAs (one tile per cluster)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kSmem;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, sgemm_tma_kernel<AK, BK>, ma, mb, (int)M, (int)N, (int)K, C, rsc, csc,
+                                   tiles_m, tiles_n, streamk, max_seg, slots, tile_cnt, err));
+  } else {
+    sgemm_tma_kernel<AK, BK><<<(unsigned)grid, kThreads, kSmem, stream>>>(
+        ma, mb, (int)M, (int)N, (int)K, C, rsc, csc, tiles_m, tiles_n, streamk, max_seg, slots, tile_cnt, err);
+  }
   return check_launch("sgemm_tma_kernel");
 }
 
@@ -483,25 +564,37 @@ gbblas_status launch_sgemm_tma(DeviceCtx* c, int64_t M, int64_t N, int64_t K, co
   const int64_t nk = (K + kBK - 1) / kBK;
   int64_t grid = c->num_sms;
   if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+  // cluster pairs need two CTAs per tile at once and two K blocks per tile;
+  // otherwise stream-K
+  if (streamk == 2 && (nk < 2 || 2 * tiles > grid)) streamk = 1;
+  if (streamk == 2) grid = 2 * tiles;
   if (!streamk) grid = std::min<int64_t>(grid, tiles);
   grid = std::min<int64_t>(grid, tiles * nk);  // stream-K: every CTA gets at least one K block
   // stream-K: a tile meets at most (nk - 1) / L + 2 CTA ranges, L the shortest range
   const int64_t shortest = tiles * nk / grid;
-  const int max_seg = streamk ? (int)((nk - 1) / shortest + 2) : 0;
-  const size_t slot_bytes = streamk ? sizeof(float) * (size_t)kBM * kBN * (size_t)(tiles * max_seg) : 0;
-  const size_t cnt_bytes = streamk ? sizeof(int) * (size_t)tiles : 0;
+  const int max_seg = streamk == 1 ? (int)((nk - 1) / shortest + 2) : 0;
+  const size_t slot_bytes = streamk == 1 ? sizeof(float) * (size_t)kBM * kBN * (size_t)(tiles * max_seg) : 0;
+  const size_t cnt_bytes = streamk == 1 ? sizeof(int) * (size_t)tiles : 0;
   void* s = nullptr;
   GB_TRY(get_scratch(c, stream, kScratchZeroBytes + slot_bytes + cnt_bytes, &s));
   int* err = reinterpret_cast<int*>(static_cast<char*>(s) + kErrWordOffset);
-  float* slots = streamk ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
-  int* tile_cnt = streamk ? reinterpret_cast<int*>(static_cast<char*>(s) + kScratchZeroBytes + slot_bytes) : nullptr;
+  float* slots = streamk == 1 ? reinterpret_cast<float*>(static_cast<char*>(s) + kScratchZeroBytes) : nullptr;
+  int* tile_cnt =
+      streamk == 1 ? reinterpret_cast<int*>(static_cast<char*>(s) + kScratchZeroBytes + slot_bytes) : nullptr;
   // the per-tile counts start at zero (the scratch is shared with other kernels on this stream)
-  if (streamk) GB_CUDA_TRY(cudaMemsetAsync(tile_cnt, 0, cnt_bytes, stream));
-  const int g = (int)grid, sk = streamk ? 1 : 0;
+  if (streamk == 1) GB_CUDA_TRY(cudaMemsetAsync(tile_cnt, 0, cnt_bytes, stream));
+  const int g = (int)grid, sk = streamk;
   if (ak && bk) return launch_cfg<true, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
   if (ak) return launch_cfg<true, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
   if (bk) return launch_cfg<false, true>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
   return launch_cfg<false, false>(c, ma, mb, M, N, K, C, rsc, csc, err, stream, g, sk, max_seg, slots, tile_cnt);
+}
+
+bool sgemm_tma_pairs_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN);
+  const int64_t nk = (K + kBK - 1) / kBK;
+  // two CTAs per tile fill at least half the SMs and fit in one wave
+  return nk >= 8 && 2 * tiles <= c->num_sms && 4 * tiles >= c->num_sms;
 }
 
 bool sgemm_tma_streamk_useful(DeviceCtx* c, int64_t M, int64_t N, int64_t K) {

@@ -371,7 +371,7 @@ TcLaunchOpts tuned_tc_opts(DeviceCtx* c, int mode, int64_t M, int64_t N, int64_t
 }
 
 int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t stream) {
-  if (const char* e = std::getenv("GBBLAS_FMA_TILE"); e && e[0] >= '0' && e[0] <= '3') return e[0] - '0';
+  if (const char* e = std::getenv("GBBLAS_FMA_TILE"); e && e[0] >= '0' && e[0] <= '4') return e[0] - '0';
   Tuner& t = Tuner::get();
   const int bm = log2_bucket(M), bn = log2_bucket(N), bk = log2_bucket(K);
   const std::string key = "gemm_fma_tile|" + device_tag(c) + "|m" + std::to_string(bm) + "|n" + std::to_string(bn) +
@@ -385,12 +385,16 @@ int tuned_fma_tile(DeviceCtx* c, int64_t M, int64_t N, int64_t K, cudaStream_t s
   if (!b.ok()) return -1;
   const gbblas_gemm_desc d = b.desc();
   // 0 = 64 x 64, 1 = 128 x 128 (register-staged), 2 = TMA-fed 128 x 128,
-  // 3 = TMA-fed stream-K, offered where whole tiles fill the SMs badly (the
-  // TMA kernels' eligibility is the caller's operands': an ineligible call falls back)
-  const int ntile = sgemm_tma_streamk_useful(c, m, n, k) ? 4 : 3;
+  // 3 = TMA-fed stream-K, offered where whole tiles fill the SMs badly, 4 =
+  // TMA-fed cluster pairs, offered where two CTAs per tile fill the SMs in
+  // one wave (the TMA kernels' eligibility is the caller's operands': an
+  // ineligible call falls back)
+  std::vector<int> tiles{0, 1, 2};
+  if (sgemm_tma_streamk_useful(c, m, n, k)) tiles.push_back(3);
+  if (sgemm_tma_pairs_useful(c, m, n, k)) tiles.push_back(4);
   int best = -1;
   float best_ms = 1e30f;
-  for (int tile = 0; tile < ntile; ++tile) {
+  for (int tile : tiles) {
     const float ms = b.time([&](cudaStream_t s) {
       return launch_gemm_fma<float>(c, d.M, d.N, d.K, d.A, d.rsa, d.csa, d.B, d.rsb, d.csb, d.C, d.rsc, d.csc, s, 0,
                                     tile);

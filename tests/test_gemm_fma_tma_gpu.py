@@ -160,3 +160,37 @@ def test_split_k_within_bound(cuda, monkeypatch, shape, la, lb, lc):
     exact = A.astype(np.float64) @ B.astype(np.float64) + C0
     scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
     assert np.all(np.abs(got.astype(np.float64) - exact) <= 2 * (K + 4) * EPS32 * scale)
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024, 1024), (1000, 1000, 1000), (896, 1152, 520), (1100, 900, 4096),
+                                   (1024, 1024, 32), (2048, 2048, 512), (129, 257, 65)])
+@pytest.mark.parametrize("la,lb,lc", [(1, 1, 1), (0, 1, 1), (1, 0, 0), (0, 0, 1)])
+def test_cluster_pairs_within_bound(cuda, monkeypatch, shape, la, lb, lc):
+    """GBBLAS_FMA_TILE=4: clusters of two CTAs per tile, each with half of
+    the tile's K blocks; the odd CTA's sums move into the even CTA's shared
+    memory, which adds them to its own in that order and updates C.  Shapes
+    whose two CTAs per tile fit the SMs at once take that form; a single K
+    block (K = 32) or more tiles (2048^2) fall back to stream-K.  Within the
+    unsplit kernels' bound, and the same bits on every run."""
+    M, N, K = shape
+    rng = np.random.default_rng(3 * M + N + K + la + 2 * lb + 4 * lc)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    got = run(cuda, A, B, C0, la, lb, lc, 4, monkeypatch)
+    np.testing.assert_array_equal(run(cuda, A, B, C0, la, lb, lc, 4, monkeypatch), got)
+    exact = A.astype(np.float64) @ B.astype(np.float64) + C0
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + np.abs(C0)
+    assert np.all(np.abs(got.astype(np.float64) - exact) <= 2 * (K + 4) * EPS32 * scale)
+
+
+def test_cluster_pairs_integer_exact(cuda, monkeypatch):
+    """Small integers: every partial sum is exact, so the two halves' sum
+    equals the unsplit kernel's result bit for bit."""
+    rng = np.random.default_rng(77)
+    M = N = K = 1024
+    A = rng.integers(-8, 9, (M, K)).astype(np.float32)
+    B = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    C0 = rng.integers(-8, 9, (M, N)).astype(np.float32)
+    np.testing.assert_array_equal(run(cuda, A, B, C0, 1, 1, 1, 4, monkeypatch),
+                                  run(cuda, A, B, C0, 1, 1, 1, 2, monkeypatch))
