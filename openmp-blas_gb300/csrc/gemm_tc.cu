@@ -713,6 +713,85 @@ __global__ void __launch_bounds__(256, 4) f16_col_scale_kernel(ScaleSide side_a,
   }
 }
 
+// Split-BF16 preparation of operands whose K is contiguous (row-major A,
+// column-major B; 16-byte aligned rows, K a multiple of 4): a warp per
+// arena row at a time, each lane 4 consecutive K per 128-bit load (four loads in
+// flight), its P pieces written as 8-byte stores - the same pieces as
+// prep_group_kernel, without the shared-memory tile or its barriers.
+// Padding rows and the K padding get zeros.
+struct RowSplitSide {
+  const SplitJob* jobs;
+  int rows;  // arena rows prepared here (0: this operand takes the tile kernel)
+  __nv_bfloat16* out;
+  int64_t piece_stride;
+};
+
+// A CTA covers 32 consecutive arena rows (each warp 4): they lie in one job,
+// since every job's rows are padded to a multiple of 128, so thread 0
+// finds it once for all of them.
+constexpr int kSplitRowsPerCta = 32;
+
+template <int P>
+__global__ void __launch_bounds__(256) split_rows_kernel(RowSplitSide side_a, RowSplitSide side_b, int njobs,
+                                                         int64_t pitch) {
+  __shared__ int sjob;
+  const int a_ctas = side_a.rows / kSplitRowsPerCta;
+  const bool on_b = (int)blockIdx.x >= a_ctas;
+  const RowSplitSide& sd = on_b ? side_b : side_a;
+  const int64_t R0 = (int64_t)((int)blockIdx.x - (on_b ? a_ctas : 0)) * kSplitRowsPerCta;  // first arena row
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;  // job: the last whose first arena row is <= R0
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sd.jobs[mid].dst_row <= R0)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    sjob = lo;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const SplitJob& j = sd.jobs[sjob];
+  for (int rr = 0; rr < kSplitRowsPerCta / 8; ++rr) {
+  const int64_t R = R0 + (threadIdx.x >> 5) * (kSplitRowsPerCta / 8) + rr;  // arena row
+  const int64_t local = R - j.dst_row;
+  const int64_t kp = (int64_t)j.tiles_k * PrepTile<P>::TK;  // the job's padded K
+  const int64_t K = local < j.rows ? j.K : 0;                // padding rows: all zeros
+  const float* __restrict__ src = j.src + (local < j.rows ? local : 0) * j.rs;
+  __nv_bfloat16* __restrict__ dst = sd.out + R * pitch;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t k0 = 4 * lane; k0 < kp; k0 += 4 * 128) {
+    float4 x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t k = k0 + 128 * u;
+      x[u] = k < K ? dev::ld_stream(reinterpret_cast<const float4*>(src + k)) : zero4;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t k = k0 + 128 * u;
+      if (k >= kp) break;
+      float4 v = x[u];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y);
+        const __nv_bfloat162 h23 = __floats2bfloat162_rn(v.z, v.w);
+        uint2 wv;
+        wv.x = *reinterpret_cast<const uint32_t*>(&h01);
+        wv.y = *reinterpret_cast<const uint32_t*>(&h23);
+        *reinterpret_cast<uint2*>(dst + p * sd.piece_stride + k) = wv;
+        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+        v.x -= f01.x;  // exact in FP32
+        v.y -= f01.y;
+        v.z -= f23.x;
+        v.w -= f23.y;
+      }
+    }
+  }
+  }
+}
+
 // Split-FP16 preparation in one pass for operands whose K is contiguous
 // (row-major A, column-major B): one CTA per arena row reads the row once
 // into registers (kRowPrepNV float4 per thread), finds its largest and its
@@ -1599,6 +1678,7 @@ struct TcGroupPlan {
   bool guard = false;  // FP16 split with the AUTO guard (F16Guard, f16_guard_fixup_kernel)
   bool row_prep_a = false, row_prep_b = false;  // FP16 split: operand prepared by f16_row_prep_kernel
   bool col_scale_a = false, col_scale_b = false;  // FP16 split: exponents by f16_col_scale_kernel
+  bool row_split_a = false, row_split_b = false;  // BF16 split: operand prepared by split_rows_kernel
   int a_col_ctas = 0, b_col_ctas = 0, col_kblk = 128;
   size_t off_gmin = 0, off_gflag = 0, off_glist = 0;  // guard arrays: A rows then B rows each
   size_t off_init_end = 0;  // the launch clears [kTileCounterOffset, off_init_end)
@@ -1716,6 +1796,15 @@ gbblas_status plan_group(int mode, const gbblas_gemm_desc* d, int64_t count, TcG
     pl.b_rows += Np;
   }
   pl.nprob = (int)pl.probs.size();
+  if (pl.mode == 2 || pl.mode == 3) {
+    // the BF16 split's pieces straight from registers where every job of an
+    // operand has K contiguous, 16-byte aligned rows and K a multiple of 4
+    auto split_ok = [](const SplitJob& j) {
+      return j.cs == 1 && (j.rs & 3) == 0 && (reinterpret_cast<uintptr_t>(j.src) & 15) == 0 && (j.K & 3) == 0;
+    };
+    pl.row_split_a = std::all_of(pl.ajobs.begin(), pl.ajobs.end(), split_ok);
+    pl.row_split_b = std::all_of(pl.bjobs.begin(), pl.bjobs.end(), split_ok);
+  }
   if (pl.f16()) {
     // one-pass preparation where every job of an operand has K contiguous,
     // 16-byte aligned rows, K a multiple of 4 within the kernel's reach
@@ -1921,8 +2010,21 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
   }
   // tiles of the operands the tile kernels prepare (the FP16 split's
   // one-pass operands are done by f16_row_prep_kernel instead)
-  const int a_tiles = pl.row_prep_a ? 0 : pl.a_tiles, b_tiles = pl.row_prep_b ? 0 : pl.b_tiles;
+  const int a_tiles = (pl.row_prep_a || pl.row_split_a) ? 0 : pl.a_tiles,
+            b_tiles = (pl.row_prep_b || pl.row_split_b) ? 0 : pl.b_tiles;
   const int prep_ctas = a_tiles + b_tiles;
+  if constexpr (MODE == 2 || MODE == 3) {
+    if (pl.row_split_a || pl.row_split_b) {
+      const RowSplitSide ra{djobs, pl.row_split_a ? (int)pl.a_rows : 0,
+                            reinterpret_cast<__nv_bfloat16*>(arena_a(pl)), (int64_t)(pl.a_rows * pl.pitch)};
+      const RowSplitSide rb{djobs + pl.njobs, pl.row_split_b ? (int)pl.b_rows : 0,
+                            reinterpret_cast<__nv_bfloat16*>(arena_b(pl)), (int64_t)(pl.b_rows * pl.pitch)};
+      // arena rows come in multiples of 128 per job: whole CTAs of 32 rows
+      const int64_t ctas = ((int64_t)ra.rows + rb.rows) / kSplitRowsPerCta;
+      split_rows_kernel<MODE><<<(unsigned)ctas, 256, 0, stream>>>(ra, rb, pl.njobs, pl.pitch);
+      GB_TRY(check_launch("split_rows_kernel"));
+    }
+  }
   if constexpr (MODE == kModeF16) {
     if (pl.row_prep_a || pl.row_prep_b) {
       const RowPrepSide ra{djobs, pl.row_prep_a ? (int)pl.a_rows : 0, reinterpret_cast<__half*>(arena_a(pl)),

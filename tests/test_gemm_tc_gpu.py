@@ -403,3 +403,22 @@ def test_column_scale_matches_tile_scale(cuda, monkeypatch, shape, accuracy):
         tol[5, :] = np.inf  # out of the plain split's span (the guard's rows)
         tol[:, 7] = np.inf
     assert np.all(np.abs(col - exact) <= tol)
+
+
+@pytest.mark.parametrize("mode", [BF16X3, BF16X6])
+@pytest.mark.parametrize("shape", [(192, 320, 1024), (130, 260, 2052), (200, 136, 100), (64, 96, 8192), (1, 5, 4)])
+def test_row_split_matches_tile_preparation(cuda, shape, mode):
+    """The BF16 split writes the pieces of an operand whose K is contiguous
+    (16-byte aligned rows, K a multiple of 4) with one warp per row; the
+    same values with a row stride of K + 1 go through the tile kernel.
+    Same pieces, so C is the same bit for bit, and within the split's bound."""
+    M, N, K = shape
+    rng = np.random.default_rng(M + 5 * N + K + mode)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    rows = _sgemm_strided(cuda, A, B, K, K, mode)
+    tiles = _sgemm_strided(cuda, A, B, K + 1, K + 1, mode)
+    np.testing.assert_array_equal(rows, tiles)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    tol = split_tol(np.abs(A).astype(np.float64), np.abs(B).astype(np.float64), K, mode)
+    assert np.all(np.abs(rows - exact) <= tol)
