@@ -32,7 +32,14 @@
 // count per tile) adds the slots in K order and then that sum into C - a
 // fixed order for a given grid, so the bits repeat run to run, within the
 // same bound as the unsplit kernels but not their bits.  No second kernel
-// and no waiting on other CTAs.  Roofline: the FMA pipes, 2*M*N*K flops.
+// and no waiting on other CTAs.  Cluster pairs (for 57-76 tiles: two CTAs
+// per tile fill the SMs in one wave): CTA 2t + r of a two-CTA cluster
+// computes half r of tile t's K blocks; the even CTA signals (remote
+// mbarrier arrive) that its stage ring is free, the odd CTA writes its sums
+// into it through distributed shared memory and signals back, the even CTA
+// adds them to its own (first half + second half) and updates C.  Every
+// wait is bounded, and neither CTA leaves while the other may still touch
+// its shared memory.  Roofline: the FMA pipes, 2*M*N*K flops.
 #include <cuda.h>
 
 #include <mutex>

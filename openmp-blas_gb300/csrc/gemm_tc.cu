@@ -8,13 +8,18 @@
 //      N x K) into one arena per operand kind: all problems' rows stacked,
 //      one common K pitch.  One pair of TMA tensor maps then covers every
 //      problem of the group.
-//      prep_group_kernel, split-BF16: every FP32 element a becomes P BF16 pieces
+//      split-BF16: every FP32 element a becomes P BF16 pieces
 //        p0 = bf16_rn(a), p1 = bf16_rn(a - p0), p2 = bf16_rn(a - p0 - p1),
-//        piece planes one after another.
-//      prep_group_kernel, split-FP16: every row of A / column of B is scaled
-//        by 2^(15 - e) (e from f16_scale_kernel: the frexp exponent of its
-//        largest magnitude) and split h = fp16_rn(v), l = fp16_rn(v - h);
-//        the epilogue multiplies by 2^(e_i + f_j - 30) again.
+//        piece planes one after another (split_rows_kernel, a warp per row,
+//        where K is contiguous; prep_group_kernel's tiles otherwise).
+//      split-FP16: every row of A / column of B is scaled by 2^(15 - e), e
+//        the frexp exponent of its largest magnitude, and split
+//        h = fp16_rn(v), l = fp16_rn(v - h); the epilogue multiplies by
+//        2^(e_i + f_j - 30) again.  K contiguous: f16_row_prep_kernel, a CTA
+//        per row, does both in one read; rows contiguous: the exponents from
+//        f16_col_scale_kernel's column reduction, the pieces from
+//        prep_group_kernel; other layouts: f16_scale_kernel and
+//        prep_group_kernel on tiles.  All routes give the same bits.
 //      prep_group_kernel, FP8: every 128-element K-block of a row becomes
 //        128 E4M3 values and one power-of-two scale, kept as its UE8M0
 //        exponent byte in 512-byte atoms (128 rows of one K-block) beside
@@ -55,7 +60,9 @@
 //   warps 2-9   epilogue: tcgen05.ld each finished chunk (warp w reads TMEM
 //   (FP8: 2-5)  lanes 32*(w%4)..+31 = tile rows; with 8 warps, warps 2-5
 //               take the first 64 columns, 6-9 the other 64) into FP32
-//               registers, release the buffer, add the registers into C.
+//               registers, release the buffer, add the registers into C
+//               (single CTAs: 32 x 32 blocks staged in shared memory and
+//               added by TMA reduce-add stores where C's layout allows).
 // Every mbarrier wait is bounded (2 s by %globaltimer); a wait that gives up
 // records GBBLAS_STATUS_TIMEOUT in the stream's error word, the CTA drains
 // its in-flight copies (bounded again), lets its MMAs finish, frees TMEM and
