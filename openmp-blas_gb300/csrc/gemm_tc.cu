@@ -733,19 +733,21 @@ struct RowSplitSide {
   int64_t piece_stride;
 };
 
-// A CTA covers 32 consecutive arena rows (each warp 4): they lie in one job,
-// since every job's rows are padded to a multiple of 128, so thread 0
-// finds it once for all of them.
-constexpr int kSplitRowsPerCta = 32;
+// A CTA covers `rows_per_cta` consecutive arena rows (8 or 32: a warp
+// each, or four each where the launch still has at least four CTAs per SM;
+// many small jobs take 32, one large matrix 8).  They lie in one job, since
+// every job's rows are padded to a multiple of 128, so thread 0 finds it
+// once for all of them.
+constexpr int kSplitRowsPerCtaMax = 32;
 
 template <int P>
 __global__ void __launch_bounds__(256) split_rows_kernel(RowSplitSide side_a, RowSplitSide side_b, int njobs,
-                                                         int64_t pitch) {
+                                                         int64_t pitch, int rows_per_cta) {
   __shared__ int sjob;
-  const int a_ctas = side_a.rows / kSplitRowsPerCta;
+  const int a_ctas = side_a.rows / rows_per_cta;
   const bool on_b = (int)blockIdx.x >= a_ctas;
   const RowSplitSide& sd = on_b ? side_b : side_a;
-  const int64_t R0 = (int64_t)((int)blockIdx.x - (on_b ? a_ctas : 0)) * kSplitRowsPerCta;  // first arena row
+  const int64_t R0 = (int64_t)((int)blockIdx.x - (on_b ? a_ctas : 0)) * rows_per_cta;  // first arena row
   if (threadIdx.x == 0) {
     int lo = 0, hi = njobs - 1;  // job: the last whose first arena row is <= R0
     while (lo < hi) {
@@ -760,8 +762,9 @@ __global__ void __launch_bounds__(256) split_rows_kernel(RowSplitSide side_a, Ro
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const SplitJob& j = sd.jobs[sjob];
-  for (int rr = 0; rr < kSplitRowsPerCta / 8; ++rr) {
-  const int64_t R = R0 + (threadIdx.x >> 5) * (kSplitRowsPerCta / 8) + rr;  // arena row
+  const int per_warp = rows_per_cta / 8;
+  for (int rr = 0; rr < per_warp; ++rr) {
+  const int64_t R = R0 + (threadIdx.x >> 5) * per_warp + rr;  // arena row
   const int64_t local = R - j.dst_row;
   const int64_t kp = (int64_t)j.tiles_k * PrepTile<P>::TK;  // the job's padded K
   const int64_t K = local < j.rows ? j.K : 0;                // padding rows: all zeros
@@ -2026,9 +2029,10 @@ gbblas_status launch_bound(DeviceCtx* c, const TcGroupPlan& pl, cudaStream_t str
                             reinterpret_cast<__nv_bfloat16*>(arena_a(pl)), (int64_t)(pl.a_rows * pl.pitch)};
       const RowSplitSide rb{djobs + pl.njobs, pl.row_split_b ? (int)pl.b_rows : 0,
                             reinterpret_cast<__nv_bfloat16*>(arena_b(pl)), (int64_t)(pl.b_rows * pl.pitch)};
-      // arena rows come in multiples of 128 per job: whole CTAs of 32 rows
-      const int64_t ctas = ((int64_t)ra.rows + rb.rows) / kSplitRowsPerCta;
-      split_rows_kernel<MODE><<<(unsigned)ctas, 256, 0, stream>>>(ra, rb, pl.njobs, pl.pitch);
+      // arena rows come in multiples of 128 per job: whole CTAs of 8 or 32 rows
+      const int64_t rows = (int64_t)ra.rows + rb.rows;
+      const int rpc = rows / kSplitRowsPerCtaMax >= 4 * (int64_t)c->num_sms ? kSplitRowsPerCtaMax : 8;
+      split_rows_kernel<MODE><<<(unsigned)(rows / rpc), 256, 0, stream>>>(ra, rb, pl.njobs, pl.pitch, rpc);
       GB_TRY(check_launch("split_rows_kernel"));
     }
   }
