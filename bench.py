@@ -1085,7 +1085,8 @@ def serving_report(args):
     """The serving configuration: Poisson arrivals at each rate of --rates of
     60 % mtm, 30 % mtv, 10 % dot; GEMM and GEMV dims log-uniform in
     [64, 4096], dot lengths log-uniform in [1k, 64M]; 80 % float32 at FP32
-    accuracy (AUTO = six-product split-BF16), 20 % float64; operands device
+    accuracy (AUTO: the guarded split-FP16 GEMM, one FMA kernel below 2^26
+    multiply-adds), 20 % float64; operands device
     resident (inputs are windows of a U[-1,1) pool, outputs from the server's
     pool), 64 GiB admission budget.  Per rate: achieved throughput, p50/p99
     latency (overall and per class) against the same requests run alone
