@@ -68,6 +68,8 @@ def test_status_strings():
     ("gbblas_sew_host", (1, 8, None, 16, 16)),
     ("gbblas_selftest_bounded_wait", (0, None)),
     ("gbblas_selftest_bounded_wait", (2000001, None)),
+    ("gbblas_server_request_times", (None, 0, 16)),
+    ("gbblas_server_request_times", (16, 0, None)),
 ])
 def test_invalid_arguments_rejected_without_device(fn, args):
     assert gbblas.status_of(fn, *args) == 1  # GBBLAS_STATUS_INVALID_VALUE
